@@ -1,0 +1,313 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300-native cuJSON parse path.
+
+One step = one full parse (UTF-8 validation, tokenization, structural
+compaction, nesting/pair recognition) of the 1 GiB standard-JSON workload
+(seeded stand-in for the reference's ~1 GB datasets: depth <= 20, 1% of strings
+64-128 KiB of backslash runs).
+
+  value        device-resident parse GB/s (input already in HBM; CUDA events on
+               the launching stream around K steps; whole job over all ranks)
+  e2e          the same metric through the C ABI with host buffers: pinned H2D of
+               the input, parse, D2H of the verdict and the result arrays
+  roofline     the dominant (scan) kernel: algorithmic bytes N + 8*S per launch
+               over its CUDA-event time, against the measured HBM copy bandwidth
+  cpu_baseline the CPU restatement of the reference's algorithm (oracle/), one
+               core, on a bounded sample of the same workload
+
+``--impl reference`` times the reference's algorithm on the host cores (the
+oracle port; the reference itself is CUDA-only and does not build on the GPU
+box), with every host thread running an independent instance.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "parse GB/s (1 GiB standard JSON, device-resident)"
+UNIT = "GB/s"
+WORKLOAD = ("standard JSON, 1 GiB (1073741824 B), seed 0xC0DE0002, top-level array of objects "
+            "(10-30 keys), nesting <= 20, 1% of strings 64-128 KiB of backslash runs")
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--size", type=int, default=1 << 30, help="input bytes (default 1 GiB)")
+    ap.add_argument("--cpu-sample", type=int, default=256 << 20, help="CPU-baseline sample bytes")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def workload(size: int):
+    import cujson_gb300 as cj
+    seed = cj.CONFIG_SEED_BASE + 2
+    return cj.synth_document(seed, size, max_depth=20, huge_string_frac=0.01,
+                             huge_string_min=64 << 10, huge_string_max=128 << 10)
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_byte():
+    p = ROOT / "profiles" / "traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            return None
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.rows = []
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(device)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def dist_setup(n_gpus: int):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def allmax(pg, x: float) -> float:
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline_sample(sample_bytes: int):
+    """Oracle (CPU restatement of the reference algorithm), one thread, on a
+    bounded sample of the same generator; returns (GB/s, description)."""
+    from oracle import cj_oracle
+    import cujson_gb300 as cj
+    d = cj.synth_document(cj.CONFIG_SEED_BASE + 2, sample_bytes, max_depth=20,
+                          huge_string_frac=0.01, huge_string_min=64 << 10,
+                          huge_string_max=128 << 10)
+    cj_oracle.parse(d[: 1 << 20])        # load + warm
+    reps, t_total = 0, 0.0
+    while t_total < 10.0 and reps < 40:
+        t0 = time.perf_counter()
+        r = cj_oracle.parse(d)
+        t_total += time.perf_counter() - t0
+        reps += 1
+    assert r.flags == 0
+    gbs = sample_bytes * reps / t_total / 1e9
+    return gbs, f"{sample_bytes} B document from the same generator, parsed {reps}x ({t_total:.1f} s)"
+
+
+def run_reference(args, world, rank):
+    """Reference arm: the reference's algorithm (oracle port) on all host cores."""
+    if rank != 0:
+        return
+    from oracle import cj_oracle
+    import cujson_gb300 as cj
+    from concurrent.futures import ThreadPoolExecutor
+    cores = os.cpu_count() or 1
+    sample = 64 << 20
+    d = cj.synth_document(cj.CONFIG_SEED_BASE + 2, sample, max_depth=20, huge_string_frac=0.01,
+                          huge_string_min=64 << 10, huge_string_max=128 << 10)
+    ex = ThreadPoolExecutor(max_workers=cores)
+
+    def step():
+        list(ex.map(lambda _: cj_oracle.parse(d).flags, range(cores)))
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    value = sample * cores * args.steps / dt / 1e9
+    desc = (f"{cores} independent instances per step, each parsing a {sample} B document of the "
+            f"same generator")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_bytes": sample},
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": desc},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local, pg):
+    import cujson_gb300 as cj
+    peak, peak_kind = measured_peaks()
+    data = workload(args.size)
+    N = data.size
+    ctx = cj.Context(local)
+    ctx.reserve(N, 1)
+    ctx.stage_standard(data)
+    ctx.run()
+    info = ctx.info()
+    if info.status != 0:
+        raise SystemExit(f"parse failed: {cj.status_string(info.status)}")
+    S, K = int(info.n_structural), int(info.n_brackets)
+
+    for _ in range(args.warmup):
+        ctx.run()
+    ctx.info()
+    clocks = Clocks(local) if rank == 0 else None
+    barrier(pg)
+    launches0 = ctx.launches
+    ctx.timing(True)
+    for _ in range(args.steps):
+        ctx.run()
+    scan_ms, pair_ms, spine_ms, runs = ctx.phase_ms()     # synchronises the stream
+    span_ms = ctx.span_ms()
+    barrier(pg)
+    launches = ctx.launches - launches0
+    ck = clocks.stop() if clocks else None
+    ctx.timing(False)
+    inf2 = ctx.info()
+    assert inf2.status == 0 and inf2.n_structural == S
+
+    span_max = allmax(pg, span_ms)
+    value = N * world * args.steps / (span_max / 1e3) / 1e9
+    B = N + 8 * S
+    scan_avg_s = scan_ms / runs / 1e3
+    achieved = B / scan_avg_s / 1e9
+    tr = traffic_per_byte()
+    traffic = None
+    if tr and "scan_bytes_per_input_byte" in tr:
+        traffic = int(tr["scan_bytes_per_input_byte"] * N)
+
+    # end to end through the C ABI: pinned host input, H2D, parse, D2H of result
+    e2e = None
+    if not args.no_e2e:
+        pin_in = cj.PinnedBuffer(N)
+        pin_in.array[:] = data
+        out_n = 2 * S + 4
+        pin_out = cj.PinnedBuffer(out_n * 4, dtype=np.int32)
+        for _ in range(max(1, args.warmup)):
+            ctx.parse_into(pin_in.array, pin_out.array)
+        barrier(pg)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            ctx.parse_into(pin_in.array, pin_out.array)
+        dt = allmax(pg, time.perf_counter() - t0)
+        barrier(pg)
+        e2e = {"value": round(N * world * args.steps / dt / 1e9, 3), "unit": UNIT,
+               "h2d_bytes_per_step": N, "d2h_bytes_per_step": out_n * 4 + 64,
+               "ms_per_step": round(dt / args.steps * 1e3, 3)}
+        pin_in.close()
+        pin_out.close()
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        v, desc = cpu_baseline_sample(args.cpu_sample)
+        cpu = {"value": round(v, 4), "unit": UNIT, "cores": 1, "kind": "port", "sample": desc}
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(span_max / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "bytes": N, "structurals": S, "brackets": K,
+                   "max_depth": int(inf2.max_depth), "parallelism": f"replicas x{world}",
+                   "l2": "input 1 GiB > 129 MB L2, no flush between steps"},
+        "roofline": {"bound": "hbm", "kernel": "scan_kernel", "achieved": round(achieved, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "peak_kind": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes": B},
+        "phases_ms_per_step": {"scan": round(scan_ms / runs, 4), "pair": round(pair_ms / runs, 4),
+                               "spine": round(spine_ms / runs, 4)},
+        "parse_roofline_frac": round(B / (span_max / args.steps / 1e3) / 1e9 / peak, 4),
+        "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": ck,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    world, rank, local, pg = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

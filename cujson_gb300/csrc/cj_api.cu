@@ -1,0 +1,583 @@
+// cj_api.cu -- host orchestration and the C ABI (include/cujson_gb300.h).
+//
+// Replaces the reference's drivers parse_standard_json
+// (cujson/parse_standard_json.cu:1584-1687) and parse_json_lines
+// (cujson/parse_json_lines.cu:1092-1264).  Differences in shape, not in output:
+//   - one device arena per context, grown to the largest input and reused, in
+//     place of ~8 cudaMalloc/cudaFree per call;
+//   - three kernel launches (scan, pair, spine) on a non-blocking stream, with
+//     no host synchronisation until the verdict and counts are read;
+//   - JSON-Lines chunks are parsed in the same launch (each chunk is a segment
+//     whose string/escape state and depth restart), not one after another;
+//   - errors are returned as a status; the process never exits.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "cj_device.cuh"
+#include "cj_kernels.h"
+#include "cujson_gb300.h"
+
+using namespace cj;
+
+namespace {
+
+thread_local int g_last_status = CJ_OK;
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t cap = 0;   // elements
+};
+
+size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
+
+}  // namespace
+
+struct cj_context {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+
+    DevBuf<uint8_t> in;
+    DevBuf<int32_t> pos, pair;
+    DevBuf<uint2> brk;
+    DevBuf<uint32_t> desc_flag;
+    DevBuf<uint4> desc_agg, desc_incl;
+    DevBuf<Segment> segs;
+    DevBuf<SegmentOut> seg_out;
+    DevBuf<uint32_t> tile_seg;
+    DevBuf<uint32_t> spine;
+    DevBuf<int4> cinfo;
+    DevBuf<unsigned long long> tree;
+    Ctrl* d_ctrl = nullptr;
+    uint64_t tree_off[kTreeLevels + 1] = {};
+    size_t chunk_cap = 0;
+
+    Ctrl* h_ctrl = nullptr;             // pinned mirrors
+    std::vector<Segment> h_segs;
+    std::vector<uint32_t> h_tile_seg;
+    SegmentOut* h_seg_out = nullptr;
+    size_t h_seg_out_cap = 0;
+
+    uint32_t epoch = 0;
+    bool staged = false;
+    bool lines = false;
+    size_t n_bytes = 0;
+    uint32_t n_segs = 0;
+    uint32_t n_tiles = 0;
+    int64_t launches = 0;
+    size_t dev_bytes = 0;
+
+    bool timing = false;
+    std::vector<cudaEvent_t> events;   // 4 per recorded run
+    size_t events_used = 0;
+};
+
+namespace {
+
+#define CJ_CUDA(call)                                                        \
+    do {                                                                     \
+        cudaError_t e_ = (call);                                             \
+        if (e_ != cudaSuccess) {                                             \
+            return (e_ == cudaErrorMemoryAllocation) ? CJ_ERR_OUT_OF_MEMORY  \
+                                                     : CJ_ERR_CUDA;          \
+        }                                                                    \
+    } while (0)
+
+template <typename T>
+cj_status ensure(cj_context* ctx, DevBuf<T>& b, size_t n)
+{
+    if (n <= b.cap && b.p) return CJ_OK;
+    if (b.p) { cudaFree(b.p); ctx->dev_bytes -= b.cap * sizeof(T); b.p = nullptr; b.cap = 0; }
+    size_t want = std::max<size_t>(n + n / 8, 64);
+    CJ_CUDA(cudaMalloc((void**)&b.p, want * sizeof(T)));
+    b.cap = want;
+    ctx->dev_bytes += want * sizeof(T);
+    return CJ_OK;
+}
+
+template <typename T>
+void release(DevBuf<T>& b) { if (b.p) cudaFree(b.p); b.p = nullptr; b.cap = 0; }
+
+// Size every buffer for an input of `bytes` in `segs` segments.  S, the
+// structural count, is at most the byte count, and so is the bracket count.
+cj_status reserve(cj_context* ctx, size_t bytes, size_t segs)
+{
+    size_t padded = round_up(bytes, kTileBytes) + segs * (size_t)kTileBytes;
+    size_t tiles = padded / kTileBytes + 1;
+    size_t s_cap = bytes + 1;
+    size_t chunks = (bytes + kChunk - 1) / kChunk + 1;
+    cj_status st;
+    if ((st = ensure(ctx, ctx->in, padded + 64))) return st;
+    if ((st = ensure(ctx, ctx->pos, s_cap))) return st;
+    if ((st = ensure(ctx, ctx->pair, s_cap))) return st;
+    if ((st = ensure(ctx, ctx->brk, s_cap))) return st;
+    bool new_desc = ctx->desc_flag.cap < tiles;
+    if ((st = ensure(ctx, ctx->desc_flag, tiles))) return st;
+    if (new_desc)
+        CJ_CUDA(cudaMemsetAsync(ctx->desc_flag.p, 0, ctx->desc_flag.cap * sizeof(uint32_t), ctx->stream));
+    if ((st = ensure(ctx, ctx->desc_agg, tiles * 4))) return st;
+    if ((st = ensure(ctx, ctx->desc_incl, tiles))) return st;
+    if ((st = ensure(ctx, ctx->segs, segs))) return st;
+    if ((st = ensure(ctx, ctx->seg_out, segs))) return st;
+    if ((st = ensure(ctx, ctx->tile_seg, tiles))) return st;
+    if ((st = ensure(ctx, ctx->spine, chunks * (size_t)kChunk))) return st;
+    if ((st = ensure(ctx, ctx->cinfo, chunks))) return st;
+    if (chunks > ctx->chunk_cap) {
+        size_t off = 0, n = chunks;
+        ctx->tree_off[0] = 0;
+        for (int l = 1; l <= kTreeLevels; l++) {
+            n = (n + 31) / 32;
+            ctx->tree_off[l] = off;
+            off += n;
+        }
+        bool fresh = ctx->tree.cap < off;
+        if ((st = ensure(ctx, ctx->tree, off))) return st;
+        if (fresh)
+            CJ_CUDA(cudaMemsetAsync(ctx->tree.p, 0, ctx->tree.cap * sizeof(unsigned long long), ctx->stream));
+        ctx->chunk_cap = chunks;
+    }
+    if (!ctx->h_ctrl) CJ_CUDA(cudaMallocHost((void**)&ctx->h_ctrl, sizeof(Ctrl)));
+    if (ctx->h_seg_out_cap < segs) {
+        if (ctx->h_seg_out) cudaFreeHost(ctx->h_seg_out);
+        size_t want = std::max<size_t>(segs, 16);
+        CJ_CUDA(cudaMallocHost((void**)&ctx->h_seg_out, want * sizeof(SegmentOut)));
+        ctx->h_seg_out_cap = want;
+    }
+    return CJ_OK;
+}
+
+// Lay the chunks out on tile boundaries and copy them to the device.
+cj_status stage(cj_context* ctx, const uint8_t* const* chunks, const size_t* sizes, size_t n,
+                bool lines)
+{
+    ctx->staged = false;
+    if (!chunks || !sizes || n == 0) return CJ_ERR_INVALID_ARGUMENT;
+    size_t total = 0;
+    for (size_t i = 0; i < n; i++) {
+        if (!chunks[i] || sizes[i] == 0) return CJ_ERR_INVALID_ARGUMENT;
+        total += sizes[i];
+    }
+    if (total > CJ_MAX_INPUT_BYTES) return CJ_ERR_TOO_LARGE;
+    CJ_CUDA(cudaSetDevice(ctx->device));
+    cj_status st = reserve(ctx, total, n);
+    if (st) return st;
+
+    ctx->h_segs.resize(n);
+    uint64_t dev_off = 0, logical = 0;
+    uint32_t tile = 0;
+    for (size_t i = 0; i < n; i++) {
+        Segment& s = ctx->h_segs[i];
+        s.dev_off = dev_off;
+        s.len = sizes[i];
+        s.logical_off = logical;
+        s.out_base = 0;
+        s.brk_base = 0;
+        s.first_tile = tile;
+        s.n_tiles = (uint32_t)((sizes[i] + kTileBytes - 1) / kTileBytes);
+        s.flags = (i > 0) ? kSegContinue : 0u;
+        s.pad = 0;
+        dev_off += (uint64_t)s.n_tiles * kTileBytes;
+        logical += sizes[i];
+        tile += s.n_tiles;
+    }
+    for (size_t i = 0; i < n; i++)
+        CJ_CUDA(cudaMemcpyAsync(ctx->in.p + ctx->h_segs[i].dev_off, chunks[i], sizes[i],
+                                cudaMemcpyHostToDevice, ctx->stream));
+    CJ_CUDA(cudaMemcpyAsync(ctx->segs.p, ctx->h_segs.data(), n * sizeof(Segment),
+                            cudaMemcpyHostToDevice, ctx->stream));
+    if (n > 1) {
+        ctx->h_tile_seg.resize(tile);
+        for (size_t i = 0; i < n; i++)
+            for (uint32_t t = 0; t < ctx->h_segs[i].n_tiles; t++)
+                ctx->h_tile_seg[ctx->h_segs[i].first_tile + t] = (uint32_t)i;
+        CJ_CUDA(cudaMemcpyAsync(ctx->tile_seg.p, ctx->h_tile_seg.data(), tile * sizeof(uint32_t),
+                                cudaMemcpyHostToDevice, ctx->stream));
+    }
+    // host vectors must outlive the copies
+    CJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->n_bytes = total;
+    ctx->n_segs = (uint32_t)n;
+    ctx->n_tiles = tile;
+    ctx->lines = lines;
+    ctx->staged = true;
+    return CJ_OK;
+}
+
+cj_status run(cj_context* ctx)
+{
+    if (!ctx->staged) return CJ_ERR_NOT_STAGED;
+    CJ_CUDA(cudaSetDevice(ctx->device));
+    ctx->epoch = (ctx->epoch + 1) & 0x3FFFFFFFu;
+    if (ctx->epoch == 0) {
+        // epoch wrapped: stale descriptors could alias, so clear them
+        CJ_CUDA(cudaMemsetAsync(ctx->desc_flag.p, 0, ctx->desc_flag.cap * sizeof(uint32_t), ctx->stream));
+        CJ_CUDA(cudaMemsetAsync(ctx->tree.p, 0, ctx->tree.cap * sizeof(unsigned long long), ctx->stream));
+        ctx->epoch = 1;
+    }
+    CJ_CUDA(cudaMemsetAsync(ctx->d_ctrl, 0, sizeof(Ctrl), ctx->stream));
+
+    cudaEvent_t* ev = nullptr;
+    if (ctx->timing) {
+        if (ctx->events_used + 4 > ctx->events.size()) {
+            for (int i = 0; i < 4; i++) {
+                cudaEvent_t e;
+                CJ_CUDA(cudaEventCreate(&e));
+                ctx->events.push_back(e);
+            }
+        }
+        ev = ctx->events.data() + ctx->events_used;
+        ctx->events_used += 4;
+        CJ_CUDA(cudaEventRecord(ev[0], ctx->stream));
+    }
+
+    ScanParams sp;
+    sp.in = ctx->in.p;
+    sp.segs = ctx->segs.p;
+    sp.tile_seg = (ctx->n_segs > 1) ? ctx->tile_seg.p : nullptr;
+    sp.n_segs = ctx->n_segs;
+    sp.n_tiles = ctx->n_tiles;
+    sp.pos = ctx->pos.p;
+    sp.pair = ctx->pair.p;
+    sp.brk = ctx->brk.p;
+    sp.desc_flag = ctx->desc_flag.p;
+    sp.desc_agg = ctx->desc_agg.p;
+    sp.desc_incl = ctx->desc_incl.p;
+    sp.ctrl = ctx->d_ctrl;
+    sp.seg_out = ctx->seg_out.p;
+    sp.epoch = ctx->epoch;
+    launch_scan(sp, ctx->lines, ctx->stream);
+    if (ev) CJ_CUDA(cudaEventRecord(ev[1], ctx->stream));
+
+    PairParams pp;
+    pp.brk = ctx->brk.p;
+    pp.pair = ctx->pair.p;
+    pp.spine = ctx->spine.p;
+    pp.cinfo = ctx->cinfo.p;
+    pp.tree = ctx->tree.p;
+    for (int l = 0; l <= kTreeLevels; l++) pp.tree_off[l] = ctx->tree_off[l];
+    pp.ctrl = ctx->d_ctrl;
+    pp.epoch = ctx->epoch;
+    pp.chunk_cap = (uint32_t)ctx->chunk_cap;
+    size_t max_chunks = (ctx->n_bytes + kChunk - 1) / kChunk;
+    int grid = (int)std::min<size_t>((max_chunks + 7) / 8 + 1, (size_t)ctx->sm_count * 8);
+    launch_pair(pp, grid, ctx->stream);
+    if (ev) CJ_CUDA(cudaEventRecord(ev[2], ctx->stream));
+    launch_spine(pp, grid, ctx->stream);
+    if (ev) CJ_CUDA(cudaEventRecord(ev[3], ctx->stream));
+    ctx->launches += (ctx->n_tiles ? 1 : 0) + 2;
+    CJ_CUDA(cudaGetLastError());
+    return CJ_OK;
+}
+
+cj_status read_info(cj_context* ctx, cj_parse_info* info)
+{
+    if (!ctx->staged) return CJ_ERR_NOT_STAGED;
+    CJ_CUDA(cudaMemcpyAsync(ctx->h_ctrl, ctx->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, ctx->stream));
+    CJ_CUDA(cudaMemcpyAsync(ctx->h_seg_out, ctx->seg_out.p, ctx->n_segs * sizeof(SegmentOut),
+                            cudaMemcpyDeviceToHost, ctx->stream));
+    CJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    const Ctrl& c = *ctx->h_ctrl;
+    uint32_t flags = c.error_flags;
+    if (c.neg_min_level > 0) flags |= CJ_FLAG_BRACKETS;
+    cj_status verdict = CJ_OK;
+    if (flags & CJ_FLAG_TIMEOUT) verdict = CJ_ERR_TIMEOUT;
+    else if (flags & CJ_FLAG_UTF8) verdict = CJ_ERR_INVALID_UTF8;
+    else if (flags & CJ_FLAG_BRACKETS) verdict = CJ_ERR_INVALID_BRACKETS;
+    if (info) {
+        info->n_structural = c.s_total;
+        info->n_brackets = c.k_total;
+        info->max_depth = c.max_depth;
+        info->status = verdict;
+        info->error_flags = flags;
+        info->n_segments = (int32_t)ctx->n_segs;
+    }
+    return CJ_OK;
+}
+
+// Reference layout into host_out (2*(S+2) entries).
+cj_status copy_result(cj_context* ctx, int64_t S, int32_t* out, size_t cap)
+{
+    if ((size_t)(2 * S + 4) > cap) return CJ_ERR_CAPACITY;
+    out[0] = 0;
+    out[S + 1] = (int32_t)(S + 1);
+    out[2 * S + 2] = 0;
+    out[2 * S + 3] = 0;
+    if (S > 0) {
+        CJ_CUDA(cudaMemcpyAsync(out + 1, ctx->pos.p, (size_t)S * sizeof(int32_t),
+                                cudaMemcpyDeviceToHost, ctx->stream));
+        CJ_CUDA(cudaMemcpyAsync(out + S + 2, ctx->pair.p, (size_t)S * sizeof(int32_t),
+                                cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    CJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    return CJ_OK;
+}
+
+cj_status to_result(cj_context* ctx, const cj_parse_info& info, cj_result* out)
+{
+    int64_t S = info.n_structural;
+    int32_t* buf = nullptr;
+    CJ_CUDA(cudaMallocHost((void**)&buf, (size_t)(2 * S + 4) * sizeof(int32_t)));
+    cj_status st = copy_result(ctx, S, buf, (size_t)(2 * S + 4));
+    if (st) { cudaFreeHost(buf); return st; }
+    out->structural = buf;
+    out->pair_pos = buf + S + 1;
+    out->n_structural = S;
+    out->total = S + 2;
+    out->max_depth = info.max_depth;
+    out->status = CJ_OK;
+    out->n_segments = ctx->n_segs;
+    out->segment_sizes = (int64_t*)malloc(sizeof(int64_t) * ctx->n_segs);
+    uint32_t prev = 0;
+    for (uint32_t i = 0; i < ctx->n_segs; i++) {
+        out->segment_sizes[i] = (int64_t)(ctx->h_seg_out[i].s_end - prev);
+        prev = ctx->h_seg_out[i].s_end;
+    }
+    return CJ_OK;
+}
+
+cj_status finish(cj_status st) { g_last_status = st; return st; }
+
+}  // namespace
+
+extern "C" {
+
+cj_status cj_context_create(int device, cj_context** out)
+{
+    if (!out) return CJ_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return CJ_ERR_NO_DEVICE;
+    if (device < 0) CJ_CUDA(cudaGetDevice(&device));
+    if (device >= n) return CJ_ERR_INVALID_ARGUMENT;
+    CJ_CUDA(cudaSetDevice(device));
+    cj_context* ctx = new cj_context();
+    ctx->device = device;
+    cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc((void**)&ctx->d_ctrl, sizeof(Ctrl)) != cudaSuccess) {
+        cj_context_destroy(ctx);
+        return CJ_ERR_CUDA;
+    }
+    *out = ctx;
+    return CJ_OK;
+}
+
+void cj_context_destroy(cj_context* ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    release(ctx->in); release(ctx->pos); release(ctx->pair); release(ctx->brk);
+    release(ctx->desc_flag); release(ctx->desc_agg); release(ctx->desc_incl);
+    release(ctx->segs); release(ctx->seg_out); release(ctx->tile_seg);
+    release(ctx->spine); release(ctx->cinfo); release(ctx->tree);
+    if (ctx->d_ctrl) cudaFree(ctx->d_ctrl);
+    if (ctx->h_ctrl) cudaFreeHost(ctx->h_ctrl);
+    if (ctx->h_seg_out) cudaFreeHost(ctx->h_seg_out);
+    for (cudaEvent_t e : ctx->events) cudaEventDestroy(e);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+cj_status cj_context_timing(cj_context* ctx, int enable)
+{
+    if (!ctx) return CJ_ERR_INVALID_ARGUMENT;
+    ctx->timing = enable != 0;
+    ctx->events_used = 0;
+    return CJ_OK;
+}
+
+cj_status cj_context_phase_ms(cj_context* ctx, double* scan_ms, double* pair_ms, double* spine_ms,
+                              int64_t* runs)
+{
+    if (!ctx) return CJ_ERR_INVALID_ARGUMENT;
+    CJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    double a = 0, b = 0, c = 0;
+    for (size_t i = 0; i + 4 <= ctx->events_used; i += 4) {
+        float x = 0, y = 0, z = 0;
+        CJ_CUDA(cudaEventElapsedTime(&x, ctx->events[i], ctx->events[i + 1]));
+        CJ_CUDA(cudaEventElapsedTime(&y, ctx->events[i + 1], ctx->events[i + 2]));
+        CJ_CUDA(cudaEventElapsedTime(&z, ctx->events[i + 2], ctx->events[i + 3]));
+        a += x; b += y; c += z;
+    }
+    if (scan_ms) *scan_ms = a;
+    if (pair_ms) *pair_ms = b;
+    if (spine_ms) *spine_ms = c;
+    if (runs) *runs = (int64_t)(ctx->events_used / 4);
+    return CJ_OK;
+}
+
+cj_status cj_context_span_ms(cj_context* ctx, double* ms)
+{
+    if (!ctx || !ms) return CJ_ERR_INVALID_ARGUMENT;
+    *ms = 0;
+    if (ctx->events_used < 4) return CJ_OK;
+    CJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    float x = 0;
+    CJ_CUDA(cudaEventElapsedTime(&x, ctx->events[0], ctx->events[ctx->events_used - 1]));
+    *ms = x;
+    return CJ_OK;
+}
+
+void* cj_host_alloc(size_t bytes)
+{
+    void* p = nullptr;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+    return p;
+}
+
+void cj_host_free(void* p) { if (p) cudaFreeHost(p); }
+
+cj_status cj_context_reserve(cj_context* ctx, size_t max_bytes, size_t max_segments)
+{
+    if (!ctx || max_segments == 0) return CJ_ERR_INVALID_ARGUMENT;
+    if (max_bytes > CJ_MAX_INPUT_BYTES) return CJ_ERR_TOO_LARGE;
+    CJ_CUDA(cudaSetDevice(ctx->device));
+    return reserve(ctx, max_bytes, max_segments);
+}
+
+void* cj_context_stream(cj_context* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+int64_t cj_context_launch_count(cj_context* ctx) { return ctx ? ctx->launches : 0; }
+size_t cj_context_device_bytes(cj_context* ctx) { return ctx ? ctx->dev_bytes : 0; }
+
+cj_context* cj_default_context(void)
+{
+    static std::mutex mu;
+    static cj_context* ctx = nullptr;
+    std::lock_guard<std::mutex> g(mu);
+    if (!ctx) {
+        if (cj_context_create(-1, &ctx) != CJ_OK) ctx = nullptr;
+    }
+    return ctx;
+}
+
+cj_status cj_parse_standard(cj_context* ctx, const uint8_t* data, size_t size, cj_result* out)
+{
+    if (out) memset(out, 0, sizeof(*out));
+    if (!ctx || !out || !data || size == 0) return finish(CJ_ERR_INVALID_ARGUMENT);
+    const uint8_t* chunks[1] = {data};
+    size_t sizes[1] = {size};
+    cj_status st = stage(ctx, chunks, sizes, 1, false);
+    if (!st) st = run(ctx);
+    cj_parse_info info;
+    if (!st) st = read_info(ctx, &info);
+    if (!st && info.status != CJ_OK) st = (cj_status)info.status;
+    if (!st) st = to_result(ctx, info, out);
+    out->status = st;
+    return finish(st);
+}
+
+cj_status cj_parse_lines(cj_context* ctx, const uint8_t* const* chunks, const size_t* chunk_sizes,
+                         size_t n_chunks, cj_result* out)
+{
+    if (out) memset(out, 0, sizeof(*out));
+    if (!ctx || !out) return finish(CJ_ERR_INVALID_ARGUMENT);
+    cj_status st = stage(ctx, chunks, chunk_sizes, n_chunks, true);
+    if (!st) st = run(ctx);
+    cj_parse_info info;
+    if (!st) st = read_info(ctx, &info);
+    if (!st && info.status != CJ_OK) st = (cj_status)info.status;
+    if (!st) st = to_result(ctx, info, out);
+    out->status = st;
+    return finish(st);
+}
+
+void cj_result_free(cj_result* res)
+{
+    if (!res) return;
+    if (res->structural) cudaFreeHost(res->structural);
+    free(res->segment_sizes);
+    memset(res, 0, sizeof(*res));
+}
+
+cj_status cj_parse_into(cj_context* ctx, const uint8_t* data, size_t size, int lines_mode,
+                        int32_t* host_out, size_t out_cap, cj_parse_info* info)
+{
+    if (!ctx || !data || size == 0 || !host_out) return finish(CJ_ERR_INVALID_ARGUMENT);
+    const uint8_t* chunks[1] = {data};
+    size_t sizes[1] = {size};
+    cj_status st = stage(ctx, chunks, sizes, 1, lines_mode != 0);
+    if (!st) st = run(ctx);
+    cj_parse_info local;
+    if (!info) info = &local;
+    if (!st) st = read_info(ctx, info);
+    if (!st && info->status != CJ_OK) st = (cj_status)info->status;
+    if (!st) st = copy_result(ctx, info->n_structural, host_out, out_cap);
+    return finish(st);
+}
+
+cj_status cj_stage_standard(cj_context* ctx, const uint8_t* data, size_t size)
+{
+    if (!ctx || !data || size == 0) return CJ_ERR_INVALID_ARGUMENT;
+    const uint8_t* chunks[1] = {data};
+    size_t sizes[1] = {size};
+    return stage(ctx, chunks, sizes, 1, false);
+}
+
+cj_status cj_stage_lines(cj_context* ctx, const uint8_t* const* chunks, const size_t* chunk_sizes,
+                         size_t n_chunks)
+{
+    if (!ctx) return CJ_ERR_INVALID_ARGUMENT;
+    return stage(ctx, chunks, chunk_sizes, n_chunks, true);
+}
+
+cj_status cj_run_staged(cj_context* ctx)
+{
+    if (!ctx) return CJ_ERR_INVALID_ARGUMENT;
+    return run(ctx);
+}
+
+cj_status cj_staged_info(cj_context* ctx, cj_parse_info* info)
+{
+    if (!ctx) return CJ_ERR_INVALID_ARGUMENT;
+    return read_info(ctx, info);
+}
+
+cj_status cj_copy_staged_result(cj_context* ctx, int32_t* host_out, size_t out_cap)
+{
+    if (!ctx || !host_out) return CJ_ERR_INVALID_ARGUMENT;
+    cj_parse_info info;
+    cj_status st = read_info(ctx, &info);
+    if (st) return st;
+    return copy_result(ctx, info.n_structural, host_out, out_cap);
+}
+
+cj_status cj_staged_device_outputs(cj_context* ctx, const int32_t** d_positions,
+                                   const int32_t** d_pair_row)
+{
+    if (!ctx || !ctx->staged) return CJ_ERR_NOT_STAGED;
+    if (d_positions) *d_positions = ctx->pos.p;
+    if (d_pair_row) *d_pair_row = ctx->pair.p;
+    return CJ_OK;
+}
+
+const char* cj_status_string(int status)
+{
+    switch (status) {
+    case CJ_OK: return "ok";
+    case CJ_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case CJ_ERR_INVALID_UTF8: return "invalid UTF-8";
+    case CJ_ERR_INVALID_BRACKETS: return "unbalanced or mismatched brackets";
+    case CJ_ERR_TOO_LARGE: return "input larger than int32 positions allow";
+    case CJ_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case CJ_ERR_CUDA: return "CUDA runtime error";
+    case CJ_ERR_TIMEOUT: return "bounded device wait expired";
+    case CJ_ERR_NO_DEVICE: return "no CUDA device";
+    case CJ_ERR_CAPACITY: return "output buffer too small";
+    case CJ_ERR_NOT_STAGED: return "no staged input";
+    default: return "unknown status";
+    }
+}
+
+int cj_last_status(void) { return g_last_status; }
+void cj_set_last_status(int status) { g_last_status = status; }
+
+}  // extern "C"

@@ -1,0 +1,194 @@
+// cj_device.cuh -- data layout shared by the parse kernels and the host
+// orchestration, plus the word-level bit algorithms (host+device so the CPU
+// model in cj_model.cpp can exercise exactly the code the kernels run).
+#pragma once
+
+#include <stdint.h>
+
+#ifdef __CUDACC__
+#define CJ_HD __host__ __device__ __forceinline__
+#else
+#define CJ_HD inline
+#endif
+
+namespace cj {
+
+// ---- tiling ---------------------------------------------------------------
+// One CTA handles one tile: 256 threads x 32 bytes.  A thread owns one 32-bit
+// word of every character-class bitmap (bit j = byte j of its 32 bytes).
+constexpr int kThreads = 256;
+constexpr int kBytesPerThread = 32;
+constexpr int kTileBytes = kThreads * kBytesPerThread;   // 8 KiB
+constexpr int kWarps = kThreads / 32;
+
+// Pairing: one warp matches a chunk of this many bracket records.
+constexpr int kChunk = 512;
+constexpr int kHeads = 2 * kChunk + 1;   // level slots per chunk (levels L0-C .. L0+C)
+constexpr int kTreeLevels = 6;           // min-tree levels above the chunk array
+
+// ---- segments ---------------------------------------------------------------
+// A segment is one standard document or one JSON-Lines chunk.  Segments start
+// on tile boundaries of the device input.  Escape/string state and depth start
+// afresh in every segment; structural and bracket counts continue from the
+// previous segment when kSegContinue is set (JSON-Lines: one merged result),
+// and restart at 0 otherwise (independent documents).
+constexpr uint32_t kSegContinue = 1u;
+
+struct Segment {
+    uint64_t dev_off;      // byte offset of the segment in the device input
+    uint64_t len;          // bytes
+    uint64_t logical_off;  // added to byte positions (reference lastChunkIndex)
+    uint64_t out_base;     // output index base (independent documents)
+    uint64_t brk_base;     // bracket-record base (independent documents)
+    uint32_t first_tile;
+    uint32_t n_tiles;
+    uint32_t flags;
+    uint32_t pad;
+};
+
+struct SegmentOut {        // written by the last tile of each segment
+    uint32_t s_end;        // structural count at segment end (global if continuing)
+    uint32_t k_end;        // bracket count at segment end
+    int32_t  depth_end;    // nesting depth at segment end (0 when balanced)
+    uint32_t instr_end;    // 1 if the segment ends inside a string
+};
+
+// Control block, zeroed before every run.
+struct Ctrl {
+    uint32_t tile_ticket;     // tiles handed out in launch order
+    uint32_t error_flags;     // CJ_FLAG_* bits
+    uint32_t s_total;
+    uint32_t k_total;
+    int32_t  neg_min_level;   // max(-level) over brackets; > 0 means a close below depth 0
+    int32_t  max_depth;
+    uint32_t n_tiles_done;
+    uint32_t pad;
+};
+
+// ---- look-back descriptors -------------------------------------------------
+// Entry state of a tile: bit1 = previous byte is an unescaped backslash (the
+// first byte is escaped), bit0 = inside a string.  A tile's aggregate maps each
+// of the 4 entry states to (exit state, structural count, bracket count, depth
+// delta); bit 2 of `st` marks a depth reset (segment start: depth restarts).
+struct Ent {
+    uint32_t st;   // bits 0-1 exit state, bit 2 depth reset
+    uint32_t s;
+    uint32_t k;
+    int32_t  d;
+};
+
+constexpr uint32_t kFlagAgg = 1u;
+constexpr uint32_t kFlagIncl = 2u;
+
+CJ_HD Ent ent_identity(uint32_t state) { Ent e; e.st = state; e.s = 0; e.k = 0; e.d = 0; return e; }
+
+// value v (state, counts, absolute depth) followed by tile table t
+CJ_HD Ent ent_apply(Ent v, const Ent t[4]) {
+    const Ent& x = t[v.st & 3u];
+    Ent r;
+    r.st = x.st & 3u;
+    r.s = v.s + x.s;
+    r.k = v.k + x.k;
+    r.d = (x.st & 4u) ? x.d : v.d + x.d;
+    return r;
+}
+
+// table a followed by table b
+CJ_HD void tab_compose(const Ent a[4], const Ent b[4], Ent out[4]) {
+    Ent tmp[4];
+    for (int s = 0; s < 4; s++) {
+        const Ent& x = a[s];
+        const Ent& y = b[x.st & 3u];
+        tmp[s].st = (y.st & 3u) | ((x.st | y.st) & 4u);
+        tmp[s].s = x.s + y.s;
+        tmp[s].k = x.k + y.k;
+        tmp[s].d = (y.st & 4u) ? y.d : x.d + y.d;
+    }
+    for (int s = 0; s < 4; s++) out[s] = tmp[s];
+}
+
+CJ_HD void tab_identity(Ent t[4]) { for (uint32_t s = 0; s < 4; s++) t[s] = ent_identity(s); }
+
+// ---- bracket records ---------------------------------------------------------
+// x = structural index | (1 << 31 if '{' / '}'), y = (level << 1) | is_open.
+// level of an open = depth before it, level of a close = depth after it, so a
+// matching pair shares its level.
+constexpr uint32_t kCurly = 0x80000000u;
+constexpr uint32_t kEmpty = 0xFFFFFFFFu;
+
+// ---- word-level bit algorithms ----------------------------------------------
+
+// high bit of every byte of w that equals the corresponding byte of pat
+CJ_HD uint32_t eq_bytes(uint32_t w, uint32_t pat) {
+    uint32_t x = w ^ pat;
+    return ~(((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x) & 0x80808080u;
+}
+
+// bits 7/15/23/31 of m -> bits 0..3 (multiplication gathers them into the top
+// nibble without carries because the partial products never overlap)
+CJ_HD uint32_t gather4(uint32_t m) { return (m * 0x00204081u) >> 28; }
+
+struct Classes {
+    uint32_t q, bs, st, op, cl, cur, hi;
+};
+
+// Character classes of 32 bytes held as 8 little-endian words.
+template <bool LINES>
+CJ_HD Classes classify32(const uint32_t w[8]) {
+    Classes c;
+    c.q = c.bs = c.st = c.op = c.cl = c.cur = c.hi = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        uint32_t x = w[k];
+        uint32_t q = eq_bytes(x, 0x22222222u);
+        uint32_t b = eq_bytes(x, 0x5C5C5C5Cu);
+        uint32_t y = x & 0xDFDFDFDFu;              // '{' -> '[', '}' -> ']'
+        uint32_t o = eq_bytes(y, 0x5B5B5B5Bu);
+        uint32_t cl = eq_bytes(y, 0x5D5D5D5Du);
+        uint32_t s = o | cl | eq_bytes(x, 0x3A3A3A3Au) | eq_bytes(x, 0x2C2C2C2Cu);
+        if (LINES) s |= eq_bytes(x, 0x0A0A0A0Au);
+        uint32_t cu = (x << 2) & (o | cl);         // bit 5 (curly) -> bit 7
+        int sh = 4 * k;
+        c.q |= gather4(q) << sh;
+        c.bs |= gather4(b) << sh;
+        c.st |= gather4(s) << sh;
+        c.op |= gather4(o) << sh;
+        c.cl |= gather4(cl) << sh;
+        c.cur |= gather4(cu) << sh;
+        c.hi |= x;
+    }
+    c.hi &= 0x80808080u;
+    return c;
+}
+
+// Escaped-character mask of one 32-byte word.  `carry` = 1 when byte 0 is
+// escaped by an odd backslash run ending in the previous word.  Within a run of
+// backslashes that starts fresh at position s, the bytes s+1, s+3, ... are
+// escaped (each backslash at s, s+2, ... escapes its successor).  Runs starting
+// at odd positions are found with one addition: adding their start bit clears
+// the run and sets the bit after it, and the XOR with the run marks its span.
+// *cout receives the carry for the next word.
+CJ_HD uint32_t escaped32(uint32_t bs, uint32_t carry, uint32_t* cout) {
+    const uint32_t ODD = 0xAAAAAAAAu;
+    uint32_t b = bs & ~carry;              // an escaped first byte starts no run
+    uint32_t starts = b & ~(b << 1);
+    uint32_t os = starts & ODD;
+    uint64_t t = (uint64_t)b + os;
+    uint32_t tl = (uint32_t)t;
+    *cout = (uint32_t)(t >> 32);
+    uint32_t odd_span = (tl ^ b) ^ os;     // s+1 .. s+L of odd-start runs
+    uint32_t span = b << 1;                // s+1 .. s+L of every run
+    return (span & (ODD ^ odd_span)) | carry;
+}
+
+// inclusive prefix XOR over the bits of x
+CJ_HD uint32_t prefix_xor(uint32_t x) {
+    x ^= x << 1;
+    x ^= x << 2;
+    x ^= x << 4;
+    x ^= x << 8;
+    x ^= x << 16;
+    return x;
+}
+
+}  // namespace cj

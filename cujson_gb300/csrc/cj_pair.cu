@@ -1,0 +1,233 @@
+// cj_pair.cu -- nesting recognition: open/close pairing by depth buckets.
+//
+// The reference keys every bracket by its depth (uint8), stable-sorts the
+// brackets by that key with thrust::stable_sort_by_key and pairs neighbours
+// (cujson/parse_standard_json.cu:1519-1582, validate_expand_MathAPI_new2
+// :1432-1514).  Here no sort is needed: every bracket record already carries
+// its level (depth before an open, depth after a close), so a matching pair
+// shares a level and, inside one level's bucket, opens and closes alternate
+// in document order.  The pass keeps one slot per level ("bucket head") that
+// holds the currently open bracket of that level:
+//
+//   kernel pair_chunks: one warp walks a chunk of 512 records, 32 at a time.
+//     __match_any_sync groups the lanes of a round by level; a close pairs
+//     with the previous same-level lane of its round, else with its level's
+//     bucket head.  The last lane of each level group then updates the head
+//     (an open becomes the head, a close empties it).  What stays unmatched
+//     in a chunk is its "spine": closes at levels entry-1 .. min (one per
+//     level) and opens at levels min .. exit-1 (one per level).
+//   kernel pair_spine: an unmatched open at level d in chunk c pairs with the
+//     unmatched close at level d of the first later chunk whose minimum depth
+//     is <= d, found through a 32-ary min-tree over the chunk minima.
+//
+// Levels are int32, so nesting is unbounded (the reference's uint8 key aliases
+// past depth 256).  Validation: every level >= 0, every pair of the same kind,
+// and depth 0 at the end of each segment (checked by the scan).
+#include "cj_device.cuh"
+#include "cj_kernels.h"
+#include "cujson_gb300.h"
+
+#include <climits>
+
+namespace cj {
+
+namespace {
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+__device__ __forceinline__ uint32_t lanemask_gt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_gt;" : "=r"(m));
+    return m;
+}
+
+__device__ __forceinline__ unsigned long long tree_pack(uint32_t epoch, int32_t level) {
+    return ((unsigned long long)epoch << 32) | (uint32_t)(0x7FFFFFFF - level);
+}
+
+__device__ __forceinline__ int32_t tree_value(const PairParams& P, int lvl, uint64_t i) {
+    if (lvl == 0) return __ldcg(&P.cinfo[i].y);
+    unsigned long long v = __ldcg(P.tree + P.tree_off[lvl] + i);
+    if ((uint32_t)(v >> 32) != P.epoch) return INT_MAX;
+    return 0x7FFFFFFF - (int32_t)(uint32_t)v;
+}
+
+// first chunk index > c whose minimum depth is <= d, or -1
+__device__ int64_t next_le(const PairParams& P, uint64_t nch, uint64_t c, int32_t d) {
+    uint64_t size[kTreeLevels + 1];
+    size[0] = nch;
+    for (int l = 1; l <= kTreeLevels; l++) size[l] = (size[l - 1] + 31) / 32;
+    uint64_t i = c + 1;
+    int lvl = 0;
+    while (true) {
+        if (i >= size[lvl]) return -1;
+        uint64_t gend = (i | 31) + 1;
+        if (gend > size[lvl]) gend = size[lvl];
+        bool found = false;
+        for (; i < gend; i++)
+            if (tree_value(P, lvl, i) <= d) { found = true; break; }
+        if (found) break;
+        if (lvl == kTreeLevels) return -1;
+        i = gend >> 5;
+        lvl++;
+    }
+    while (lvl > 0) {
+        lvl--;
+        i *= 32;
+        uint64_t gend = i + 32;
+        if (gend > size[lvl]) gend = size[lvl];
+        for (; i < gend; i++)
+            if (tree_value(P, lvl, i) <= d) break;
+        if (i >= gend) return -1;   // inconsistent tree (only on a timeout path)
+    }
+    return (int64_t)i;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(256) pair_chunks(PairParams P)
+{
+    extern __shared__ uint32_t s_heads_all[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    uint32_t* heads = s_heads_all + wib * kHeads;
+    const uint32_t FULL = 0xFFFFFFFFu;
+    const uint32_t K = P.ctrl->k_total;
+    const uint64_t nch = ((uint64_t)K + kChunk - 1) / kChunk;
+    const uint64_t gwarp = (uint64_t)blockIdx.x * (blockDim.x >> 5) + wib;
+    const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    const uint32_t lt = lanemask_lt(), gt = lanemask_gt();
+    uint32_t err = 0;
+
+    for (uint64_t c = gwarp; c < nch; c += nwarps) {
+        const uint64_t base = c * kChunk;
+        const int cnt = (int)min((uint64_t)kChunk, (uint64_t)K - base);
+        for (int i = lane; i < kHeads; i += 32) heads[i] = kEmpty;
+        const uint2 r0 = __ldcg(P.brk + base);
+        const int32_t L0 = (int32_t)r0.y >> 1;
+        const int32_t d_entry = (r0.y & 1u) ? L0 : L0 + 1;
+        int32_t dmin = d_entry, maxd = INT_MIN;
+        int32_t last_lvl = 0;
+        uint32_t last_open = 0;
+        __syncwarp();
+
+        for (int r = 0; r < cnt; r += 32) {
+            const bool valid = (r + lane) < cnt;
+            uint2 rec = make_uint2(0u, 0u);
+            if (valid) rec = __ldcg(P.brk + base + r + lane);
+            const int32_t lvl = (int32_t)rec.y >> 1;
+            const uint32_t is_open = rec.y & 1u;
+            const uint32_t key = valid ? (uint32_t)lvl : (0xC0000000u | (uint32_t)lane);
+            const uint32_t peers = __match_any_sync(FULL, key);
+            const uint32_t prevp = peers & lt;
+            const int plane = prevp ? 31 - __clz(prevp) : lane;
+            const uint32_t p_x = __shfl_sync(FULL, rec.x, plane);
+            const uint32_t p_open = __shfl_sync(FULL, is_open, plane);
+            const int slot = lvl - L0 + kChunk;
+            if (valid && !is_open) {
+                uint32_t partner = kEmpty;
+                if (prevp) {
+                    if (p_open) partner = p_x;
+                    else err |= CJ_FLAG_BRACKETS;     // two closes in a row at one level
+                } else if (slot >= 0 && slot < kHeads) {
+                    partner = heads[slot];
+                    if (partner == kEmpty) {
+                        // unmatched inside the chunk: part of the spine
+                        const int32_t idx = d_entry - 1 - lvl;
+                        if (idx >= 0 && idx < kChunk) P.spine[base + idx] = rec.x;
+                        else err |= CJ_FLAG_BRACKETS;
+                    }
+                }
+                if (partner != kEmpty) {
+                    if ((partner ^ rec.x) & kCurly) err |= CJ_FLAG_BRACKETS;
+                    P.pair[partner & ~kCurly] = (int32_t)((rec.x & ~kCurly) + 1u);
+                }
+            }
+            __syncwarp();
+            if (valid && (peers & gt) == 0u && slot >= 0 && slot < kHeads)
+                heads[slot] = is_open ? rec.x : kEmpty;
+            __syncwarp();
+            if (valid) {
+                if (!is_open) dmin = min(dmin, lvl);
+                else maxd = max(maxd, lvl + 1);
+            }
+            const int lastlane = min(31, cnt - r - 1);
+            last_lvl = __shfl_sync(FULL, lvl, lastlane);
+            last_open = __shfl_sync(FULL, is_open, lastlane);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            dmin = min(dmin, __shfl_xor_sync(FULL, dmin, o));
+            maxd = max(maxd, __shfl_xor_sync(FULL, maxd, o));
+        }
+        const int32_t d_exit = last_open ? last_lvl + 1 : last_lvl;
+        for (int i = lane; i < kHeads; i += 32) {
+            const uint32_t h = heads[i];
+            if (h != kEmpty) {
+                const int32_t lvl = i - kChunk + L0;
+                const int32_t idx = lvl - dmin;
+                if (idx >= 0 && idx < kChunk) P.spine[base + (kChunk - 1 - idx)] = h;
+                else err |= CJ_FLAG_BRACKETS;
+            }
+        }
+        if (lane == 0) {
+            P.cinfo[c] = make_int4(d_entry, dmin, d_exit, 0);
+            if (dmin < 0) atomicMax(&P.ctrl->neg_min_level, -dmin);
+            if (maxd > 0) atomicMax(&P.ctrl->max_depth, maxd);
+            const unsigned long long pk = tree_pack(P.epoch, dmin);
+            for (int l = 1; l <= kTreeLevels; l++)
+                atomicMax(P.tree + P.tree_off[l] + (c >> (5 * l)), pk);
+        }
+        __syncwarp();
+    }
+    err = __reduce_or_sync(FULL, err);
+    if (lane == 0 && err) atomicOr(&P.ctrl->error_flags, err);
+}
+
+__global__ void __launch_bounds__(256) pair_spine(PairParams P)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t K = P.ctrl->k_total;
+    const uint32_t S = P.ctrl->s_total;
+    const uint64_t nch = ((uint64_t)K + kChunk - 1) / kChunk;
+    const uint64_t gwarp = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    uint32_t err = 0;
+    for (uint64_t c = gwarp; c < nch; c += nwarps) {
+        const int4 ci = __ldcg(&P.cinfo[c]);
+        const int32_t n_uo = ci.z - ci.y;          // opens still open at chunk end
+        const int32_t n_uc = ci.x - ci.y;          // closes unmatched inside the chunk
+        if (n_uo < 0 || n_uc < 0 || n_uo + n_uc > kChunk) { err |= CJ_FLAG_BRACKETS; continue; }
+        for (int32_t i = lane; i < n_uo; i += 32) {
+            const int32_t d = ci.y + i;
+            const uint32_t ox = __ldcg(P.spine + c * kChunk + (kChunk - 1 - i));
+            const int64_t c2 = next_le(P, nch, c, d);
+            if (c2 < 0) { err |= CJ_FLAG_BRACKETS; continue; }
+            const int4 cj2 = __ldcg(&P.cinfo[c2]);
+            const int32_t idx = cj2.x - 1 - d;
+            if (idx < 0 || idx >= kChunk || idx >= cj2.x - cj2.y) { err |= CJ_FLAG_BRACKETS; continue; }
+            const uint32_t cx = __ldcg(P.spine + (uint64_t)c2 * kChunk + idx);
+            if ((ox ^ cx) & kCurly) err |= CJ_FLAG_BRACKETS;
+            if ((ox & ~kCurly) >= S || (cx & ~kCurly) >= S) { err |= CJ_FLAG_BRACKETS; continue; }
+            P.pair[ox & ~kCurly] = (int32_t)((cx & ~kCurly) + 1u);
+        }
+    }
+    err = __reduce_or_sync(0xFFFFFFFFu, err);
+    if (lane == 0 && err) atomicOr(&P.ctrl->error_flags, err);
+}
+
+void launch_pair(const PairParams& p, int grid, cudaStream_t stream)
+{
+    const size_t smem = sizeof(uint32_t) * kHeads * 8;   // 32.8 KB: under the 48 KB default
+    pair_chunks<<<grid, 256, smem, stream>>>(p);
+}
+
+void launch_spine(const PairParams& p, int grid, cudaStream_t stream)
+{
+    pair_spine<<<grid, 256, 0, stream>>>(p);
+}
+
+}  // namespace cj

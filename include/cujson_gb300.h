@@ -1,0 +1,186 @@
+/*
+ * cujson_gb300.h -- C ABI of the GB300-native cuJSON parse path.
+ *
+ * Plain C: pointers, sizes and status codes, no C++ or torch types.  The
+ * drop-in C++ headers include/cujson/cujson.h and include/cujson/cujsonlines.h
+ * (which keep the reference's type layouts and function names) are thin
+ * inline wrappers over these entry points; other languages bind them directly
+ * (see INTEGRATION.md for the ctypes / cgo / JNI stubs).
+ *
+ * Reference interfaces replaced (file:line within AutomataLab/cuJSON):
+ *   cj_parse_standard  <- cuJSONResult parse_standard_json(cuJSONInput)
+ *                         cujson/parse_standard_json.h:9, parse_standard_json.cu:1584
+ *   cj_parse_lines     <- cuJSONResult parse_json_lines(cuJSONLinesInput)
+ *                         cujson/parse_json_lines.h:9, parse_json_lines.cu:1092
+ *   cj_result_free     <- cuJSONIterator::freeJson (cudaFreeHost of the result)
+ *                         cujson/query/query_iterator_standard_json.cpp:143-146
+ * Everything else here (contexts, staged device-resident runs, the generator)
+ * has no counterpart in the reference, which has no library boundary at all.
+ *
+ * Result layout (identical to the reference's pinned result buffer,
+ * cujson/parse_standard_json.cu:1659-1680): one pinned int32 buffer of
+ * 2*(S+2) entries.  structural = buf; structural[0] = 0 (virtual root '['),
+ * structural[1..S] = 1-based byte offsets of { } [ ] : , (and '\n' for JSON
+ * Lines) outside strings, structural[S+1] = S+1 (virtual ']').
+ * pair_pos = buf + S + 1; pair_pos[0] = S+1; for each open at structural index
+ * i (1-based), pair_pos[i] = the structural index of its matching close.
+ * Deliberate differences: pair_pos at non-open entries is 0 (the reference
+ * leaves it uninitialised), the JSON-Lines virtual-root slots are written, and
+ * errors return a status instead of calling exit(0).
+ */
+#ifndef CUJSON_GB300_H
+#define CUJSON_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CJ_ABI_VERSION 1
+
+typedef enum cj_status {
+    CJ_OK = 0,
+    CJ_ERR_INVALID_ARGUMENT = 1,  /* null data, zero size, bad chunk table */
+    CJ_ERR_INVALID_UTF8 = 2,      /* ill-formed UTF-8 (RFC 3629) */
+    CJ_ERR_INVALID_BRACKETS = 3,  /* unbalanced or mismatched { } [ ] */
+    CJ_ERR_TOO_LARGE = 4,         /* input does not fit int32 positions */
+    CJ_ERR_OUT_OF_MEMORY = 5,
+    CJ_ERR_CUDA = 6,              /* a CUDA runtime call failed */
+    CJ_ERR_TIMEOUT = 7,           /* a bounded device-side wait expired */
+    CJ_ERR_NO_DEVICE = 8,
+    CJ_ERR_CAPACITY = 9,          /* caller-provided output buffer too small */
+    CJ_ERR_NOT_STAGED = 10        /* cj_run_staged without a staged input */
+} cj_status;
+
+/* detail bits in cj_parse_info.error_flags */
+#define CJ_FLAG_UTF8        0x01u
+#define CJ_FLAG_BRACKETS    0x02u
+#define CJ_FLAG_TIMEOUT     0x04u
+#define CJ_FLAG_OVERFLOW    0x08u
+
+/* Largest input in bytes: positions are int32 (reference, cujson_types.h:26). */
+#define CJ_MAX_INPUT_BYTES 2147483646ull
+
+typedef struct cj_parse_info {
+    int64_t  n_structural;   /* S */
+    int64_t  n_brackets;     /* opens + closes outside strings */
+    int32_t  max_depth;      /* deepest nesting (the reference never sets it) */
+    int32_t  status;         /* cj_status verdict */
+    uint32_t error_flags;    /* CJ_FLAG_* */
+    int32_t  n_segments;     /* 1, or the number of JSON-Lines chunks */
+} cj_parse_info;
+
+/* Result of cj_parse_standard / cj_parse_lines.  `structural` is a pinned
+ * host allocation (cudaMallocHost) released by cj_result_free. */
+typedef struct cj_result {
+    int32_t* structural;
+    int32_t* pair_pos;
+    int64_t  n_structural;         /* S */
+    int64_t  total;                /* S + 2 (cuJSONResult::totalResultSize) */
+    int32_t  max_depth;
+    int32_t  status;
+    int64_t  n_segments;
+    int64_t* segment_sizes;        /* malloc'd: S per JSON-Lines chunk */
+} cj_result;
+
+typedef struct cj_context cj_context;
+
+/* ---- contexts -------------------------------------------------------------
+ * A context owns one device, one non-blocking stream and a device arena that
+ * grows to the largest input seen.  A context is not thread safe; use one per
+ * host thread.  `device` < 0 means the current device. */
+cj_status cj_context_create(int device, cj_context** out);
+void      cj_context_destroy(cj_context* ctx);
+/* Pre-size the arena for inputs up to `max_bytes` in up to `max_segments`
+ * JSON-Lines chunks (avoids growth inside timed regions). */
+cj_status cj_context_reserve(cj_context* ctx, size_t max_bytes, size_t max_segments);
+void*     cj_context_stream(cj_context* ctx);           /* cudaStream_t */
+int64_t   cj_context_launch_count(cj_context* ctx);     /* kernels launched so far */
+size_t    cj_context_device_bytes(cj_context* ctx);     /* arena size */
+
+/* Process-wide default context on the current device (used by the drop-in
+ * C++ headers); created on first use. */
+cj_context* cj_default_context(void);
+
+/* ---- one-shot parses (drop-in semantics) ------------------------------------ */
+cj_status cj_parse_standard(cj_context* ctx, const uint8_t* host_data, size_t size,
+                            cj_result* out);
+cj_status cj_parse_lines(cj_context* ctx, const uint8_t* const* chunks,
+                         const size_t* chunk_sizes, size_t n_chunks, cj_result* out);
+void      cj_result_free(cj_result* res);
+
+/* One-shot parse into a caller-provided host buffer (pinned for full speed)
+ * of `out_cap` int32 entries, in the layout above; needs 2*(S+2) entries.
+ * `lines_mode` != 0 treats the input as one JSON-Lines chunk. */
+cj_status cj_parse_into(cj_context* ctx, const uint8_t* host_data, size_t size, int lines_mode,
+                        int32_t* host_out, size_t out_cap, cj_parse_info* info);
+
+/* ---- staged, device-resident runs -------------------------------------------
+ * Stage copies the input into the context arena (synchronously); run launches
+ * the parse kernels on the context stream without any host synchronisation;
+ * info synchronises and reads the verdict and counts; copy_result writes the
+ * reference layout into a host buffer.  Used for device-resident throughput. */
+cj_status cj_stage_standard(cj_context* ctx, const uint8_t* host_data, size_t size);
+cj_status cj_stage_lines(cj_context* ctx, const uint8_t* const* chunks,
+                         const size_t* chunk_sizes, size_t n_chunks);
+cj_status cj_run_staged(cj_context* ctx);
+cj_status cj_staged_info(cj_context* ctx, cj_parse_info* info);
+cj_status cj_copy_staged_result(cj_context* ctx, int32_t* host_out, size_t out_cap);
+/* Device pointers of the staged run's outputs (valid until the next run):
+ * positions[S] (1-based byte offsets) and pair_row[S] (pair_row[i] = 1-based
+ * close index for opens, else 0). */
+cj_status cj_staged_device_outputs(cj_context* ctx, const int32_t** d_positions,
+                                   const int32_t** d_pair_row);
+
+/* ---- measurement and host memory --------------------------------------------
+ * With timing enabled, every run records CUDA events on the context stream
+ * around each kernel; cj_context_phase_ms synchronises and returns the summed
+ * milliseconds of the scan, pair and spine kernels over the runs recorded since
+ * timing was (re-)enabled. */
+cj_status cj_context_timing(cj_context* ctx, int enable);
+cj_status cj_context_phase_ms(cj_context* ctx, double* scan_ms, double* pair_ms,
+                              double* spine_ms, int64_t* runs);
+/* Milliseconds from the first recorded run's start to the last one's end. */
+cj_status cj_context_span_ms(cj_context* ctx, double* ms);
+/* Pinned host memory (cudaMallocHost / cudaFreeHost) for callers without the
+ * CUDA runtime headers. */
+void* cj_host_alloc(size_t bytes);
+void  cj_host_free(void* p);
+
+const char* cj_status_string(int status);
+/* Status of the calling thread's last drop-in parse (parse_standard_json /
+ * parse_json_lines return an empty result on failure, as the reference's
+ * callers expect). */
+int cj_last_status(void);
+void cj_set_last_status(int status);
+
+/* ---- synthetic inputs -------------------------------------------------------
+ * Seeded generators standing in for the reference's evaluation datasets (not
+ * available offline).  Deterministic for a given seed on every machine. */
+typedef struct cj_synth_params {
+    int32_t  max_depth;          /* nesting limit of values */
+    int32_t  keys_min, keys_max; /* members per top-level object */
+    int32_t  nested_max_items;   /* members / elements per nested container */
+    int32_t  str_min, str_max;   /* string lengths */
+    double   huge_string_frac;   /* fraction of strings that are huge */
+    int64_t  huge_string_min, huge_string_max;
+    uint64_t block_bytes;        /* independent generation block */
+    double   record_median, record_sigma;   /* JSON-Lines lognormal sizes */
+    int64_t  record_min, record_max;
+    uint32_t threads;            /* 0 = all host threads */
+} cj_synth_params;
+
+void   cj_synth_default_params(cj_synth_params* p);
+size_t cj_synth_document(uint64_t seed, size_t size, const cj_synth_params* p, uint8_t* out);
+size_t cj_synth_lines(uint64_t seed, size_t size, const cj_synth_params* p, uint8_t* out,
+                      uint64_t* n_records);
+size_t cj_synth_deep(size_t depth, uint8_t* out);
+size_t cj_synth_backslash_string(uint64_t seed, size_t body, uint8_t* out);
+int    cj_synth_corrupt(uint8_t* doc, size_t n, int kind, uint64_t seed);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

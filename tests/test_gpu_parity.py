@@ -1,0 +1,136 @@
+"""GPU parse vs the oracle, through the C ABI (bit-exact; integer outputs)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def assert_same(res, ref):
+    assert res.n_structural == ref.n_structural
+    np.testing.assert_array_equal(res.positions, ref.positions)
+    np.testing.assert_array_equal(res.pair_row, ref.pair_row)
+    np.testing.assert_array_equal(res.buffer, ref.reference_layout())
+
+
+@pytest.mark.parametrize("doc", [
+    b"[1,2]", b'{"a":"b\\"c,d"}', b'["\\\\",1]', b'["\\\\\\"",1]', b'{"k":[{},[]],"x":{}}',
+    b'"[{,:}]"', b"123", b"   ", b'[":" , "{" ]', b"[]", b"{}", b'[[[[{"a":[]}]]]]',
+])
+def test_small(ctx, oracle, doc):
+    st, res = ctx.try_parse(doc)
+    assert st == 0
+    assert_same(res, oracle.parse(doc))
+
+
+@pytest.mark.parametrize("n", [1, 2, 31, 32, 33, 255, 8191, 8192, 8193, 16384, 65537, 300001])
+def test_sizes(cj, ctx, oracle, n):
+    d = cj.synth_document(n, max(n, 2))[:n] if n >= 2 else np.frombuffer(b"1", np.uint8)
+    if n >= 2:
+        d = cj.synth_document(n, n)
+    st, res = ctx.try_parse(d)
+    ref = oracle.parse(d)
+    assert st == 0 and ref.flags == 0
+    assert_same(res, ref)
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_documents(cj, ctx, oracle, seed):
+    n = [5000, 70000, 1 << 20, 3 << 20, 123457, 9999, 2 << 20, 777777][seed]
+    d = cj.synth_document(2000 + seed, n, max_depth=10)
+    res = ctx.parse_standard_json(d)
+    assert_same(res, oracle.parse(d))
+
+
+def test_huge_strings(cj, ctx, oracle):
+    d = cj.synth_document(78, 4 << 20, max_depth=20, huge_string_frac=0.05,
+                          huge_string_min=20000, huge_string_max=90000)
+    assert_same(ctx.parse_standard_json(d), oracle.parse(d))
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_backslash_runs(cj, ctx, oracle, seed):
+    d = cj.synth_backslash_string(seed, 200000 + 4093 * seed)
+    assert_same(ctx.parse_standard_json(d), oracle.parse(d))
+
+
+@pytest.mark.parametrize("depth", [1, 256, 257, 10000, 100000])
+def test_deep(cj, ctx, oracle, depth):
+    d = cj.synth_deep(depth)
+    res = ctx.parse_standard_json(d)
+    assert_same(res, oracle.parse(d))
+    assert res.max_depth == depth
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_random_bytes(cj, ctx, oracle, seed):
+    rng = np.random.default_rng(seed)
+    alphabet = np.frombuffer(b'[]{}:,"\\ ab\n', np.uint8)
+    n = int(rng.integers(1, 60000))
+    d = alphabet[rng.integers(0, alphabet.size, n)]
+    lines = bool(seed & 1)
+    st, res = ctx.try_parse(d, lines=lines)
+    ref = oracle.parse(d, lines=lines)
+    if ref.flags:
+        assert st in (2, 3)
+    else:
+        assert st == 0
+        assert_same(res, ref)
+
+
+def test_lines(cj, ctx, oracle):
+    d, _ = cj.synth_lines(5, 3 << 20)
+    nl = np.flatnonzero(d == 10)
+    cuts = [0] + [int(nl[i * len(nl) // 4]) + 1 for i in range(1, 4)] + [d.size]
+    sizes = [cuts[i + 1] - cuts[i] for i in range(4)]
+    res = ctx.parse_json_lines([d[cuts[i]:cuts[i + 1]] for i in range(4)])
+    ref = oracle.parse(d, lines=True, chunk_sizes=sizes)
+    assert_same(res, ref)
+    assert sum(res.segment_sizes) == res.n_structural and len(res.segment_sizes) == 4
+
+
+@pytest.mark.parametrize("kind,status", [(1, 2), (2, 2), (3, 2), (4, 3), (5, 3)])
+def test_invalid(cj, ctx, oracle, kind, status):
+    d = cj.synth_document(500 + kind, 200000)
+    assert cj.synth_corrupt(d, kind, 3)
+    st, res = ctx.try_parse(d)
+    assert st == status and res is None
+
+
+@pytest.mark.parametrize("doc", [b"[}", b"{]", b"[[]", b"[]]", b"][", b"}{{}", b"[{]}", b"]"])
+def test_invalid_brackets(ctx, doc):
+    st, _ = ctx.try_parse(doc)
+    assert st == 3
+
+
+def test_utf8_cases(ctx, oracle):
+    for body, ok in [("é€😀".encode(), True), (b"\xc0\x80", False), (b"\xe0\x80\x80", False),
+                     (b"\xed\xa0\x80", False), (b"\xf5\x80\x80\x80", False), (b"\xe2\x82", False),
+                     (b"\x80", False), (b"\xc3\x41", False)]:
+        for pad in (0, 29, 30, 31, 8190):
+            doc = b"[" + b" " * pad + b'"' + body + b'"]'
+            st, _ = ctx.try_parse(doc)
+            assert (st == 0) == ok, (body, pad, st)
+
+
+def test_repeat_deterministic(cj, ctx):
+    d = cj.synth_document(99, 2 << 20)
+    first = ctx.parse_standard_json(d).buffer
+    for _ in range(20):
+        assert np.array_equal(ctx.parse_standard_json(d).buffer, first)
+
+
+def test_staged_and_into(cj, ctx, oracle):
+    d = cj.synth_document(123, 1 << 20)
+    ref = oracle.parse(d)
+    ctx.stage_standard(d)
+    ctx.run()
+    assert_same(ctx.staged_result(), ref)
+    out = np.zeros(2 * ref.n_structural + 4, np.int32)
+    inf = ctx.parse_into(d, out)
+    assert inf.n_structural == ref.n_structural
+    np.testing.assert_array_equal(out, ref.reference_layout())
+
+
+def test_empty_input_rejected(ctx):
+    st, _ = ctx.try_parse(b"")
+    assert st == 1
