@@ -43,6 +43,7 @@ size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
 struct cj_context {
     int device = 0;
     int sm_count = 0;
+    uint32_t scan_grid = 0;             // resident scan CTAs (persistent grid)
     cudaStream_t stream = nullptr;
 
     DevBuf<uint8_t> in;
@@ -110,8 +111,8 @@ void release(DevBuf<T>& b) { if (b.p) cudaFree(b.p); b.p = nullptr; b.cap = 0; }
 // structural count, is at most the byte count, and so is the bracket count.
 cj_status reserve(cj_context* ctx, size_t bytes, size_t segs)
 {
-    size_t padded = round_up(bytes, kTileBytes) + segs * (size_t)kTileBytes;
-    size_t tiles = padded / kTileBytes + 1;
+    size_t padded = round_up(bytes, kPadBytes) + segs * (size_t)kPadBytes;
+    size_t tiles = bytes / kTileBytes + segs + 1;
     size_t s_cap = bytes + 1;
     size_t chunks = (bytes + kChunk - 1) / kChunk + 1;
     cj_status st;
@@ -184,7 +185,7 @@ cj_status stage(cj_context* ctx, const uint8_t* const* chunks, const size_t* siz
         s.n_tiles = (uint32_t)((sizes[i] + kTileBytes - 1) / kTileBytes);
         s.flags = (i > 0) ? kSegContinue : 0u;
         s.pad = 0;
-        dev_off += (uint64_t)s.n_tiles * kTileBytes;
+        dev_off += round_up(sizes[i], kPadBytes);
         logical += sizes[i];
         tile += s.n_tiles;
     }
@@ -253,7 +254,7 @@ cj_status run(cj_context* ctx)
     sp.ctrl = ctx->d_ctrl;
     sp.seg_out = ctx->seg_out.p;
     sp.epoch = ctx->epoch;
-    launch_scan(sp, ctx->lines, ctx->stream);
+    launch_scan(sp, ctx->lines, (int)std::min<uint32_t>(ctx->n_tiles, ctx->scan_grid), ctx->stream);
     if (ev) CJ_CUDA(cudaEventRecord(ev[1], ctx->stream));
 
     PairParams pp;
@@ -361,6 +362,15 @@ cj_status cj_context_create(int device, cj_context** out)
     cj_context* ctx = new cj_context();
     ctx->device = device;
     cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    int per_sm = 0;
+    if (scan_configure() != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, scan_kernel_ptr(), kThreads,
+                                                      scan_smem_bytes()) != cudaSuccess ||
+        per_sm < 1) {
+        delete ctx;
+        return CJ_ERR_CUDA;
+    }
+    ctx->scan_grid = (uint32_t)(per_sm * ctx->sm_count);
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMalloc((void**)&ctx->d_ctrl, sizeof(Ctrl)) != cudaSuccess) {
         cj_context_destroy(ctx);

@@ -14,12 +14,20 @@
 namespace cj {
 
 // ---- tiling ---------------------------------------------------------------
-// One CTA handles one tile: 256 threads x 32 bytes.  A thread owns one 32-bit
-// word of every character-class bitmap (bit j = byte j of its 32 bytes).
+// A warp step is what one warp classifies at once: 32 lanes x 32 bytes, so a
+// lane owns one 32-bit word of every character-class bitmap (bit j = byte j
+// of its 32 bytes).  Each warp of a CTA owns a contiguous region of
+// kStepsPerWarp steps and carries the escape / string state across its steps
+// by itself; a tile is the kWarps regions of one CTA, and the cross-tile carry
+// (decoupled look-back) runs once per tile.
 constexpr int kThreads = 256;
-constexpr int kBytesPerThread = 32;
-constexpr int kTileBytes = kThreads * kBytesPerThread;   // 8 KiB
 constexpr int kWarps = kThreads / 32;
+constexpr int kBytesPerThread = 32;
+constexpr int kStepBytes = 32 * kBytesPerThread;          // 1 KiB, one TMA copy
+constexpr int kStepsPerWarp = 16;
+constexpr int kWarpBytes = kStepBytes * kStepsPerWarp;    // 16 KiB per warp region
+constexpr int kTileBytes = kWarpBytes * kWarps;           // 128 KiB per tile
+constexpr int kPadBytes = kStepBytes;                     // segment padding granule
 
 // Pairing: one warp matches a chunk of this many bracket records.
 constexpr int kChunk = 512;
@@ -28,7 +36,8 @@ constexpr int kTreeLevels = 6;           // min-tree levels above the chunk arra
 
 // ---- segments ---------------------------------------------------------------
 // A segment is one standard document or one JSON-Lines chunk.  Segments start
-// on tile boundaries of the device input.  Escape/string state and depth start
+// on kPadBytes boundaries of the device input and are padded to a whole number
+// of warp steps; tiles are counted per segment.  Escape/string state and depth start
 // afresh in every segment; structural and bracket counts continue from the
 // previous segment when kSegContinue is set (JSON-Lines: one merged result),
 // and restart at 0 otherwise (independent documents).
@@ -82,9 +91,16 @@ constexpr uint32_t kFlagIncl = 2u;
 
 CJ_HD Ent ent_identity(uint32_t state) { Ent e; e.st = state; e.s = 0; e.k = 0; e.d = 0; return e; }
 
+// t[i] through selects, so tables stay in registers (no local-memory indexing)
+CJ_HD Ent ent_select(const Ent t[4], uint32_t i) {
+    Ent lo = (i & 1u) ? t[1] : t[0];
+    Ent hi = (i & 1u) ? t[3] : t[2];
+    return (i & 2u) ? hi : lo;
+}
+
 // value v (state, counts, absolute depth) followed by tile table t
 CJ_HD Ent ent_apply(Ent v, const Ent t[4]) {
-    const Ent& x = t[v.st & 3u];
+    const Ent x = ent_select(t, v.st & 3u);
     Ent r;
     r.st = x.st & 3u;
     r.s = v.s + x.s;
@@ -97,8 +113,8 @@ CJ_HD Ent ent_apply(Ent v, const Ent t[4]) {
 CJ_HD void tab_compose(const Ent a[4], const Ent b[4], Ent out[4]) {
     Ent tmp[4];
     for (int s = 0; s < 4; s++) {
-        const Ent& x = a[s];
-        const Ent& y = b[x.st & 3u];
+        const Ent x = a[s];
+        const Ent y = ent_select(b, x.st & 3u);
         tmp[s].st = (y.st & 3u) | ((x.st | y.st) & 4u);
         tmp[s].s = x.s + y.s;
         tmp[s].k = x.k + y.k;
@@ -132,13 +148,14 @@ struct Classes {
     uint32_t q, bs, st, op, cl, cur, hi;
 };
 
-// Character classes of 32 bytes held as 8 little-endian words.
+// Character classes of 16 bytes held as 4 little-endian words; bit j of each
+// mask is byte j.  `hi` keeps the high bits of all bytes (non-ASCII test).
 template <bool LINES>
-CJ_HD Classes classify32(const uint32_t w[8]) {
+CJ_HD Classes classify16(const uint32_t w[4]) {
     Classes c;
     c.q = c.bs = c.st = c.op = c.cl = c.cur = c.hi = 0;
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
+    for (int k = 0; k < 4; k++) {
         uint32_t x = w[k];
         uint32_t q = eq_bytes(x, 0x22222222u);
         uint32_t b = eq_bytes(x, 0x5C5C5C5Cu);
@@ -158,6 +175,17 @@ CJ_HD Classes classify32(const uint32_t w[8]) {
         c.hi |= x;
     }
     c.hi &= 0x80808080u;
+    return c;
+}
+
+// Character classes of 32 bytes held as 8 little-endian words.
+template <bool LINES>
+CJ_HD Classes classify32(const uint32_t w[8]) {
+    Classes a = classify16<LINES>(w), b = classify16<LINES>(w + 4);
+    Classes c;
+    c.q = a.q | (b.q << 16); c.bs = a.bs | (b.bs << 16); c.st = a.st | (b.st << 16);
+    c.op = a.op | (b.op << 16); c.cl = a.cl | (b.cl << 16); c.cur = a.cur | (b.cur << 16);
+    c.hi = a.hi | b.hi;
     return c;
 }
 

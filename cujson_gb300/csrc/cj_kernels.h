@@ -18,7 +18,7 @@ struct ScanParams {
     int32_t* pair;
     uint2* brk;
     uint32_t* desc_flag;
-    uint4* desc_agg;            // 4 entries per tile
+    uint4* desc_agg;            // 4 entries per tile (tiles of kTileBytes)
     uint4* desc_incl;           // 1 entry per tile
     Ctrl* ctrl;
     SegmentOut* seg_out;
@@ -38,7 +38,10 @@ struct PairParams {
     uint32_t chunk_cap;
 };
 
-void launch_scan(const ScanParams& p, bool lines, cudaStream_t stream);
+void launch_scan(const ScanParams& p, bool lines, int grid, cudaStream_t stream);
+cudaError_t scan_configure();      // opt in to the scan kernel's dynamic shared memory
+size_t scan_smem_bytes();
+const void* scan_kernel_ptr();     // for occupancy queries
 void launch_pair(const PairParams& p, int grid, cudaStream_t stream);
 void launch_spine(const PairParams& p, int grid, cudaStream_t stream);
 

@@ -94,10 +94,11 @@ extern "C" int cjm_parse(const uint8_t* data, size_t n, int lines, const size_t*
             const int tile_len = (int)std::min<uint64_t>(kTileBytes, sg.len - tile_off);
             const bool seg_first = tin == 0, seg_last = tin + 1 == ntiles;
             const bool immediate = seg_first && !sg.cont;
-            Classes c[kThreads];
-            uint32_t cout0[kThreads];
-            bool all_bs[kThreads];
-            for (int t = 0; t < kThreads; t++) {
+            constexpr int W = kTileBytes / 32;    // 32-byte words per tile
+            static Classes c[W];
+            static uint32_t cout0[W];
+            static bool all_bs[W];
+            for (int t = 0; t < W; t++) {
                 uint32_t w[8];
                 for (int k = 0; k < 8; k++) {
                     uint32_t v = 0;
@@ -113,11 +114,11 @@ extern "C" int cjm_parse(const uint8_t* data, size_t n, int lines, const size_t*
                 all_bs[t] = c[t].bs == 0xFFFFFFFFu;
             }
             // carries (tile entered without escape), parities, masks, counts
-            uint32_t M[kThreads], own1[kThreads], own2[kThreads], own3[kThreads];
+            static uint32_t M[W], own1[W], own2[W], own3[W];
             uint32_t carry = 0, par = 0;
             bool tall = true;
             uint32_t tflip = 0, tcout = 0;
-            for (int t = 0; t < kThreads; t++) {
+            for (int t = 0; t < W; t++) {
                 uint32_t dummy;
                 uint32_t esc = escaped32(c[t].bs, carry, &dummy);
                 uint32_t rq = c[t].q & ~esc;
@@ -138,10 +139,12 @@ extern "C" int cjm_parse(const uint8_t* data, size_t n, int lines, const size_t*
                 own3[t] = __builtin_popcount(c[t].op & ~M[t]) | (__builtin_popcount(c[t].op) << 16);
             }
             uint32_t tqpar = par;
-            uint32_t tot1 = 0, tot2 = 0, tot3 = 0;
-            for (int t = 0; t < kThreads; t++) { tot1 += own1[t]; tot2 += own2[t]; tot3 += own3[t]; }
-            int32_t C0 = tot1 & 0xFFFF, Ct = tot1 >> 16, K0 = tot2 & 0xFFFF, Kt = tot2 >> 16;
-            int32_t O0 = tot3 & 0xFFFF, Ot = tot3 >> 16;
+            int32_t C0 = 0, Ct = 0, K0 = 0, Kt = 0, O0 = 0, Ot = 0;
+            for (int t = 0; t < W; t++) {
+                C0 += own1[t] & 0xFFFF; Ct += own1[t] >> 16;
+                K0 += own2[t] & 0xFFFF; Kt += own2[t] >> 16;
+                O0 += own3[t] & 0xFFFF; Ot += own3[t] >> 16;
+            }
             int32_t D0 = 2 * O0 - K0, Dt = 2 * Ot - Kt;
             std::array<Ent, 4> T;
             uint32_t Tev[4];
@@ -181,12 +184,12 @@ extern "C" int cjm_parse(const uint8_t* data, size_t n, int lines, const size_t*
             uint32_t e = Tev[entry.st & 3];
             if (seg_last && incl.d != 0) flags |= 2;
             // outputs
-            uint32_t pre1 = 0, pre2 = 0, pre3 = 0;
-            for (int t = 0; t < kThreads; t++) {
+            uint32_t pre1lo = 0, pre1hi = 0, pre2lo = 0, pre2hi = 0, pre3lo = 0, pre3hi = 0;
+            for (int t = 0; t < W; t++) {
                 uint32_t Mf = M[t] ^ (e ? 0xFFFFFFFFu : 0u);
                 uint32_t stm = c[t].st & ~Mf, brm = (c[t].op | c[t].cl) & ~Mf, opm = c[t].op & ~Mf;
-                uint32_t p1lo = pre1 & 0xFFFF, p1hi = pre1 >> 16, p2lo = pre2 & 0xFFFF, p2hi = pre2 >> 16;
-                uint32_t p3lo = pre3 & 0xFFFF, p3hi = pre3 >> 16;
+                uint32_t p1lo = pre1lo, p1hi = pre1hi, p2lo = pre2lo, p2hi = pre2hi;
+                uint32_t p3lo = pre3lo, p3hi = pre3hi;
                 uint32_t sidx = entry.s + (e ? p1hi - p1lo : p1lo);
                 uint32_t kidx = entry.k + (e ? p2hi - p2lo : p2lo);
                 int32_t d0 = 2 * (int32_t)p3lo - (int32_t)p2lo, dt = 2 * (int32_t)p3hi - (int32_t)p2hi;
@@ -209,7 +212,9 @@ extern "C" int cjm_parse(const uint8_t* data, size_t n, int lines, const size_t*
                     }
                     sidx++;
                 }
-                pre1 += own1[t]; pre2 += own2[t]; pre3 += own3[t];
+                pre1lo += own1[t] & 0xFFFF; pre1hi += own1[t] >> 16;
+                pre2lo += own2[t] & 0xFFFF; pre2hi += own2[t] >> 16;
+                pre3lo += own3[t] & 0xFFFF; pre3hi += own3[t] >> 16;
             }
         }
     }

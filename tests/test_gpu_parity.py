@@ -22,11 +22,10 @@ def test_small(ctx, oracle, doc):
     assert_same(res, oracle.parse(doc))
 
 
-@pytest.mark.parametrize("n", [1, 2, 31, 32, 33, 255, 8191, 8192, 8193, 16384, 65537, 300001])
+@pytest.mark.parametrize("n", [1, 2, 31, 32, 33, 255, 8191, 8192, 8193, 16384, 65537, 131071,
+                               131072, 131073, 300001, 1 << 21])
 def test_sizes(cj, ctx, oracle, n):
-    d = cj.synth_document(n, max(n, 2))[:n] if n >= 2 else np.frombuffer(b"1", np.uint8)
-    if n >= 2:
-        d = cj.synth_document(n, n)
+    d = cj.synth_document(n, n) if n >= 2 else np.frombuffer(b"1", np.uint8)
     st, res = ctx.try_parse(d)
     ref = oracle.parse(d)
     assert st == 0 and ref.flags == 0
@@ -61,11 +60,11 @@ def test_deep(cj, ctx, oracle, depth):
     assert res.max_depth == depth
 
 
-@pytest.mark.parametrize("seed", range(24))
+@pytest.mark.parametrize("seed", range(32))
 def test_random_bytes(cj, ctx, oracle, seed):
     rng = np.random.default_rng(seed)
     alphabet = np.frombuffer(b'[]{}:,"\\ ab\n', np.uint8)
-    n = int(rng.integers(1, 60000))
+    n = int(rng.integers(1, 60000)) if seed < 16 else int(rng.integers(100000, 700000))
     d = alphabet[rng.integers(0, alphabet.size, n)]
     lines = bool(seed & 1)
     st, res = ctx.try_parse(d, lines=lines)
@@ -106,10 +105,14 @@ def test_utf8_cases(ctx, oracle):
     for body, ok in [("é€😀".encode(), True), (b"\xc0\x80", False), (b"\xe0\x80\x80", False),
                      (b"\xed\xa0\x80", False), (b"\xf5\x80\x80\x80", False), (b"\xe2\x82", False),
                      (b"\x80", False), (b"\xc3\x41", False)]:
-        for pad in (0, 29, 30, 31, 8190):
+        for pad in (0, 1, 2, 29, 30, 31, 8189, 8190, 8191, 131069, 131070, 131071):
             doc = b"[" + b" " * pad + b'"' + body + b'"]'
             st, _ = ctx.try_parse(doc)
             assert (st == 0) == ok, (body, pad, st)
+            # the same bytes as the very end of the input
+            doc = b'[""]' + b" " * pad + body
+            st, _ = ctx.try_parse(doc)
+            assert (st == 0) == (ok and oracle.utf8_valid(doc)), (body, pad, st)
 
 
 def test_repeat_deterministic(cj, ctx):
