@@ -20,12 +20,12 @@ namespace cj {
 // kStepsPerWarp steps and carries the escape / string state across its steps
 // by itself; a tile is the kWarps regions of one CTA, and the cross-tile carry
 // (decoupled look-back) runs once per tile.
-constexpr int kThreads = 256;
+constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
 constexpr int kBytesPerThread = 32;
 constexpr int kStepBytes = 32 * kBytesPerThread;          // 1 KiB, one TMA copy
-constexpr int kStepsPerWarp = 16;
-constexpr int kWarpBytes = kStepBytes * kStepsPerWarp;    // 16 KiB per warp region
+constexpr int kStepsPerWarp = 8;
+constexpr int kWarpBytes = kStepBytes * kStepsPerWarp;    // 8 KiB per warp region
 constexpr int kTileBytes = kWarpBytes * kWarps;           // 128 KiB per tile
 constexpr int kPadBytes = kStepBytes;                     // segment padding granule
 
@@ -150,22 +150,34 @@ struct Classes {
 
 // Character classes of 16 bytes held as 4 little-endian words; bit j of each
 // mask is byte j.  `hi` keeps the high bits of all bytes (non-ASCII test).
+// Each equality test is a zero-byte test on (low 7 bits ^ pattern) + 0x7F per
+// byte (the high bit of the sum is set unless the byte matched), combined with
+// the byte's own high bit; '[' and '{' (and ']' and '}') share one test on the
+// byte with bit 5 cleared.
 template <bool LINES>
 CJ_HD Classes classify16(const uint32_t w[4]) {
+    const uint32_t H = 0x80808080u, K = 0x7F7F7F7Fu;
     Classes c;
     c.q = c.bs = c.st = c.op = c.cl = c.cur = c.hi = 0;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        uint32_t x = w[k];
-        uint32_t q = eq_bytes(x, 0x22222222u);
-        uint32_t b = eq_bytes(x, 0x5C5C5C5Cu);
-        uint32_t y = x & 0xDFDFDFDFu;              // '{' -> '[', '}' -> ']'
-        uint32_t o = eq_bytes(y, 0x5B5B5B5Bu);
-        uint32_t cl = eq_bytes(y, 0x5D5D5D5Du);
-        uint32_t s = o | cl | eq_bytes(x, 0x3A3A3A3Au) | eq_bytes(x, 0x2C2C2C2Cu);
-        if (LINES) s |= eq_bytes(x, 0x0A0A0A0Au);
-        uint32_t cu = (x << 2) & (o | cl);         // bit 5 (curly) -> bit 7
-        int sh = 4 * k;
+        const uint32_t x = w[k];
+        const uint32_t xl = x & K, yl = x & 0x5F5F5F5Fu;
+        const uint32_t tq = (xl ^ 0x22222222u) + K;
+        const uint32_t tb = (xl ^ 0x5C5C5C5Cu) + K;
+        const uint32_t to = (yl ^ 0x5B5B5B5Bu) + K;
+        const uint32_t tc = (yl ^ 0x5D5D5D5Du) + K;
+        const uint32_t tn = (xl ^ 0x3A3A3A3Au) + K;
+        const uint32_t tm = (xl ^ 0x2C2C2C2Cu) + K;
+        uint32_t tall = to & tc & tn & tm;
+        if (LINES) tall &= (xl ^ 0x0A0A0A0Au) + K;
+        const uint32_t q = ~(tq | x) & H;
+        const uint32_t b = ~(tb | x) & H;
+        const uint32_t o = ~(to | x) & H;
+        const uint32_t cl = ~(tc | x) & H;
+        const uint32_t s = ~(tall | x) & H;
+        const uint32_t cu = (x << 2) & (o | cl);   // bit 5 (curly) -> bit 7
+        const int sh = 4 * k;
         c.q |= gather4(q) << sh;
         c.bs |= gather4(b) << sh;
         c.st |= gather4(s) << sh;
@@ -174,7 +186,7 @@ CJ_HD Classes classify16(const uint32_t w[4]) {
         c.cur |= gather4(cu) << sh;
         c.hi |= x;
     }
-    c.hi &= 0x80808080u;
+    c.hi &= H;
     return c;
 }
 
@@ -207,6 +219,62 @@ CJ_HD uint32_t escaped32(uint32_t bs, uint32_t carry, uint32_t* cout) {
     uint32_t odd_span = (tl ^ b) ^ os;     // s+1 .. s+L of odd-start runs
     uint32_t span = b << 1;                // s+1 .. s+L of every run
     return (span & (ODD ^ odd_span)) | carry;
+}
+
+// (hi:lo << s) >> 32 for 0 < s < 32: the bytes of `hi` moved up by s/8 byte
+// positions, filled from the top of `lo` (the word before it)
+CJ_HD uint32_t funnel_l(uint32_t lo, uint32_t hi, int s) {
+#ifdef __CUDA_ARCH__
+    return __funnelshift_l(lo, hi, s);
+#else
+    return (hi << s) | (lo >> (32 - s));
+#endif
+}
+
+// RFC 3629 validity of one lane's 32 bytes (8 little-endian words, bytes past
+// the end of the segment already zeroed), given the 4 bytes before them in
+// `pw`.  Works on byte-form masks (bit 7 of each byte): leads >= C0, >= E0,
+// >= F0, and continuation bytes (10xxxxxx).  A lead expects continuation bytes
+// at its next 1, 2 or 3 positions (funnel shifts carry that across words and
+// from `pw`); the expected positions must be exactly the continuation bytes.
+// C0, C1 and F5..FF are rejected, and the byte after E0 / ED / F0 / F4 is
+// range-checked (overlong and surrogate forms, code points above U+10FFFF).
+// A sequence still open at the end of the 32 bytes is the next lane's to check,
+// unless the segment ends there (`seg_end`).  Returns nonzero on an error.
+CJ_HD uint32_t utf8_errors(const uint32_t w[8], uint32_t pw, bool seg_end) {
+    const uint32_t H = 0x80808080u;
+    uint32_t c2p = pw & (pw << 1) & H, c3p = c2p & (pw << 2), c4p = c3p & (pw << 3);
+    uint32_t err = 0, any3 = c3p;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const uint32_t x = w[k];
+        const uint32_t c2 = x & (x << 1) & H;
+        const uint32_t c3 = c2 & (x << 2);
+        const uint32_t c4 = c3 & (x << 3);
+        const uint32_t cont = x & ~(x << 1) & H;
+        const uint32_t E = funnel_l(c2p, c2, 8) | funnel_l(c3p, c3, 16) | funnel_l(c4p, c4, 24);
+        err |= E ^ cont;
+        err |= c2 & ~c3 & ~((x & 0x1E1E1E1Eu) + 0x7F7F7F7Fu);      // C0, C1
+        err |= c4 & (((x & 0x0F0F0F0Fu) + 0x0B0B0B0Bu) << 3);      // F5..FF
+        any3 |= c3;
+        c2p = c2; c3p = c3; c4p = c4;
+    }
+    if (seg_end) err |= (c2p >> 24) | (c3p >> 16) | (c4p >> 8);
+    if (any3) {
+        uint32_t p = pw;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const uint32_t x = w[k];
+            const uint32_t pb = funnel_l(p, x, 8);                   // byte before each position
+            const uint32_t b5 = x << 2, b4 = x << 3;                 // bits 5 / 4 -> bit 7
+            err |= eq_bytes(pb, 0xE0E0E0E0u) & ~b5;                  // E0 then < A0
+            err |= eq_bytes(pb, 0xEDEDEDEDu) & b5;                   // ED then >= A0
+            err |= eq_bytes(pb, 0xF0F0F0F0u) & ~(b5 | b4);           // F0 then < 90
+            err |= eq_bytes(pb, 0xF4F4F4F4u) & (b5 | b4);            // F4 then >= 90
+            p = x;
+        }
+    }
+    return err & H;
 }
 
 // inclusive prefix XOR over the bits of x

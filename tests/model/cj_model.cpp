@@ -109,7 +109,17 @@ extern "C" int cjm_parse(const uint8_t* data, size_t n, int lines, const size_t*
                     w[k] = v;
                 }
                 c[t] = lines ? classify32<true>(w) : classify32<false>(w);
-                if (c[t].hi && !utf8_ok32(sb, sg.len, tile_off + t * 32)) flags |= 1;
+                {
+                    // previous 4 bytes of the segment (zero before its start)
+                    uint32_t pw = 0;
+                    const int64_t o0 = (int64_t)tile_off + t * 32;
+                    for (int b = 0; b < 4; b++) {
+                        const int64_t o = o0 - 4 + b;
+                        if (o >= 0 && (uint64_t)o < sg.len) pw |= (uint32_t)sb[o] << (8 * b);
+                    }
+                    const bool seg_end = (uint64_t)(o0 + 32) >= sg.len;
+                    if ((uint64_t)o0 < sg.len && utf8_errors(w, pw, seg_end)) flags |= 1;
+                }
                 escaped32(c[t].bs, 0, &cout0[t]);
                 all_bs[t] = c[t].bs == 0xFFFFFFFFu;
             }

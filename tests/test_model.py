@@ -96,3 +96,48 @@ def test_corrupt(cj, oracle, model):
         d = cj.synth_document(42 + kind, 50000)
         assert cj.synth_corrupt(d, kind, kind)
         check(model, oracle, d)
+
+
+def _utf8_soup(rng, n):
+    """Mostly well-formed UTF-8 with sprinkled defects, as raw bytes."""
+    out = bytearray()
+    pieces = ["a", " ", "é", "€", "😀", "ߺ", "ࠀ", "￿", "\U00010000", "\U0010ffff", "퟿"]
+    bad = [b"\xc0\x80", b"\xc1\xbf", b"\xe0\x80\x80", b"\xe0\x9f\xbf", b"\xed\xa0\x80", b"\xed\xbf\xbf",
+           b"\xf0\x80\x80\x80", b"\xf0\x8f\xbf\xbf", b"\xf4\x90\x80\x80", b"\xf5\x80\x80\x80", b"\xff",
+           b"\x80", b"\xbf", b"\xc3", b"\xe2\x82", b"\xf0\x9f\x98", b"\xc3\x41", b"\xe2\x41\x82"]
+    while len(out) < n:
+        if rng.random() < 0.02:
+            out += bad[int(rng.integers(len(bad)))]
+        else:
+            out += pieces[int(rng.integers(len(pieces)))].encode("utf-8", "surrogatepass")
+    return bytes(out[:n])
+
+
+@pytest.mark.parametrize("seed", range(60))
+def test_utf8_fuzz(oracle, model, seed):
+    rng = np.random.default_rng(1000 + seed)
+    n = int(rng.integers(1, 3000)) if seed < 40 else int(rng.integers(120000, 140000))
+    body = _utf8_soup(rng, n)
+    if seed % 3 == 0:
+        # sometimes cut the soup so the input ends inside a sequence
+        body = body[: max(1, len(body) - int(rng.integers(0, 3)))]
+    doc = b'["' + body.replace(b'"', b'x').replace(b'\\', b'x') + b'"]'
+    p, q, fl = run_model(model, doc)
+    assert bool(fl & 1) == (not oracle.utf8_valid(doc)), seed
+
+
+def test_utf8_dense_short(oracle, model):
+    # dense high bytes: every lead/continuation/invalid byte pattern near word,
+    # lane and input-end boundaries
+    rng = np.random.default_rng(77)
+    vals = np.array(list(range(0x80, 0x100)) + [0x41, 0x20], dtype=np.uint8)
+    for i in range(1500):
+        n = int(rng.integers(1, 14))
+        body = bytes(vals[rng.integers(0, vals.size, n)])
+        pad = int(rng.integers(0, 40))
+        doc = b"[" + b" " * pad + b'"' + body + b'"]'
+        _, _, fl = run_model(model, doc)
+        assert bool(fl & 1) == (not oracle.utf8_valid(doc)), (body, pad)
+        doc2 = b'[""]' + b" " * pad + body        # the bytes end the input
+        _, _, fl = run_model(model, doc2)
+        assert bool(fl & 1) == (not oracle.utf8_valid(doc2)), (body, pad)
