@@ -20,8 +20,8 @@ namespace cj {
 // kStepsPerWarp steps and carries the escape / string state across its steps
 // by itself; a tile is the kWarps regions of one CTA, and the cross-tile carry
 // (decoupled look-back) runs once per tile.
-constexpr int kThreads = 512;
-constexpr int kWarps = kThreads / 32;
+constexpr int kWarps = 16;                                // classifying warps per CTA
+constexpr int kThreads = (kWarps + 1) * 32;               // + one coordinator warp
 constexpr int kBytesPerThread = 32;
 constexpr int kStepBytes = 32 * kBytesPerThread;          // 1 KiB, one TMA copy
 constexpr int kStepsPerWarp = 8;

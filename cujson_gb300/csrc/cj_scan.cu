@@ -1,13 +1,14 @@
 // cj_scan.cu -- the single-pass structural scan (persistent, TMA-staged,
 // warp-independent, software-pipelined across tiles).
 //
-// A persistent grid of CTAs (one per SM, 16 warps) takes 128 KiB tiles in
-// document order from an atomic ticket.  Each warp owns a contiguous 8 KiB
-// region of a tile and works through it in 1 KiB steps (32 lanes x 32 bytes)
-// staged in its own 3-deep shared-memory ring by bulk TMA copies
-// (cp.async.bulk completing on per-warp mbarriers).
+// A persistent grid of CTAs (one per SM: 16 classifying warps and one
+// coordinator warp) takes 128 KiB tiles in document order from an atomic
+// ticket.  Each classifying warp owns a contiguous 8 KiB region of a tile and
+// works through it in 1 KiB steps (32 lanes x 32 bytes) staged in its own
+// 3-deep shared-memory ring by bulk TMA copies (cp.async.bulk completing on
+// per-warp mbarriers).
 //
-//   A. (tile t) every warp, on its own: builds the quote, backslash,
+//   A. (tile t) every classifying warp, on its own: builds the quote, backslash,
 //      structural and bracket bitmaps of each lane's 32 bytes, validates UTF-8
 //      (byte-parallel, only on steps holding non-ASCII bytes), resolves
 //      escapes and the in-string mask assuming its region is entered outside
@@ -15,17 +16,21 @@
 //      shuffles, step to step in registers), keeps the masks in shared memory
 //      and sums the counts into a transfer table: for each of the 4 entry
 //      states (escape, in-string), the exit state, structural count, bracket
-//      count and depth delta.  Warp 0 composes the 16 warp tables into the
-//      tile's table and publishes it (decoupled look-back descriptor).
-//   B. (tile t-1) warp 0 finds the previous tile's exclusive prefix by
+//      count and depth delta.
+//   B. (tile t, coordinator warp, while the classifying warps run phase A of
+//      tile t+1) composes the 16 warp tables into the tile's table, publishes
+//      it (decoupled look-back descriptor), finds the tile's exclusive prefix by
 //      look-back (32 predecessors per step, loaded in parallel and composed
-//      with an ordered shuffle reduction), publishes its inclusive value, and
-//      derives each warp's entry value.  Phase A of tile t has given every
-//      predecessor that much time to publish, so the content-dependent spread
-//      of phase-A times is absorbed instead of stalling every CTA.
-//   C. (tile t-1) every warp replays its masks with its entry value and writes
-//      1-based structural positions, a zeroed pair row and one bracket record
-//      (structural index, level, open flag, brace or bracket) per bracket.
+//      with an ordered shuffle reduction), publishes the inclusive value and
+//      derives each warp's entry value.
+//   C. (tile t, after phase A of tile t+1) every classifying warp replays its
+//      masks with its entry value and writes 1-based structural positions, a
+//      zeroed pair row and one bracket record (structural index, level, open
+//      flag, brace or bracket) per bracket.
+// Hand-offs between the two roles use named barriers (bar.arrive / bar.sync),
+// one pair per mask slot, so a barrier is never re-armed before its previous
+// phase completed; the look-back never stalls the classifying warps unless it
+// takes longer than a whole phase A.
 //
 // This replaces the reference's stage 1 (checkAscii + checkUTF8,
 // cujson/parse_standard_json.cu:186-327) and stage 2 (bitMapCreatorSimd :446,
@@ -91,6 +96,19 @@ __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
 
 __device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// named barriers: 0 is __syncthreads; 1-2 "phase A done" per slot, 3-4
+// "prefix ready" per slot, 5 the classifying warps among themselves
+constexpr uint32_t kBarA = 1, kBarP = 3, kBarCompute = 5;
+constexpr uint32_t kAll = kThreads, kCompute = kWarps * 32;
+
+__device__ __forceinline__ void bar_sync(uint32_t id, uint32_t n) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
+__device__ __forceinline__ void bar_arrive(uint32_t id, uint32_t n) {
+    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
 }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -462,89 +480,85 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
     extern __shared__ __align__(128) uint8_t smem_raw[];
     Smem& S = *reinterpret_cast<Smem*>(smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    WarpSmem& W = S.w[warp];
-    const uint32_t lt = lanemask_lt();
     const uint32_t ep = P.epoch & 0x3FFFFFFFu;
 
-    if (lane == 0) {
-        for (int s = 0; s < kStages; s++) mbar_init(&W.mbar[s], 1);
+    if (warp < kWarps && lane == 0) {
+        for (int s = 0; s < kStages; s++) mbar_init(&S.w[warp].mbar[s], 1);
         fence_mbar_init();
     }
-    if (tid == 0) { S.slot[0].tile = kNoTile; S.slot[1].tile = kNoTile; }
     __syncthreads();
-    uint32_t parity = 0;   // bit s: phase parity to wait for on stage s
-    int cur = 0;
 
-    while (true) {
-        if (tid == 0) S.ticket = atomicAdd(&P.ctrl->tile_ticket, 1u);
-        __syncthreads();
-        const uint32_t tile = S.ticket;
-        const bool have_cur = tile < P.n_tiles;
-        Slot& sc = S.slot[cur];
-        Slot& sp = S.slot[cur ^ 1];
-        // read once here: the slot's fields are only rewritten after the next
-        // iteration's ticket barrier
-        const uint32_t prev_tile = sp.tile;
-        const bool have_prev = prev_tile != kNoTile;
-
-        // ---- A: the new tile ------------------------------------------------------
-        TileGeom gc;
-        if (have_cur) {
-            gc = tile_geom(P, tile);
-            phase_a<LINES>(P, gc, W, sc, parity, warp, lane, lt);
-        }
-        __syncthreads();
-
-        // ---- publish the new tile, resolve the previous one (warp 0) ---------------
-        if (warp == 0) {
-            if (have_cur) {
-                Ent T[4];
-                tab_identity(T);
+    if (warp == kWarps) {
+        // ---- coordinator: publish, look back, derive entries -------------------------
+        int s = 0;
+        while (true) {
+            bar_sync(kBarA + s, kAll);
+            Slot& sl = S.slot[s];
+            const uint32_t tile = sl.tile;
+            if (tile == kNoTile) break;
+            const TileGeom g = tile_geom(P, tile);
+            Ent T[4];
+            tab_identity(T);
 #pragma unroll 1
-                for (int v = 0; v < kWarps; v++) tab_compose(T, sc.wtab[v], T);
-                if (gc.seg_first) {
-                    // a segment starts outside strings and escapes, at depth 0
-                    const Ent t0 = T[0];
+            for (int v = 0; v < kWarps; v++) tab_compose(T, sl.wtab[v], T);
+            if (g.seg_first) {
+                // a segment starts outside strings and escapes, at depth 0
+                const Ent t0 = T[0];
 #pragma unroll
-                    for (int s = 0; s < 4; s++) { T[s] = t0; T[s].st |= 4u; }
-                }
+                for (int k = 0; k < 4; k++) { T[k] = t0; T[k].st |= 4u; }
+            }
+            if (lane == 0) {
+#pragma unroll
+                for (int k = 0; k < 4; k++) sl.T[k] = T[k];
+            }
+            __syncwarp();
+            if (g.immediate) {
+                if (lane == 0) finish_prefix(P, g, sl, ent_identity(0), ep);
+            } else {
                 if (lane == 0) {
 #pragma unroll
-                    for (int s = 0; s < 4; s++) sc.T[s] = T[s];
-                    sc.tile = tile;
-                    sc.resolved = 0;
-                    if (gc.immediate) {
-                        finish_prefix(P, gc, sc, ent_identity(0), ep);
-                    } else {
-#pragma unroll
-                        for (int s = 0; s < 4; s++)
-                            __stcg(P.desc_agg + (size_t)tile * 4 + s,
-                                   make_uint4(T[s].st, T[s].s, T[s].k, (uint32_t)T[s].d));
-                        __threadfence();
-                        st_release(P.desc_flag + tile, (ep << 2) | kFlagAgg);
-                    }
+                    for (int k = 0; k < 4; k++)
+                        __stcg(P.desc_agg + (size_t)tile * 4 + k,
+                               make_uint4(T[k].st, T[k].s, T[k].k, (uint32_t)T[k].d));
+                    __threadfence();
+                    st_release(P.desc_flag + tile, (ep << 2) | kFlagAgg);
                 }
+                const Ent excl = look_back(P, tile, ep, lane);
+                if (lane == 0) finish_prefix(P, g, sl, excl, ep);
             }
-            if (have_prev) {
-                __syncwarp();
-                if (!sp.resolved) {
-                    const TileGeom gp = tile_geom(P, prev_tile);
-                    const Ent excl = look_back(P, prev_tile, ep, lane);
-                    if (lane == 0) finish_prefix(P, gp, sp, excl, ep);
-                }
-            }
+            __syncwarp();
+            bar_arrive(kBarP + s, kAll);
+            s ^= 1;
         }
-        __syncthreads();
+        return;
+    }
 
-        // ---- C: the previous tile's outputs --------------------------------------------
-        if (have_prev) {
-            const TileGeom gp = tile_geom(P, prev_tile);
-            phase_c(P, gp, sp, warp, lane);
+    // ---- classifying warps -----------------------------------------------------------
+    WarpSmem& W = S.w[warp];
+    const uint32_t lt = lanemask_lt();
+    uint32_t parity = 0;   // bit s: phase parity to wait for on stage s
+    int s = 0;
+    uint32_t prev_tile = kNoTile;
+    while (true) {
+        if (tid == 0) {
+            const uint32_t t = atomicAdd(&P.ctrl->tile_ticket, 1u);
+            S.slot[s].tile = (t < P.n_tiles) ? t : kNoTile;
         }
-        if (!have_cur) break;
-        // slot `cur` now holds the previous tile; the next ticket's barrier
-        // orders this iteration's reads of the other slot before its reuse
-        cur ^= 1;
+        bar_sync(kBarCompute, kCompute);
+        const uint32_t tile = S.slot[s].tile;
+        if (tile != kNoTile) {
+            const TileGeom g = tile_geom(P, tile);
+            phase_a<LINES>(P, g, W, S.slot[s], parity, warp, lane, lt);
+        }
+        bar_arrive(kBarA + s, kAll);
+        if (prev_tile != kNoTile) {
+            bar_sync(kBarP + (s ^ 1), kAll);
+            const TileGeom g = tile_geom(P, prev_tile);
+            phase_c(P, g, S.slot[s ^ 1], warp, lane);
+        }
+        if (tile == kNoTile) break;
+        prev_tile = tile;
+        s ^= 1;
     }
 }
 
