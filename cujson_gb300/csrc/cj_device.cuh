@@ -144,23 +144,42 @@ CJ_HD uint32_t eq_bytes(uint32_t w, uint32_t pat) {
 // nibble without carries because the partial products never overlap)
 CJ_HD uint32_t gather4(uint32_t m) { return (m * 0x00204081u) >> 28; }
 
+// a * b + c on the multiply-add pipe (keeps the integer ALU pipe, which bounds
+// the classification, free for the logic operations)
+CJ_HD uint32_t mad_u32(uint32_t a, uint32_t b, uint32_t c) {
+#ifdef __CUDA_ARCH__
+    uint32_t d;
+    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+#else
+    return a * b + c;
+#endif
+}
+
+// acc + (gathered nibble of m << sh): the multiply and the placement run on
+// the multiply-add pipe, only the shift on the ALU
+CJ_HD uint32_t gather4_into(uint32_t m, int sh, uint32_t acc) {
+    return mad_u32(gather4(m), 1u << sh, acc);
+}
+
 struct Classes {
     uint32_t q, bs, st, op, cl, cur, hi;
 };
 
-// Character classes of 16 bytes held as 4 little-endian words; bit j of each
+// Character classes of N*4 bytes held as N little-endian words; bit j of each
 // mask is byte j.  `hi` keeps the high bits of all bytes (non-ASCII test).
 // Each equality test is a zero-byte test on (low 7 bits ^ pattern) + 0x7F per
 // byte (the high bit of the sum is set unless the byte matched), combined with
 // the byte's own high bit; '[' and '{' (and ']' and '}') share one test on the
-// byte with bit 5 cleared.
-template <bool LINES>
-CJ_HD Classes classify16(const uint32_t w[4]) {
+// byte with bit 5 cleared.  The per-byte results (bit 7 of each byte) are
+// gathered into bit masks by multiplication (gather4_into).
+template <bool LINES, int N>
+CJ_HD Classes classify_words(const uint32_t* w) {
     const uint32_t H = 0x80808080u, K = 0x7F7F7F7Fu;
     Classes c;
     c.q = c.bs = c.st = c.op = c.cl = c.cur = c.hi = 0;
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
+    for (int k = 0; k < N; k++) {
         const uint32_t x = w[k];
         const uint32_t xl = x & K, yl = x & 0x5F5F5F5Fu;
         const uint32_t tq = (xl ^ 0x22222222u) + K;
@@ -178,27 +197,33 @@ CJ_HD Classes classify16(const uint32_t w[4]) {
         const uint32_t s = ~(tall | x) & H;
         const uint32_t cu = (x << 2) & (o | cl);   // bit 5 (curly) -> bit 7
         const int sh = 4 * k;
-        c.q |= gather4(q) << sh;
-        c.bs |= gather4(b) << sh;
-        c.st |= gather4(s) << sh;
-        c.op |= gather4(o) << sh;
-        c.cl |= gather4(cl) << sh;
-        c.cur |= gather4(cu) << sh;
+        c.q = gather4_into(q, sh, c.q);
+        c.bs = gather4_into(b, sh, c.bs);
+        c.st = gather4_into(s, sh, c.st);
+        c.op = gather4_into(o, sh, c.op);
+        c.cl = gather4_into(cl, sh, c.cl);
+        c.cur = gather4_into(cu, sh, c.cur);
         c.hi |= x;
     }
     c.hi &= H;
     return c;
 }
 
+template <bool LINES>
+CJ_HD Classes classify16(const uint32_t w[4]) { return classify_words<LINES, 4>(w); }
+
 // Character classes of 32 bytes held as 8 little-endian words.
 template <bool LINES>
-CJ_HD Classes classify32(const uint32_t w[8]) {
-    Classes a = classify16<LINES>(w), b = classify16<LINES>(w + 4);
-    Classes c;
-    c.q = a.q | (b.q << 16); c.bs = a.bs | (b.bs << 16); c.st = a.st | (b.st << 16);
-    c.op = a.op | (b.op << 16); c.cl = a.cl | (b.cl << 16); c.cur = a.cur | (b.cur << 16);
-    c.hi = a.hi | b.hi;
-    return c;
+CJ_HD Classes classify32(const uint32_t w[8]) { return classify_words<LINES, 8>(w); }
+
+// carry out of a 32-byte word entered without escape: whether its trailing
+// backslash run has odd length (not meaningful for an all-backslash word)
+CJ_HD uint32_t escape_cout(uint32_t bs) {
+#ifdef __CUDA_ARCH__
+    return (uint32_t)__clz(~bs) & 1u;
+#else
+    return (uint32_t)(bs == 0xFFFFFFFFu ? 0 : __builtin_clz(~bs)) & 1u;
+#endif
 }
 
 // Escaped-character mask of one 32-byte word.  `carry` = 1 when byte 0 is

@@ -251,11 +251,7 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileGeom& g, 
         if (16 > valid) mask_chunk(lo, valid);
         if (32 > valid) mask_chunk(hi, valid - 16);
         const uint32_t w[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
-        const Classes ca = classify16<LINES>(w), cb = classify16<LINES>(w + 4);
-        Classes c;
-        c.q = ca.q | (cb.q << 16); c.bs = ca.bs | (cb.bs << 16); c.st = ca.st | (cb.st << 16);
-        c.op = ca.op | (cb.op << 16); c.cl = ca.cl | (cb.cl << 16); c.cur = ca.cur | (cb.cur << 16);
-        c.hi = ca.hi | cb.hi;
+        const Classes c = classify32<LINES>(w);
 
         // UTF-8, byte-parallel, on steps that hold a non-ASCII byte
         {
@@ -270,8 +266,7 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileGeom& g, 
         }
 
         // escapes: carry from the nearest earlier lane that is not all backslashes
-        uint32_t cout0;
-        (void)escaped32(c.bs, 0u, &cout0);
+        const uint32_t cout0 = escape_cout(c.bs);
         const bool all_bs = (c.bs == FULL);
         const uint32_t nonall = __ballot_sync(FULL, !all_bs);
         const uint32_t prior = nonall & lt;
@@ -436,6 +431,7 @@ __device__ __forceinline__ void phase_c(const ScanParams& P, const TileGeom& g, 
         const uint32_t (&m)[kMaskFields][32] = sl.masks[warp][j];
         const uint32_t Mf = m[4][lane] ^ flip;
         uint32_t stm = m[0][lane] & ~Mf;
+        if (!__any_sync(FULL, stm)) continue;      // nothing outside strings in this step
         const uint32_t brm = m[1][lane] & ~Mf;
         const uint32_t opm = m[2][lane] & ~Mf;
         const uint32_t curm = m[3][lane];
