@@ -110,6 +110,13 @@ _SIGNATURES = {
     "cj_context_span_ms": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
     "cj_host_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
     "cj_host_free": (None, [ctypes.c_void_p]),
+    "cj_load_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p),
+                                    ctypes.POINTER(ctypes.c_size_t)]),
+    "cj_plan_lines_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
+                                           ctypes.c_void_p]),
+    "cj_plan_lines_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
+                                           ctypes.c_void_p, ctypes.c_size_t,
+                                           ctypes.POINTER(ctypes.c_size_t)]),
     "cj_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "cj_last_status": (ctypes.c_int, []),
     "cj_set_last_status": (None, [ctypes.c_int]),
@@ -365,6 +372,25 @@ class PinnedBuffer:
             self.close()
         except Exception:
             pass
+
+
+def plan_lines_count(data, chunk_count: int) -> List[int]:
+    buf = _u8(data)
+    out = np.zeros(chunk_count, dtype=np.uint64)
+    _check(lib().cj_plan_lines_count(buf.ctypes.data if buf.size else None, buf.size, chunk_count,
+                                     out.ctypes.data), "plan_lines_count")
+    return [int(x) for x in out]
+
+
+def plan_lines_bytes(data, chunk_bytes: int) -> List[int]:
+    buf = _u8(data)
+    n = ctypes.c_size_t()
+    _check(lib().cj_plan_lines_bytes(buf.ctypes.data if buf.size else None, buf.size, chunk_bytes,
+                                     None, 0, ctypes.byref(n)), "plan_lines_bytes")
+    out = np.zeros(max(1, n.value), dtype=np.uint64)
+    _check(lib().cj_plan_lines_bytes(buf.ctypes.data if buf.size else None, buf.size, chunk_bytes,
+                                     out.ctypes.data, out.size, ctypes.byref(n)), "plan_lines_bytes")
+    return [int(x) for x in out[: n.value]]
 
 
 # ---------------------------------------------------------------------------

@@ -149,6 +149,21 @@ cj_status cj_context_span_ms(cj_context* ctx, double* ms);
 void* cj_host_alloc(size_t bytes);
 void  cj_host_free(void* p);
 
+/* ---- loaders and JSON-Lines chunk planning ----------------------------------
+ * cj_load_file reads a whole file into pinned host memory (free it with
+ * cj_host_free or cudaFreeHost); replaces loadJSON, cujson/load_file.cu:7.
+ * cj_plan_lines_count splits a buffer into `chunk_count` chunks of whole lines
+ * (replaces loadJSONLines_chunkCount, cujson/load_file.cu:38);
+ * cj_plan_lines_bytes closes a chunk before the line that would make it
+ * exceed `chunk_bytes` (replaces loadJSONLines_chunkSizeBytes /
+ * _chunkSizeMegaBytes, cujson/load_file.cu:109, :182).  With chunk_sizes ==
+ * NULL it only counts the chunks. */
+cj_status cj_load_file(const char* path, uint8_t** data, size_t* size);
+cj_status cj_plan_lines_count(const uint8_t* data, size_t size, size_t chunk_count,
+                              size_t* chunk_sizes);
+cj_status cj_plan_lines_bytes(const uint8_t* data, size_t size, size_t chunk_bytes,
+                              size_t* chunk_sizes, size_t cap, size_t* n_chunks);
+
 const char* cj_status_string(int status);
 /* Status of the calling thread's last drop-in parse (parse_standard_json /
  * parse_json_lines return an empty result on failure, as the reference's
