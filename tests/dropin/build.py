@@ -31,3 +31,19 @@ def build(force: bool = False) -> dict:
 
 if __name__ == "__main__":
     print(build(force=True))
+
+
+def build_example(libdir: Path, force: bool = False) -> Path:
+    """tests/dropin/example_parse.cu against include/cujson/ and libcujson_gb300."""
+    BUILD.mkdir(parents=True, exist_ok=True)
+    exe = BUILD / "example_parse"
+    src = HERE / "example_parse.cu"
+    deps = [src, *HEADERS, REPO / "include" / "cujson" / "cujson_api.h", REPO / "include" / "cujson" / "cujson.h"]
+    if force or not exe.exists() or exe.stat().st_mtime < max(p.stat().st_mtime for p in deps):
+        cmd = ["nvcc", "-std=c++17", "-O2", "-gencode", "arch=compute_103a,code=sm_103a",
+               f"-I{REPO / 'include'}", str(src), "-o", str(exe), f"-L{libdir}", "-lcujson_gb300",
+               "-Xlinker", f"-rpath,{libdir}"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"example build failed:\n{r.stderr}")
+    return exe

@@ -144,3 +144,43 @@ def test_reference_examples_compile_unchanged(example, cj, tmp_path):
            f"-Xlinker", f"-rpath,{libdir}"]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr[-3000:]
+
+
+def test_example_program_builds(cj):
+    if shutil.which("nvcc") is None:
+        pytest.skip("nvcc not available")
+    exe = dropin_build.build_example(Path(cj.lib()._name).parent)
+    assert exe.exists()
+
+
+def _read_layout(path: Path):
+    w = np.fromfile(path, dtype="<i4")
+    S, depth, n = int(w[0]), int(w[1]), int(w[2])
+    return S, depth, w[3:3 + n], w[3 + n:]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode,arg", [("std", None), ("lines", 1), ("lines", 3), ("lines_mb", 1)])
+def test_example_program_on_gpu(cj, oracle, tmp_path, mode, arg):
+    """A user program over the drop-in headers: loadJSON / loadJSONLines_*,
+    parse_*, iterator, freeJson -- its result buffer equals the oracle's."""
+    exe = dropin_build.build_example(Path(cj.lib()._name).parent)
+    f = tmp_path / "doc.json"
+    if mode == "std":
+        doc = cj.synth_document(0xD0C0001, 3 << 20, max_depth=12)
+        f.write_bytes(doc.tobytes())
+        args = [str(exe), mode, str(f), str(tmp_path / "out.bin")]
+        ref = oracle.parse(doc)
+    else:
+        doc, _ = cj.synth_lines(0xD0C0002, 3 << 20)
+        f.write_bytes(doc.tobytes())
+        args = [str(exe), mode, str(f), str(arg), str(tmp_path / "out.bin")]
+        sizes = (cj.plan_lines_count(doc, arg) if mode == "lines"
+                 else cj.plan_lines_bytes(doc, arg << 20))
+        ref = oracle.parse(doc, lines=True, chunk_sizes=sizes)
+    r = subprocess.run(args, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith("first: ")
+    S, depth, _, buf = _read_layout(tmp_path / "out.bin")
+    assert S == ref.n_structural and depth == ref.max_depth
+    np.testing.assert_array_equal(buf, ref.reference_layout())
