@@ -94,6 +94,8 @@ _SIGNATURES = {
     "cj_result_free": (None, [ctypes.POINTER(_Result)]),
     "cj_parse_into": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
                                      ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ParseInfo)]),
+    "cj_parse_standard_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
+                                                 ctypes.c_size_t, ctypes.POINTER(ParseInfo), ctypes.c_void_p]),
     "cj_stage_standard": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
     "cj_stage_lines": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                       ctypes.c_size_t]),

@@ -117,6 +117,32 @@ void      cj_result_free(cj_result* res);
 cj_status cj_parse_into(cj_context* ctx, const uint8_t* host_data, size_t size, int lines_mode,
                         int32_t* host_out, size_t out_cap, cj_parse_info* info);
 
+/* ---- parse without allocating -----------------------------------------------
+ * This entry point has no counterpart in the reference, which allocates
+ * device memory on every call.  It exists for callers that may not allocate:
+ * a host program that owns the device's memory and gives each library a fixed
+ * budget, or a latency-critical loop in which the device-wide synchronisation
+ * that cudaMalloc and cudaFree bring would stall its other streams.
+ *
+ * Parses one standard JSON document of `size` bytes that is already in device
+ * memory (`d_data`) and writes the reference layout (2*(S+2) int32, as above)
+ * into the caller's device buffer `d_out` of `out_cap` entries, on `stream`
+ * (a cudaStream_t; NULL is the default stream) of the current device.  It
+ * allocates nothing, on the device or the host: its scratch is a fixed
+ * __device__ array of the library, sized for documents of at most
+ * CJ_NOALLOC_MAX_BYTES (about 21 MiB of device memory).  Larger documents are
+ * refused with CJ_ERR_TOO_LARGE; an `out_cap` under 2*(S+2) with
+ * CJ_ERR_CAPACITY (nothing is written to `d_out` then).  Returns once the
+ * parse has finished, with `info` filled and the verdict as the status.
+ *
+ * The first call on each device resolves the scratch address and sets up the
+ * kernels; make that first call before any stream capture.  All calls on one
+ * device share the scratch: calls must not overlap (two in flight at once,
+ * from two host threads or on two unordered streams, race on it). */
+#define CJ_NOALLOC_MAX_BYTES 1048576ull
+cj_status cj_parse_standard_noalloc(const uint8_t* d_data, size_t size, int32_t* d_out,
+                                    size_t out_cap, cj_parse_info* info, void* stream);
+
 /* ---- staged, device-resident runs -------------------------------------------
  * Stage copies the input into the context arena (synchronously); run launches
  * the parse kernels on the context stream without any host synchronisation;
