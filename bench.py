@@ -22,6 +22,7 @@ box), with every host thread running an independent instance.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -52,6 +53,8 @@ def parse_args():
     ap.add_argument("--cpu-sample", type=int, default=256 << 20, help="CPU-baseline sample bytes")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-documents measurement")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     return ap.parse_args()
 
 
@@ -209,6 +212,175 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+BATCH_DOCS = 4096
+BATCH_BYTES = 2 << 30
+
+
+def plain_parse(cj, ctx, view, out):
+    """One document through the per-document drop-in path (cj_parse_into)."""
+    info = cj.ParseInfo()
+    return cj.lib().cj_parse_into(ctx.handle, view.ctypes.data, view.size, 0, out.ctypes.data, out.size,
+                                  ctypes.byref(info))
+
+
+def run_batch(args, local):
+    """Batched documents: one graph replay parses the whole batch, against a
+    loop of plain per-document parses of the same documents."""
+    import cujson_gb300 as cj
+    seed = cj.CONFIG_SEED_BASE + 4
+    pin = cj.PinnedBuffer(BATCH_BYTES + (256 << 20))
+    t_gen = time.perf_counter()
+    packed, sizes, kinds = cj.batch_input(seed, BATCH_DOCS, BATCH_BYTES, out=pin.array)
+    t_gen = time.perf_counter() - t_gen
+    n = int(sizes.size)
+    N = int(sizes.sum())
+    ctx = cj.Context(local)
+    ctx.stage_batch_packed(packed, sizes)
+    best, tried = ctx.autotune(reps=2)
+    ctx.run_graph()
+    layout, status, S, depth, off = ctx.batch_layout()
+    verdicts_ok = bool(((status != 0) == (kinds > 0)).all())
+    total_out = int(off[-1])
+
+    # device-resident: graph replays of the staged batch
+    for _ in range(args.warmup):
+        ctx.run_graph()
+    ctx.batch_info()
+    launches0 = ctx.launches
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.run_graph()
+    ctx.batch_info()                       # synchronises
+    dev_s = (time.perf_counter() - t0) / args.steps
+    launches = (ctx.launches - launches0) // args.steps
+
+    # end to end: pinned packed input -> one H2D + scatter, graph replay,
+    # per-document verdicts, one D2H of every document's layout
+    out_pin = cj.PinnedBuffer(total_out * 4 + 64, dtype=np.int32)
+    for _ in range(max(1, args.warmup)):
+        ctx.stage_batch_packed(packed, sizes)
+        ctx.run_graph()
+        ctx.batch_layout(out_pin.array)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.stage_batch_packed(packed, sizes)
+        ctx.run_graph()
+        ctx.batch_layout(out_pin.array)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    same = bool(np.array_equal(out_pin.array[:total_out], layout))
+
+    # plain loop: one cj_parse_into per document, pinned input slices
+    ctx2 = cj.Context(local)
+    ctx2.reserve(int(sizes.max()), 1)
+    plain_out = cj.PinnedBuffer((2 * int(sizes.max()) + 4) * 4, dtype=np.int32)
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    views = [packed[offs[i]:offs[i + 1]] for i in range(n)]
+    for i in range(min(n, 64)):
+        plain_parse(cj, ctx2, views[i], plain_out.array)
+    t0 = time.perf_counter()
+    plain_bad = 0
+    for i in range(n):
+        plain_bad += plain_parse(cj, ctx2, views[i], plain_out.array) != 0
+    plain_s = time.perf_counter() - t0
+    plain_ok = plain_bad == int((kinds > 0).sum())
+    out = {
+        "workload": f"{n} standard documents, {N} B, lognormal sizes 1 KiB-16 MiB (seed {seed:#x}), "
+                    f"{int((kinds > 0).sum())} invalid (UTF-8 overlong/surrogate, unbalanced/mismatched)",
+        "docs": n, "bytes": N, "structurals": int(S.sum()),
+        "docs_per_s": round(n / dev_s, 1), "ms_per_batch": round(dev_s * 1e3, 3),
+        "e2e_docs_per_s": round(n / e2e_s, 1), "e2e_ms_per_batch": round(e2e_s * 1e3, 3),
+        "e2e_h2d_bytes": N, "e2e_d2h_bytes": total_out * 4,
+        "plain_loop_docs_per_s": round(n / plain_s, 1), "plain_loop_ms": round(plain_s * 1e3, 1),
+        "speedup_e2e_vs_plain": round(plain_s / e2e_s, 2),
+        "speedup_device_vs_plain": round(plain_s / dev_s, 2),
+        "verdicts_match_generator": verdicts_ok and plain_ok, "replay_results_identical": same,
+        "gpu_launches_per_batch": int(launches), "graph": True,
+        "tuning": best.as_dict(), "tuning_candidates": len(tried),
+        "generation_s": round(t_gen, 1),
+    }
+    ctx.close()
+    ctx2.close()
+    pin.close()
+    out_pin.close()
+    plain_out.close()
+    return out
+
+
+SERVE_REQUESTS = 2000
+SERVE_LOADS = (0.1, 0.5, 0.8, 1.0, 1.2)
+
+
+def plain_parse_any(cj, ctx, doc, lines, out):
+    info = cj.ParseInfo()
+    return cj.lib().cj_parse_into(ctx.handle, doc.ctypes.data, doc.size, int(lines), out.ctypes.data, out.size,
+                                  ctypes.byref(info))
+
+
+def run_serve(args, local):
+    """Serving: Poisson arrivals replayed against the continuous-batching
+    server at fractions of its measured capacity, under a fixed device-memory
+    budget; beside it the plain per-document loop on the same requests."""
+    import cujson_gb300 as cj
+    seed = cj.CONFIG_SEED_BASE + 5
+    t_gen = time.perf_counter()
+    docs, lines, kinds = cj.serve_requests(seed, SERVE_REQUESTS)
+    t_gen = time.perf_counter() - t_gen
+    # requests live in pinned memory, as a server's receive buffers would
+    offs = np.concatenate([[0], np.cumsum([d.size for d in docs])])
+    arena = cj.PinnedBuffer(int(offs[-1]))
+    views = []
+    for i, d in enumerate(docs):
+        v = arena.array[int(offs[i]):int(offs[i + 1])]
+        v[:] = d
+        views.append(v)
+    n = len(views)
+    total = sum(v.size for v in views)
+    budget = 16 << 30
+    srv = cj.Server(device=local, slots=2, max_batch_docs=1024, memory_budget=budget)
+    zero = np.zeros(n)
+    srv.replay(views, lines, zero)                        # warm the arenas
+    status, lat, mk = srv.replay(views, lines, zero)      # saturated: capacity
+    capacity = n / mk
+    ok = int((status == 0).sum())
+    rng = np.random.default_rng(seed)
+    sweep = []
+    for load in SERVE_LOADS:
+        rate = load * capacity
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+        arrivals -= arrivals[0]
+        st, lat, mk = srv.replay(views, lines, arrivals)
+        sweep.append({"offered_frac": load, "offered_docs_per_s": round(rate, 1),
+                      "docs_per_s": round(n / mk, 1), "p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 3),
+                      "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 3),
+                      "all_ok": bool((st == 0).all())})
+    stats = srv.stats().as_dict()
+    srv.close()
+    # plain loop: one cj_parse_into per request
+    ctx = cj.Context(local)
+    ctx.reserve(max(v.size for v in views), 1)
+    out = cj.PinnedBuffer((2 * max(v.size for v in views) + 4) * 4, dtype=np.int32)
+    for i in range(min(n, 32)):
+        plain_parse_any(cj, ctx, views[i], lines[i], out.array)
+    t0 = time.perf_counter()
+    for i in range(n):
+        plain_parse_any(cj, ctx, views[i], lines[i], out.array)
+    plain_s = time.perf_counter() - t0
+    ctx.close()
+    out.close()
+    arena.close()
+    return {
+        "workload": f"{n} requests, {total} B, lognormal sizes (median 64 KiB, up to 64 MiB), "
+                    f"{int((kinds == 1).sum())} JSON Lines, {int((kinds >= 2).sum())} adversarial "
+                    f"(depth-10000 nesting, 32 MiB backslash string); Poisson arrivals (seed {seed:#x})",
+        "slots": 2, "max_batch_docs": 1024, "memory_budget_bytes": budget,
+        "capacity_docs_per_s": round(capacity, 1), "capacity_GBps": round(total / (n / capacity) / 1e9, 2),
+        "requests_ok": ok, "sweep": sweep,
+        "plain_loop_docs_per_s": round(n / plain_s, 1),
+        "capacity_vs_plain": round(capacity / (n / plain_s), 2),
+        "stats": stats, "generation_s": round(t_gen, 1),
+    }
+
+
 def run_ours(args, world, rank, local, pg):
     import cujson_gb300 as cj
     peak, peak_kind = measured_peaks()
@@ -274,6 +446,8 @@ def run_ours(args, world, rank, local, pg):
 
     if rank != 0:
         return
+    batch = None if args.no_batch else run_batch(args, local)
+    serve = None if args.no_serve else run_serve(args, local)
     cpu = None
     if not args.no_cpu_baseline:
         v, desc = cpu_baseline_sample(args.cpu_sample)
@@ -294,6 +468,7 @@ def run_ours(args, world, rank, local, pg):
                                "spine": round(spine_ms / runs, 4)},
         "parse_roofline_frac": round(B / (span_max / args.steps / 1e3) / 1e9 / peak, 4),
         "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": ck,
+        "batch": batch, "serving": serve,
     }
     print(json.dumps(line), flush=True)
 

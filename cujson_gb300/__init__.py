@@ -15,6 +15,7 @@ built, or no GPU is present, the calls raise.
 from __future__ import annotations
 
 import ctypes
+import os
 from dataclasses import dataclass, field
 from pathlib import Path
 from typing import List, Optional, Sequence
@@ -65,6 +66,16 @@ class _Result(ctypes.Structure):
                 ("segment_sizes", ctypes.POINTER(ctypes.c_int64))]
 
 
+class Tuning(ctypes.Structure):
+    """Launch shapes (cj_tuning): 0 = default."""
+    _fields_ = [("scan_ctas", ctypes.c_int32), ("pair_blocks", ctypes.c_int32),
+                ("pair_threads", ctypes.c_int32), ("ms", ctypes.c_float)]
+
+    def as_dict(self):
+        return {"scan_ctas": self.scan_ctas, "pair_blocks": self.pair_blocks,
+                "pair_threads": self.pair_threads, "ms": round(float(self.ms), 4)}
+
+
 class SynthParams(ctypes.Structure):
     _fields_ = [("max_depth", ctypes.c_int32), ("keys_min", ctypes.c_int32),
                 ("keys_max", ctypes.c_int32), ("nested_max_items", ctypes.c_int32),
@@ -100,6 +111,29 @@ _SIGNATURES = {
     "cj_stage_lines": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                       ctypes.c_size_t]),
     "cj_run_staged": (ctypes.c_int, [ctypes.c_void_p]),
+    "cj_run_staged_graph": (ctypes.c_int, [ctypes.c_void_p]),
+    "cj_server_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "cj_server_destroy": (None, [ctypes.c_void_p]),
+    "cj_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
+                                        ctypes.POINTER(ctypes.c_uint64)]),
+    "cj_server_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int64, ctypes.c_void_p,
+                                      ctypes.POINTER(ctypes.c_double)]),
+    "cj_server_take": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_size_t]),
+    "cj_server_get_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "cj_server_replay": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.POINTER(ctypes.c_double)]),
+    "cj_stage_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                      ctypes.c_int]),
+    "cj_stage_batch_packed": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                             ctypes.c_int]),
+    "cj_batch_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                     ctypes.c_void_p, ctypes.c_size_t]),
+    "cj_copy_batch_result": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
+    "cj_context_set_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "cj_context_get_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "cj_autotune_staged": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
     "cj_staged_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ParseInfo)]),
     "cj_copy_staged_result": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
     "cj_staged_device_outputs": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p),
@@ -309,6 +343,81 @@ class Context:
         _check(lib().cj_copy_staged_result(self._h, buf.ctypes.data, buf.size), "copy")
         return ParseResult(buf, S, int(inf.max_depth))
 
+    def run_graph(self) -> None:
+        _check(lib().cj_run_staged_graph(self._h), "run_graph")
+
+    # ---- batches of independent documents ------------------------------------------
+    def stage_batch(self, docs: Sequence, lines: bool = False) -> None:
+        """Stage documents given one buffer each (kept alive by the caller until
+        this returns)."""
+        bufs = [_u8(d) for d in docs]
+        ptrs = (ctypes.c_void_p * len(bufs))(*[b.ctypes.data for b in bufs])
+        sizes = (ctypes.c_size_t * len(bufs))(*[b.size for b in bufs])
+        self._batch_n = len(bufs)
+        _check(lib().cj_stage_batch(self._h, ptrs, sizes, len(bufs), int(lines)), "stage_batch")
+
+    def stage_batch_packed(self, packed, sizes: Sequence[int], lines: bool = False) -> None:
+        """Stage documents laid back to back in one buffer (pinned for speed)."""
+        buf = _u8(packed)
+        sz = np.ascontiguousarray(np.asarray(sizes, dtype=np.uint64))
+        if int(sz.sum()) > buf.size:
+            raise ValueError("sizes exceed the packed buffer")
+        self._batch_n = int(sz.size)
+        _check(lib().cj_stage_batch_packed(self._h, buf.ctypes.data, sz.ctypes.data, int(sz.size),
+                                           int(lines)), "stage_batch_packed")
+
+    def batch_info(self):
+        """(status int32[n], n_structural int64[n], max_depth int32[n], offsets int64[n+1])."""
+        n = self._batch_n
+        status = np.zeros(n, np.int32)
+        S = np.zeros(n, np.int64)
+        depth = np.zeros(n, np.int32)
+        off = np.zeros(n + 1, np.int64)
+        _check(lib().cj_batch_info(self._h, status.ctypes.data, S.ctypes.data, depth.ctypes.data,
+                                   off.ctypes.data, n), "batch_info")
+        return status, S, depth, off
+
+    def batch_layout(self, out: Optional[np.ndarray] = None):
+        """Every document's reference layout back to back, with the info arrays."""
+        status, S, depth, off = self.batch_info()
+        total = int(off[-1])
+        if out is None or out.size < total:
+            out = np.empty(total, np.int32)
+        _check(lib().cj_copy_batch_result(self._h, out.ctypes.data, out.size), "copy_batch")
+        return out, status, S, depth, off
+
+    def batch_results(self):
+        """List of (status, ParseResult or None) per document."""
+        layout, status, S, depth, off = self.batch_layout()
+        res = []
+        for i in range(status.size):
+            if status[i] != OK:
+                res.append((int(status[i]), None))
+            else:
+                buf = layout[off[i]:off[i + 1]].copy()
+                res.append((OK, ParseResult(buf, int(S[i]), int(depth[i]))))
+        return res
+
+    # ---- launch shapes -------------------------------------------------------------
+    def set_tuning(self, scan_ctas: int = 0, pair_blocks: int = 0, pair_threads: int = 0) -> None:
+        t = Tuning(scan_ctas, pair_blocks, pair_threads, 0.0)
+        _check(lib().cj_context_set_tuning(self._h, ctypes.byref(t)), "set_tuning")
+
+    def get_tuning(self) -> Tuning:
+        t = Tuning()
+        _check(lib().cj_context_get_tuning(self._h, ctypes.byref(t)), "get_tuning")
+        return t
+
+    def autotune(self, reps: int = 3):
+        """Times graph replays of the staged input for each candidate launch
+        shape and keeps the fastest; returns (best, [tried])."""
+        best = Tuning()
+        tried = (Tuning * 64)()
+        n = ctypes.c_size_t()
+        _check(lib().cj_autotune_staged(self._h, reps, ctypes.byref(best), tried, 64, ctypes.byref(n)),
+               "autotune")
+        return best, [tried[i] for i in range(n.value)]
+
     def timing(self, enable: bool = True) -> None:
         _check(lib().cj_context_timing(self._h, int(enable)), "timing")
 
@@ -332,6 +441,137 @@ class Context:
                                  out.size, ctypes.byref(inf))
         _check(st, "parse_into")
         return inf
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("slots", ctypes.c_uint32),
+                ("max_batch_docs", ctypes.c_uint32), ("memory_budget", ctypes.c_uint64)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("batches", ctypes.c_uint64), ("docs", ctypes.c_uint64), ("bytes", ctypes.c_uint64),
+                ("max_batch_docs", ctypes.c_uint64), ("peak_admitted_bytes", ctypes.c_uint64),
+                ("device_bytes", ctypes.c_uint64), ("fault", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
+class Server:
+    """Parse server with continuous batching (cj_server_*).  Submitted buffers
+    must stay alive until their request completes; the server keeps a
+    reference to each submitted array until it is taken."""
+
+    def __init__(self, device: int = -1, slots: int = 2, max_batch_docs: int = 1024,
+                 memory_budget: int = 16 << 30):
+        cfg = ServerConfig(device, slots, max_batch_docs, memory_budget)
+        h = ctypes.c_void_p()
+        _check(lib().cj_server_create(ctypes.byref(cfg), ctypes.byref(h)), "cj_server_create")
+        self._h = h
+        self._keep = {}
+
+    def close(self) -> None:
+        if self._h:
+            lib().cj_server_destroy(self._h)
+            self._h = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, data, lines: bool = False) -> int:
+        buf = _u8(data)
+        t = ctypes.c_uint64()
+        _check(lib().cj_server_submit(self._h, buf.ctypes.data, buf.size, int(lines), ctypes.byref(t)),
+               "submit")
+        self._keep[t.value] = buf
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1):
+        """(ParseInfo, latency seconds)."""
+        inf = ParseInfo()
+        lat = ctypes.c_double()
+        _check(lib().cj_server_wait(self._h, ticket, timeout_ms, ctypes.byref(inf), ctypes.byref(lat)),
+               "wait")
+        return inf, lat.value
+
+    def take(self, ticket: int):
+        """(status, ParseResult or None) of a completed request; releases it."""
+        inf, _ = self.wait(ticket)
+        S = int(inf.n_structural)
+        out = np.zeros(2 * S + 4, np.int32) if inf.status == OK else None
+        st = lib().cj_server_take(self._h, ticket, out.ctypes.data if out is not None else None,
+                                  out.size if out is not None else 0)
+        self._keep.pop(ticket, None)
+        if st != OK:
+            return st, None
+        return st, ParseResult(out, S, int(inf.max_depth))
+
+    def stats(self) -> ServerStats:
+        st = ServerStats()
+        _check(lib().cj_server_get_stats(self._h, ctypes.byref(st)), "stats")
+        return st
+
+    def replay(self, docs: Sequence, lines: Sequence[bool], arrival_s: Sequence[float]):
+        """Submit docs[i] at arrival_s[i] (seconds from now), wait for all;
+        returns (status int32[n], latency float64[n], makespan seconds)."""
+        n = len(docs)
+        bufs = [_u8(d) for d in docs]
+        ptrs = (ctypes.c_void_p * n)(*[b.ctypes.data for b in bufs])
+        sizes = np.ascontiguousarray([b.size for b in bufs], dtype=np.uint64)
+        ln = np.ascontiguousarray(lines, dtype=np.int32)
+        arr = np.ascontiguousarray(arrival_s, dtype=np.float64)
+        status = np.zeros(n, np.int32)
+        lat = np.zeros(n, np.float64)
+        mk = ctypes.c_double()
+        _check(lib().cj_server_replay(self._h, ptrs, sizes.ctypes.data, ln.ctypes.data, arr.ctypes.data, n,
+                                      status.ctypes.data, lat.ctypes.data, ctypes.byref(mk)), "replay")
+        return status, lat, mk.value
+
+
+def serve_requests(seed: int, n: int, median: int = 64 << 10, sigma: float = 1.6,
+                   min_size: int = 256, max_size: int = 64 << 20, lines_frac: float = 0.2,
+                   adversarial_frac: float = 0.005, deep_depth: int = 10000,
+                   backslash_bytes: int = 32 << 20):
+    """Seeded request pool: lognormal sizes (median `median`, tail clamped to
+    `max_size`), `lines_frac` JSON-Lines documents, and `adversarial_frac`
+    adversarial documents, alternately a `deep_depth`-deep [[...]] nesting and
+    one string of `backslash_bytes` of backslash runs.  Returns (list of uint8
+    arrays, lines flags bool[n], kinds: 0 standard, 1 JSON Lines, 2 deep,
+    3 backslash string)."""
+    rng = np.random.default_rng(seed)
+    sizes = np.clip(np.round(median * rng.lognormal(0.0, sigma, n)), min_size, max_size).astype(np.int64)
+    kinds = np.where(rng.random(n) < lines_frac, 1, 0)
+    n_adv = int(round(adversarial_frac * n))
+    adv = rng.choice(n, size=n_adv, replace=False) if n_adv else []
+    for j, i in enumerate(adv):
+        kinds[i] = 2 + (j % 2)
+    docs = [None] * n
+
+    def make(i):
+        k = int(kinds[i])
+        if k == 0:
+            docs[i] = synth_document(seed * 7919 + i, int(sizes[i]), max_depth=8, threads=1)
+        elif k == 1:
+            docs[i] = synth_lines(seed * 7919 + i, int(sizes[i]), threads=1)[0]
+        elif k == 2:
+            docs[i] = synth_deep(deep_depth)
+        else:
+            docs[i] = synth_backslash_string(seed + i, backslash_bytes)
+
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+        list(ex.map(make, range(n)))
+    return docs, kinds == 1, kinds
 
 
 _default: Optional[Context] = None
@@ -417,6 +657,16 @@ def synth_document(seed: int, size: int, **kw) -> np.ndarray:
     return out
 
 
+def synth_document_into(seed: int, out: np.ndarray, **kw) -> None:
+    """synth_document written into a contiguous uint8 view (a slice of a batch buffer)."""
+    if out.dtype != np.uint8 or not out.flags["C_CONTIGUOUS"]:
+        raise ValueError("out must be a contiguous uint8 array")
+    p = synth_params(**kw)
+    n = lib().cj_synth_document(seed, out.size, ctypes.byref(p), out.ctypes.data)
+    if n != out.size:
+        raise ValueError("synth_document failed")
+
+
 def synth_lines(seed: int, size: int, **kw):
     out = np.empty(size, dtype=np.uint8)
     p = synth_params(**kw)
@@ -441,6 +691,54 @@ def synth_backslash_string(seed: int, body: int) -> np.ndarray:
 
 def synth_corrupt(doc: np.ndarray, kind: int, seed: int = 0) -> bool:
     return bool(lib().cj_synth_corrupt(doc.ctypes.data, doc.size, kind, seed))
+
+
+# corruption kinds of cj_synth_corrupt
+CORRUPT_OVERLONG2, CORRUPT_OVERLONG3, CORRUPT_SURROGATE, CORRUPT_UNBALANCED, CORRUPT_MISMATCHED = 1, 2, 3, 4, 5
+
+
+def batch_input(seed: int, n_docs: int, total_bytes: int, min_size: int = 1 << 10,
+                max_size: int = 16 << 20, sigma: float = 2.0, invalid_utf8: float = 0.01,
+                invalid_brackets: float = 0.01, out: Optional[np.ndarray] = None):
+    """A seeded batch of independent standard documents, back to back.
+
+    Sizes are lognormal (sigma `sigma`), clamped to [min_size, max_size] and
+    scaled so that they sum to about `total_bytes`.  A fraction of the
+    documents gets an invalid UTF-8 sequence (overlong C0 80 / E0 80 80 or a
+    surrogate ED A0 80 inside a string) and another fraction an unbalanced or
+    mismatched bracket.  Returns (packed uint8 array, sizes int64[n],
+    kinds int32[n]) where kinds[i] is 0 or the cj_synth_corrupt kind applied.
+    `out` (>= the returned size, e.g. pinned) receives the documents if given.
+    """
+    rng = np.random.default_rng(seed)
+    raw = rng.lognormal(mean=0.0, sigma=sigma, size=n_docs)
+    sizes = raw * (total_bytes / raw.sum())
+    for _ in range(8):   # re-scale after clamping
+        sizes = np.clip(sizes, min_size, max_size)
+        sizes *= total_bytes / sizes.sum()
+    sizes = np.clip(np.round(sizes), min_size, max_size).astype(np.int64)
+    total = int(sizes.sum())
+    packed = out[:total] if out is not None else np.empty(total, np.uint8)
+    kinds = np.zeros(n_docs, np.int32)
+    n_utf = int(round(invalid_utf8 * n_docs))
+    n_brk = int(round(invalid_brackets * n_docs))
+    pick = rng.permutation(n_docs)
+    for j, i in enumerate(pick[:n_utf]):
+        kinds[i] = (CORRUPT_OVERLONG2, CORRUPT_OVERLONG3, CORRUPT_SURROGATE)[j % 3]
+    for j, i in enumerate(pick[n_utf:n_utf + n_brk]):
+        kinds[i] = (CORRUPT_UNBALANCED, CORRUPT_MISMATCHED)[j % 2]
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+
+    def make(i):
+        view = packed[int(offs[i]):int(offs[i + 1])]
+        synth_document_into(seed * 1000003 + i, view, max_depth=8, threads=1)
+        if kinds[i] and not synth_corrupt(view, int(kinds[i]), seed + i):
+            kinds[i] = 0
+
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+        list(ex.map(make, range(n_docs)))
+    return packed, sizes, kinds
 
 
 def config_input(config: int, size: Optional[int] = None):

@@ -79,6 +79,33 @@ struct cj_context {
     bool timing = false;
     std::vector<cudaEvent_t> events;   // 4 per recorded run
     size_t events_used = 0;
+
+    // batches of independent documents
+    bool batch = false;
+    uint64_t batch_chunks = 0;          // pairing chunks of the batch layout
+    DevBuf<uint32_t> seg_err;
+    DevBuf<int32_t> seg_depth;
+    DevBuf<uint64_t> rchunk_off;
+    DevBuf<uint64_t> layout_off;
+    DevBuf<int32_t> layout;
+    DevBuf<uint8_t> pack;               // packed staging copy of a batch
+    DevBuf<uint64_t> pack_off;          // per document: packed byte offset, then word offsets
+    std::vector<uint64_t> h_pack_off;
+    bool batch_read = false;            // host mirrors below are current
+    std::vector<SegmentOut> h_bseg_out;
+    std::vector<uint32_t> h_seg_err;
+    std::vector<int32_t> h_seg_depth;
+    std::vector<uint64_t> h_layout_off;
+
+    // CUDA graph of the staged run, replayed by cj_run_staged_graph
+    cudaGraphExec_t graph_exec = nullptr;
+    bool graph_valid = false;
+    uint64_t arena_gen = 0;             // bumped whenever a device buffer is (re)allocated
+
+    // launch shapes (0 = default), set by cj_context_set_tuning / cj_autotune_staged
+    uint32_t tune_scan_ctas = 0;
+    uint32_t tune_pair_blocks = 0;
+    uint32_t tune_pair_threads = 0;
 };
 
 namespace {
@@ -100,6 +127,7 @@ cj_status ensure(cj_context* ctx, DevBuf<T>& b, size_t n)
     size_t want = std::max<size_t>(n + n / 8, 64);
     CJ_CUDA(cudaMalloc((void**)&b.p, want * sizeof(T)));
     b.cap = want;
+    ctx->arena_gen++;
     ctx->dev_bytes += want * sizeof(T);
     return CJ_OK;
 }
@@ -160,6 +188,7 @@ cj_status stage(cj_context* ctx, const uint8_t* const* chunks, const size_t* siz
                 bool lines)
 {
     ctx->staged = false;
+    ctx->graph_valid = false;
     if (!chunks || !sizes || n == 0) return CJ_ERR_INVALID_ARGUMENT;
     size_t total = 0;
     for (size_t i = 0; i < n; i++) {
@@ -208,25 +237,45 @@ cj_status stage(cj_context* ctx, const uint8_t* const* chunks, const size_t* siz
     ctx->n_segs = (uint32_t)n;
     ctx->n_tiles = tile;
     ctx->lines = lines;
+    ctx->batch = false;
+    ctx->graph_valid = false;
     ctx->staged = true;
     return CJ_OK;
 }
 
-cj_status run(cj_context* ctx)
+uint32_t pair_threads(const cj_context* ctx)
 {
-    if (!ctx->staged) return CJ_ERR_NOT_STAGED;
-    CJ_CUDA(cudaSetDevice(ctx->device));
-    ctx->epoch = (ctx->epoch + 1) & 0x3FFFFFFFu;
-    if (ctx->epoch == 0) {
-        // epoch wrapped: stale descriptors could alias, so clear them
-        CJ_CUDA(cudaMemsetAsync(ctx->desc_flag.p, 0, ctx->desc_flag.cap * sizeof(uint32_t), ctx->stream));
+    return ctx->tune_pair_threads ? ctx->tune_pair_threads : 256u;
+}
+
+// Every kernel of one staged run, on the context stream, without host
+// synchronisation.  `graph` selects the form that a CUDA graph replays: the
+// epoch stays fixed and the descriptor flags and min-tree are cleared by the
+// run itself instead of being told apart by epoch.
+cj_status enqueue(cj_context* ctx, bool graph)
+{
+    if (!graph) {
+        ctx->epoch = (ctx->epoch + 1) & 0x3FFFFFFFu;
+        if (ctx->epoch == 0) {
+            // epoch wrapped: stale descriptors could alias, so clear them
+            CJ_CUDA(cudaMemsetAsync(ctx->desc_flag.p, 0, ctx->desc_flag.cap * sizeof(uint32_t), ctx->stream));
+            CJ_CUDA(cudaMemsetAsync(ctx->tree.p, 0, ctx->tree.cap * sizeof(unsigned long long), ctx->stream));
+            ctx->epoch = 1;
+        }
+    } else {
+        CJ_CUDA(cudaMemsetAsync(ctx->desc_flag.p, 0, (size_t)ctx->n_tiles * sizeof(uint32_t), ctx->stream));
         CJ_CUDA(cudaMemsetAsync(ctx->tree.p, 0, ctx->tree.cap * sizeof(unsigned long long), ctx->stream));
-        ctx->epoch = 1;
     }
     CJ_CUDA(cudaMemsetAsync(ctx->d_ctrl, 0, sizeof(Ctrl), ctx->stream));
+    if (ctx->batch) {
+        CJ_CUDA(cudaMemsetAsync(ctx->seg_err.p, 0, ctx->n_segs * sizeof(uint32_t), ctx->stream));
+        CJ_CUDA(cudaMemsetAsync(ctx->seg_depth.p, 0, ctx->n_segs * sizeof(int32_t), ctx->stream));
+        // chunks without records read as kNoLevel (bytes 0x7F) in the next-lower search
+        CJ_CUDA(cudaMemsetAsync(ctx->cinfo.p, 0x7F, (ctx->batch_chunks + 1) * sizeof(int4), ctx->stream));
+    }
 
     cudaEvent_t* ev = nullptr;
-    if (ctx->timing) {
+    if (ctx->timing && !graph) {
         if (ctx->events_used + 4 > ctx->events.size()) {
             for (int i = 0; i < 4; i++) {
                 cudaEvent_t e;
@@ -239,7 +288,8 @@ cj_status run(cj_context* ctx)
         CJ_CUDA(cudaEventRecord(ev[0], ctx->stream));
     }
 
-    ScanParams sp;
+    ScanParams sp{};
+    sp.one = 1;
     sp.in = ctx->in.p;
     sp.segs = ctx->segs.p;
     sp.tile_seg = (ctx->n_segs > 1) ? ctx->tile_seg.p : nullptr;
@@ -254,10 +304,18 @@ cj_status run(cj_context* ctx)
     sp.ctrl = ctx->d_ctrl;
     sp.seg_out = ctx->seg_out.p;
     sp.epoch = ctx->epoch;
-    launch_scan(sp, ctx->lines, (int)std::min<uint32_t>(ctx->n_tiles, ctx->scan_grid), ctx->stream);
+    sp.seg_err = ctx->batch ? ctx->seg_err.p : nullptr;
+    uint32_t scan_grid = ctx->scan_grid;
+    if (ctx->tune_scan_ctas) scan_grid = std::min(scan_grid, ctx->tune_scan_ctas);
+    launch_scan(sp, ctx->lines, (int)std::min<uint32_t>(ctx->n_tiles, scan_grid), ctx->stream);
+    if (ctx->batch) {
+        launch_batch_prefix(ctx->segs.p, ctx->seg_out.p, ctx->n_segs, ctx->layout_off.p, ctx->rchunk_off.p,
+                            ctx->stream);
+        ctx->launches += 1;
+    }
     if (ev) CJ_CUDA(cudaEventRecord(ev[1], ctx->stream));
 
-    PairParams pp;
+    PairParams pp{};
     pp.brk = ctx->brk.p;
     pp.pair = ctx->pair.p;
     pp.spine = ctx->spine.p;
@@ -267,14 +325,68 @@ cj_status run(cj_context* ctx)
     pp.ctrl = ctx->d_ctrl;
     pp.epoch = ctx->epoch;
     pp.chunk_cap = (uint32_t)ctx->chunk_cap;
-    size_t max_chunks = (ctx->n_bytes + kChunk - 1) / kChunk;
-    int grid = (int)std::min<size_t>((max_chunks + 7) / 8 + 1, (size_t)ctx->sm_count * 8);
-    launch_pair(pp, grid, ctx->stream);
+    pp.rchunk_off = ctx->batch ? ctx->rchunk_off.p : nullptr;
+    pp.n_bsegs = ctx->batch ? ctx->n_segs : 0u;
+    pp.segs = ctx->segs.p;
+    pp.seg_out = ctx->seg_out.p;
+    pp.seg_err = ctx->batch ? ctx->seg_err.p : nullptr;
+    pp.seg_depth = ctx->batch ? ctx->seg_depth.p : nullptr;
+    pp.n_chunks = ctx->batch ? ctx->batch_chunks : 0;
+    const uint32_t pthreads = pair_threads(ctx);
+    // batch: the chunks holding records are at most bytes / 8 / kChunk + one per document
+    const size_t max_chunks = ctx->batch ? ctx->n_bytes / 8 / kChunk + ctx->n_segs
+                                         : (ctx->n_bytes + kChunk - 1) / kChunk;
+    const size_t warps_per_block = pthreads / 32;
+    int grid = (int)std::min<size_t>((max_chunks + warps_per_block - 1) / warps_per_block + 1,
+                                     (size_t)ctx->sm_count * 8 * 256 / pthreads);
+    if (ctx->tune_pair_blocks) grid = (int)std::min<size_t>((size_t)grid, ctx->tune_pair_blocks);
+    launch_pair(pp, grid, ctx->stream, (int)pthreads);
     if (ev) CJ_CUDA(cudaEventRecord(ev[2], ctx->stream));
-    launch_spine(pp, grid, ctx->stream);
+    launch_spine(pp, grid, ctx->stream, (int)pthreads);
     if (ev) CJ_CUDA(cudaEventRecord(ev[3], ctx->stream));
     ctx->launches += (ctx->n_tiles ? 1 : 0) + 2;
+    if (ctx->batch) {
+        launch_batch_layout(ctx->segs.p, ctx->seg_out.p, ctx->n_segs, ctx->pos.p, ctx->pair.p,
+                            ctx->layout_off.p, ctx->layout.p, ctx->sm_count, ctx->stream);
+        ctx->launches += 1;
+        ctx->batch_read = false;
+    }
     CJ_CUDA(cudaGetLastError());
+    return CJ_OK;
+}
+
+cj_status run(cj_context* ctx)
+{
+    if (!ctx->staged) return CJ_ERR_NOT_STAGED;
+    CJ_CUDA(cudaSetDevice(ctx->device));
+    return enqueue(ctx, false);
+}
+
+// Capture the staged run once into a CUDA graph, then replay it.
+cj_status run_graph(cj_context* ctx)
+{
+    if (!ctx->staged) return CJ_ERR_NOT_STAGED;
+    CJ_CUDA(cudaSetDevice(ctx->device));
+    if (!ctx->graph_valid) {
+        if (ctx->graph_exec) { cudaGraphExecDestroy(ctx->graph_exec); ctx->graph_exec = nullptr; }
+        ctx->epoch = (ctx->epoch + 1) & 0x3FFFFFFFu;
+        if (ctx->epoch == 0) ctx->epoch = 1;
+        CJ_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        const int64_t launches0 = ctx->launches;
+        cj_status st = enqueue(ctx, true);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+        ctx->launches = launches0;
+        if (st) { if (g) cudaGraphDestroy(g); return st; }
+        if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return CJ_ERR_CUDA; }
+        e = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) { ctx->graph_exec = nullptr; return CJ_ERR_CUDA; }
+        ctx->graph_valid = true;
+    }
+    CJ_CUDA(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+    ctx->launches += (ctx->n_tiles ? 1 : 0) + 2 + (ctx->batch ? 2 : 0);
+    ctx->batch_read = false;
     return CJ_OK;
 }
 
@@ -344,6 +456,186 @@ cj_status to_result(cj_context* ctx, const cj_parse_info& info, cj_result* out)
     return CJ_OK;
 }
 
+// ---- batches of independent documents ---------------------------------------
+//
+// Device layout of a batch of n documents with sizes b_i:
+//   in:    document i at dev_off_i = sum_{j<i} round_up(b_j, 1 KiB)
+//   pos, pair: out_base_i = sum_{j<i} (b_j + 1)            (S_i <= b_i)
+//   brk:   brk_base_i = sum_{j<i} round_up(b_j, kChunk)   (K_i <= b_i; chunk-aligned,
+//          so a pairing chunk never holds two documents)
+//   layout: every document's 2*(S_i+2) result back to back (offsets on the device)
+cj_status reserve_batch(cj_context* ctx, uint64_t in_bytes, uint64_t out_cap, uint64_t brk_cap,
+                        uint64_t tiles, size_t n, uint64_t layout_cap, uint64_t pack_bytes)
+{
+    const uint64_t chunks = brk_cap / kChunk + 1;
+    cj_status st;
+    if ((st = ensure(ctx, ctx->in, in_bytes + 64))) return st;
+    if ((st = ensure(ctx, ctx->pos, out_cap))) return st;
+    if ((st = ensure(ctx, ctx->pair, out_cap))) return st;
+    if ((st = ensure(ctx, ctx->brk, brk_cap + 1))) return st;
+    if ((st = ensure(ctx, ctx->desc_flag, tiles))) return st;
+    if ((st = ensure(ctx, ctx->desc_agg, tiles * 4))) return st;
+    if ((st = ensure(ctx, ctx->desc_incl, tiles))) return st;
+    if ((st = ensure(ctx, ctx->segs, n))) return st;
+    if ((st = ensure(ctx, ctx->seg_out, n))) return st;
+    if ((st = ensure(ctx, ctx->tile_seg, tiles))) return st;
+    if ((st = ensure(ctx, ctx->spine, chunks * (size_t)kChunk))) return st;
+    if ((st = ensure(ctx, ctx->cinfo, chunks))) return st;
+    if ((st = ensure(ctx, ctx->seg_err, n))) return st;
+    if ((st = ensure(ctx, ctx->seg_depth, n))) return st;
+    if ((st = ensure(ctx, ctx->rchunk_off, n + 1))) return st;
+    if ((st = ensure(ctx, ctx->layout_off, n + 1))) return st;
+    if ((st = ensure(ctx, ctx->layout, layout_cap))) return st;
+    if (pack_bytes) {
+        if ((st = ensure(ctx, ctx->pack, pack_bytes + 16))) return st;
+        if ((st = ensure(ctx, ctx->pack_off, 2 * (n + 1)))) return st;
+    }
+    if (chunks > ctx->chunk_cap) {
+        size_t off = 0, m = chunks;
+        ctx->tree_off[0] = 0;
+        for (int l = 1; l <= kTreeLevels; l++) {
+            m = (m + 31) / 32;
+            ctx->tree_off[l] = off;
+            off += m;
+        }
+        if ((st = ensure(ctx, ctx->tree, off))) return st;
+        ctx->chunk_cap = chunks;
+    }
+    // a fresh or regrown descriptor / tree array must not hold stale tags
+    CJ_CUDA(cudaMemsetAsync(ctx->desc_flag.p, 0, ctx->desc_flag.cap * sizeof(uint32_t), ctx->stream));
+    CJ_CUDA(cudaMemsetAsync(ctx->tree.p, 0, ctx->tree.cap * sizeof(unsigned long long), ctx->stream));
+    if (!ctx->h_ctrl) CJ_CUDA(cudaMallocHost((void**)&ctx->h_ctrl, sizeof(Ctrl)));
+    return CJ_OK;
+}
+
+// `docs` (one host pointer per document) or `packed` (documents back to back)
+cj_status stage_batch(cj_context* ctx, const uint8_t* const* docs, const uint8_t* packed,
+                      const size_t* sizes, size_t n, bool lines)
+{
+    // a captured graph stays valid for a new batch of the same document sizes
+    // in the same buffers
+    bool same = ctx->graph_valid && ctx->batch && ctx->staged && ctx->lines == lines && sizes &&
+                ctx->h_segs.size() == n;
+    for (size_t i = 0; same && i < n; i++) same = ctx->h_segs[i].len == sizes[i];
+    const uint64_t gen0 = ctx->arena_gen;
+    ctx->staged = false;
+    ctx->graph_valid = false;
+    if (!sizes || n == 0 || n > 0xFFFFFFFEu || (!docs && !packed)) return CJ_ERR_INVALID_ARGUMENT;
+    uint64_t in_bytes = 0, out_cap = 0, brk_cap = 0, tiles = 0, layout_cap = 0, total = 0;
+    for (size_t i = 0; i < n; i++) {
+        if (sizes[i] == 0 || (docs && !docs[i])) return CJ_ERR_INVALID_ARGUMENT;
+        if (sizes[i] > CJ_MAX_INPUT_BYTES) return CJ_ERR_TOO_LARGE;
+        in_bytes += round_up(sizes[i], kPadBytes);
+        out_cap += sizes[i] + 1;
+        brk_cap += round_up(sizes[i], kChunk);
+        tiles += (sizes[i] + kTileBytes - 1) / kTileBytes;
+        layout_cap += 2 * (uint64_t)sizes[i] + 4;
+        total += sizes[i];
+    }
+    if (tiles >= 0xFFFFFFFFull) return CJ_ERR_TOO_LARGE;
+    CJ_CUDA(cudaSetDevice(ctx->device));
+    cj_status st = reserve_batch(ctx, in_bytes, out_cap, brk_cap, tiles + 1, n, layout_cap,
+                                 packed ? total : 0);
+    if (st) return st;
+
+    ctx->h_segs.resize(n);
+    ctx->h_tile_seg.resize(tiles);
+    uint64_t dev_off = 0, out_base = 0, brk_base = 0;
+    uint32_t tile = 0;
+    for (size_t i = 0; i < n; i++) {
+        Segment& g = ctx->h_segs[i];
+        g.dev_off = dev_off;
+        g.len = sizes[i];
+        g.logical_off = 0;
+        g.out_base = out_base;
+        g.brk_base = brk_base;
+        g.first_tile = tile;
+        g.n_tiles = (uint32_t)((sizes[i] + kTileBytes - 1) / kTileBytes);
+        g.flags = 0;
+        g.pad = 0;
+        for (uint32_t t = 0; t < g.n_tiles; t++) ctx->h_tile_seg[tile + t] = (uint32_t)i;
+        dev_off += round_up(sizes[i], kPadBytes);
+        out_base += sizes[i] + 1;
+        brk_base += round_up(sizes[i], kChunk);
+        tile += g.n_tiles;
+    }
+    if (packed) {
+        // one copy of the packed documents, then a kernel moves each one to
+        // its aligned place
+        ctx->h_pack_off.assign(2 * (n + 1), 0);
+        uint64_t so = 0, wo = 0;
+        for (size_t i = 0; i < n; i++) {
+            ctx->h_pack_off[i] = so;
+            ctx->h_pack_off[n + 1 + i] = wo;
+            so += sizes[i];
+            wo += (sizes[i] + 3) / 4;
+        }
+        ctx->h_pack_off[n] = so;
+        ctx->h_pack_off[2 * n + 1] = wo;
+        CJ_CUDA(cudaMemcpyAsync(ctx->pack.p, packed, total, cudaMemcpyHostToDevice, ctx->stream));
+        CJ_CUDA(cudaMemcpyAsync(ctx->pack_off.p, ctx->h_pack_off.data(), ctx->h_pack_off.size() * sizeof(uint64_t),
+                                cudaMemcpyHostToDevice, ctx->stream));
+    } else {
+        for (size_t i = 0; i < n; i++)
+            CJ_CUDA(cudaMemcpyAsync(ctx->in.p + ctx->h_segs[i].dev_off, docs[i], sizes[i],
+                                    cudaMemcpyHostToDevice, ctx->stream));
+    }
+    CJ_CUDA(cudaMemcpyAsync(ctx->segs.p, ctx->h_segs.data(), n * sizeof(Segment), cudaMemcpyHostToDevice,
+                            ctx->stream));
+    CJ_CUDA(cudaMemcpyAsync(ctx->tile_seg.p, ctx->h_tile_seg.data(), tiles * sizeof(uint32_t),
+                            cudaMemcpyHostToDevice, ctx->stream));
+    if (packed) {
+        launch_batch_scatter(ctx->pack.p, ctx->pack_off.p, ctx->pack_off.p + n + 1, ctx->segs.p, (uint32_t)n,
+                             ctx->h_pack_off[2 * n + 1], ctx->in.p, ctx->sm_count, ctx->stream);
+        ctx->launches += 1;
+    }
+    ctx->batch_chunks = brk_cap / kChunk;
+    CJ_CUDA(cudaGetLastError());
+    CJ_CUDA(cudaStreamSynchronize(ctx->stream));   // host vectors must outlive the copies
+    ctx->n_bytes = total;
+    ctx->n_segs = (uint32_t)n;
+    ctx->n_tiles = tile;
+    ctx->lines = lines;
+    ctx->batch = true;
+    ctx->batch_read = false;
+    ctx->graph_valid = same && ctx->arena_gen == gen0;
+    ctx->staged = true;
+    return CJ_OK;
+}
+
+// per-document counts, verdicts, depths and layout offsets into host mirrors
+cj_status read_batch(cj_context* ctx)
+{
+    if (!ctx->staged || !ctx->batch) return CJ_ERR_NOT_STAGED;
+    if (ctx->batch_read) return CJ_OK;
+    const size_t n = ctx->n_segs;
+    ctx->h_bseg_out.resize(n);
+    ctx->h_seg_err.resize(n);
+    ctx->h_seg_depth.resize(n);
+    ctx->h_layout_off.resize(n + 1);
+    CJ_CUDA(cudaMemcpyAsync(ctx->h_ctrl, ctx->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, ctx->stream));
+    CJ_CUDA(cudaMemcpyAsync(ctx->h_bseg_out.data(), ctx->seg_out.p, n * sizeof(SegmentOut),
+                            cudaMemcpyDeviceToHost, ctx->stream));
+    CJ_CUDA(cudaMemcpyAsync(ctx->h_seg_err.data(), ctx->seg_err.p, n * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    CJ_CUDA(cudaMemcpyAsync(ctx->h_seg_depth.data(), ctx->seg_depth.p, n * sizeof(int32_t),
+                            cudaMemcpyDeviceToHost, ctx->stream));
+    CJ_CUDA(cudaMemcpyAsync(ctx->h_layout_off.data(), ctx->layout_off.p, (n + 1) * sizeof(uint64_t),
+                            cudaMemcpyDeviceToHost, ctx->stream));
+    CJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->batch_read = true;
+    return CJ_OK;
+}
+
+cj_status doc_verdict(const cj_context* ctx, size_t i)
+{
+    if (ctx->h_ctrl->error_flags & CJ_FLAG_TIMEOUT) return CJ_ERR_TIMEOUT;
+    const uint32_t e = ctx->h_seg_err[i];
+    if (e & CJ_FLAG_UTF8) return CJ_ERR_INVALID_UTF8;
+    if (e & CJ_FLAG_BRACKETS) return CJ_ERR_INVALID_BRACKETS;
+    return CJ_OK;
+}
+
 cj_status finish(cj_status st) { g_last_status = st; return st; }
 
 }  // namespace
@@ -389,6 +681,9 @@ void cj_context_destroy(cj_context* ctx)
     release(ctx->desc_flag); release(ctx->desc_agg); release(ctx->desc_incl);
     release(ctx->segs); release(ctx->seg_out); release(ctx->tile_seg);
     release(ctx->spine); release(ctx->cinfo); release(ctx->tree);
+    release(ctx->seg_err); release(ctx->seg_depth); release(ctx->rchunk_off);
+    release(ctx->layout_off); release(ctx->layout); release(ctx->pack); release(ctx->pack_off);
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     if (ctx->d_ctrl) cudaFree(ctx->d_ctrl);
     if (ctx->h_ctrl) cudaFreeHost(ctx->h_ctrl);
     if (ctx->h_seg_out) cudaFreeHost(ctx->h_seg_out);
@@ -567,6 +862,131 @@ cj_status cj_staged_device_outputs(cj_context* ctx, const int32_t** d_positions,
     if (d_positions) *d_positions = ctx->pos.p;
     if (d_pair_row) *d_pair_row = ctx->pair.p;
     return CJ_OK;
+}
+
+cj_status cj_stage_batch(cj_context* ctx, const uint8_t* const* docs, const size_t* sizes, size_t n_docs,
+                         int lines_mode)
+{
+    if (!ctx || !docs) return finish(CJ_ERR_INVALID_ARGUMENT);
+    return finish(stage_batch(ctx, docs, nullptr, sizes, n_docs, lines_mode != 0));
+}
+
+cj_status cj_stage_batch_packed(cj_context* ctx, const uint8_t* packed, const size_t* sizes, size_t n_docs,
+                                int lines_mode)
+{
+    if (!ctx || !packed) return finish(CJ_ERR_INVALID_ARGUMENT);
+    return finish(stage_batch(ctx, nullptr, packed, sizes, n_docs, lines_mode != 0));
+}
+
+cj_status cj_batch_info(cj_context* ctx, int32_t* status, int64_t* n_structural, int32_t* max_depth,
+                        int64_t* layout_offsets, size_t n_docs)
+{
+    if (!ctx) return finish(CJ_ERR_INVALID_ARGUMENT);
+    cj_status st = read_batch(ctx);
+    if (st) return finish(st);
+    if (n_docs != ctx->n_segs) return finish(CJ_ERR_INVALID_ARGUMENT);
+    for (size_t i = 0; i < n_docs; i++) {
+        if (status) status[i] = doc_verdict(ctx, i);
+        if (n_structural) n_structural[i] = std::min<int64_t>(ctx->h_bseg_out[i].s_end, ctx->h_segs[i].len);
+        if (max_depth) max_depth[i] = ctx->h_seg_depth[i];
+    }
+    if (layout_offsets)
+        for (size_t i = 0; i <= n_docs; i++) layout_offsets[i] = (int64_t)ctx->h_layout_off[i];
+    return finish(CJ_OK);
+}
+
+cj_status cj_copy_batch_result(cj_context* ctx, int32_t* host_out, size_t out_cap)
+{
+    if (!ctx || !host_out) return finish(CJ_ERR_INVALID_ARGUMENT);
+    cj_status st = read_batch(ctx);
+    if (st) return finish(st);
+    const uint64_t total = ctx->h_layout_off[ctx->n_segs];
+    if (total > out_cap) return finish(CJ_ERR_CAPACITY);
+    if (cudaMemcpyAsync(host_out, ctx->layout.p, total * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                        ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+        return finish(CJ_ERR_CUDA);
+    return finish(CJ_OK);
+}
+
+cj_status cj_run_staged_graph(cj_context* ctx)
+{
+    if (!ctx) return finish(CJ_ERR_INVALID_ARGUMENT);
+    return finish(run_graph(ctx));
+}
+
+cj_status cj_context_set_tuning(cj_context* ctx, const cj_tuning* t)
+{
+    if (!ctx) return CJ_ERR_INVALID_ARGUMENT;
+    uint32_t sc = t ? (uint32_t)std::max(0, t->scan_ctas) : 0u;
+    uint32_t pb = t ? (uint32_t)std::max(0, t->pair_blocks) : 0u;
+    uint32_t pt = t ? (uint32_t)std::max(0, t->pair_threads) : 0u;
+    if (pt && pt != 64 && pt != 128 && pt != 256) return CJ_ERR_INVALID_ARGUMENT;
+    ctx->tune_scan_ctas = sc;
+    ctx->tune_pair_blocks = pb;
+    ctx->tune_pair_threads = pt;
+    ctx->graph_valid = false;
+    return CJ_OK;
+}
+
+cj_status cj_context_get_tuning(cj_context* ctx, cj_tuning* t)
+{
+    if (!ctx || !t) return CJ_ERR_INVALID_ARGUMENT;
+    t->scan_ctas = (int32_t)(ctx->tune_scan_ctas ? std::min(ctx->tune_scan_ctas, ctx->scan_grid) : ctx->scan_grid);
+    t->pair_blocks = (int32_t)ctx->tune_pair_blocks;
+    t->pair_threads = (int32_t)pair_threads(ctx);
+    t->ms = 0.f;
+    return CJ_OK;
+}
+
+cj_status cj_autotune_staged(cj_context* ctx, int32_t reps, cj_tuning* best, cj_tuning* tried,
+                             size_t tried_cap, size_t* n_tried)
+{
+    if (!ctx || reps < 1) return finish(CJ_ERR_INVALID_ARGUMENT);
+    if (!ctx->staged) return finish(CJ_ERR_NOT_STAGED);
+    CJ_CUDA(cudaSetDevice(ctx->device));
+    const uint32_t full = ctx->scan_grid, sm = (uint32_t)ctx->sm_count;
+    std::vector<cj_tuning> cand;
+    for (uint32_t scan : {full, std::max(1u, full * 3 / 4), std::max(1u, full / 2)})
+        for (int pt : {128, 256})
+            for (uint32_t pb : {0u, sm * 2, sm * 4}) {
+                cj_tuning t;
+                t.scan_ctas = (int32_t)scan;
+                t.pair_threads = pt;
+                t.pair_blocks = (int32_t)pb;
+                t.ms = 0.f;
+                cand.push_back(t);
+            }
+    cudaEvent_t e0, e1;
+    CJ_CUDA(cudaEventCreate(&e0));
+    CJ_CUDA(cudaEventCreate(&e1));
+    cj_tuning keep;
+    cj_context_get_tuning(ctx, &keep);
+    float best_ms = 1e30f;
+    cj_tuning win = cand[0];
+    size_t k = 0;
+    for (cj_tuning& t : cand) {
+        cj_context_set_tuning(ctx, &t);
+        cj_status st = run_graph(ctx);   // capture + one untimed replay
+        if (st) { cudaEventDestroy(e0); cudaEventDestroy(e1); return finish(st); }
+        if (cudaEventRecord(e0, ctx->stream) != cudaSuccess) return finish(CJ_ERR_CUDA);
+        for (int r = 0; r < reps; r++)
+            if ((st = run_graph(ctx))) { cudaEventDestroy(e0); cudaEventDestroy(e1); return finish(st); }
+        if (cudaEventRecord(e1, ctx->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess)
+            return finish(CJ_ERR_CUDA);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        t.ms = ms / (float)reps;
+        if (tried && k < tried_cap) tried[k] = t;
+        k++;
+        if (t.ms < best_ms) { best_ms = t.ms; win = t; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (n_tried) *n_tried = k;
+    cj_context_set_tuning(ctx, &win);
+    if (best) *best = win;
+    return finish(CJ_OK);
 }
 
 const char* cj_status_string(int status)

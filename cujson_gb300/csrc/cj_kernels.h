@@ -23,6 +23,9 @@ struct ScanParams {
     Ctrl* ctrl;
     SegmentOut* seg_out;
     uint32_t epoch;
+    uint32_t* seg_err;          // per-segment verdict bits (independent documents),
+                                // nullptr: verdicts go to ctrl->error_flags
+    uint32_t one;               // 1 (a run-time value, see classify_words)
 };
 
 struct PairParams {
@@ -36,13 +39,40 @@ struct PairParams {
     Ctrl* ctrl;
     uint32_t epoch;
     uint32_t chunk_cap;
+    // Independent documents (batch): each document's bracket records start on
+    // a chunk boundary at its segment's brk_base, so a chunk never holds two
+    // documents; the record count of a segment is its seg_out[].k_end.  Only
+    // chunks that hold records are work items: rchunk_off[d] is the number of
+    // such chunks before document d (n_bsegs + 1 entries).  Chunks without
+    // records keep the cinfo fill kNoLevel.  Verdicts and depths go per segment.
+    // rchunk_off == nullptr: one record sequence of ctrl->k_total records.
+    const uint64_t* rchunk_off;
+    uint32_t n_bsegs;
+    const Segment* segs;
+    const SegmentOut* seg_out;
+    uint32_t* seg_err;
+    int32_t* seg_depth;
+    uint64_t n_chunks;                    // size of the batch's chunk index space
 };
+
+// cinfo fill of a batch chunk without records (bytes 0x7F): above every level
+constexpr int32_t kNoLevel = 0x7F7F7F7F;
 
 void launch_scan(const ScanParams& p, bool lines, int grid, cudaStream_t stream);
 cudaError_t scan_configure();      // opt in to the scan kernel's dynamic shared memory
 size_t scan_smem_bytes();
 const void* scan_kernel_ptr();     // for occupancy queries
-void launch_pair(const PairParams& p, int grid, cudaStream_t stream);
-void launch_spine(const PairParams& p, int grid, cudaStream_t stream);
+void launch_pair(const PairParams& p, int grid, cudaStream_t stream, int threads = 256);
+void launch_spine(const PairParams& p, int grid, cudaStream_t stream, int threads = 256);
+
+// batches of independent documents (cj_batch.cu)
+void launch_batch_scatter(const uint8_t* packed, const uint64_t* src_off, const uint64_t* word_off,
+                          const Segment* segs, uint32_t n, uint64_t total_words, uint8_t* in, int sm_count,
+                          cudaStream_t stream);
+void launch_batch_prefix(const Segment* segs, const SegmentOut* seg_out, uint32_t n, uint64_t* layout_off,
+                         uint64_t* rchunk_off, cudaStream_t stream);
+void launch_batch_layout(const Segment* segs, const SegmentOut* seg_out, uint32_t n, const int32_t* pos,
+                         const int32_t* pair, const uint64_t* off, int32_t* layout, int sm_count,
+                         cudaStream_t stream);
 
 }  // namespace cj

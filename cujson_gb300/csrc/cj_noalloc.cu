@@ -191,7 +191,8 @@ cj_status parse_noalloc(const uint8_t* d_data, size_t size, int32_t* d_out, size
     if ((st = cuda_status(cudaMemcpyAsync(s->in, d_data, size, cudaMemcpyDeviceToDevice, stream)))) return st;
     noalloc_setup<<<1, 32, 0, stream>>>(s, size);
 
-    ScanParams sp;
+    ScanParams sp{};
+    sp.one = 1;
     sp.in = s->in;
     sp.segs = &s->seg;
     sp.tile_seg = nullptr;
@@ -208,7 +209,7 @@ cj_status parse_noalloc(const uint8_t* d_data, size_t size, int32_t* d_out, size
     sp.epoch = epoch;
     launch_scan(sp, false, (int)std::min<uint32_t>(n_tiles, d->scan_grid), stream);
 
-    PairParams pp;
+    PairParams pp{};
     pp.brk = s->brk;
     pp.pair = s->pair;
     pp.spine = s->spine;

@@ -86,6 +86,18 @@ __device__ int64_t next_le(const PairParams& P, uint64_t nch, uint64_t c, int32_
     return (int64_t)i;
 }
 
+// batch: the document of work item w, largest d with rchunk_off[d] <= w
+__device__ __forceinline__ uint32_t doc_of_item(const PairParams& P, uint64_t w)
+{
+    uint32_t lo = 0, hi = P.n_bsegs;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldcg(P.rchunk_off + mid) <= w) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
 }  // namespace
 
 __global__ void __launch_bounds__(256) pair_chunks(PairParams P)
@@ -95,16 +107,30 @@ __global__ void __launch_bounds__(256) pair_chunks(PairParams P)
     const int wib = threadIdx.x >> 5;
     uint32_t* heads = s_heads_all + wib * kHeads;
     const uint32_t FULL = 0xFFFFFFFFu;
-    const uint32_t K = P.ctrl->k_total;
-    const uint64_t nch = ((uint64_t)K + kChunk - 1) / kChunk;
+    const bool batch = P.rchunk_off != nullptr;
+    const uint32_t K = batch ? 0u : P.ctrl->k_total;
+    const uint64_t items = batch ? __ldcg(P.rchunk_off + P.n_bsegs) : ((uint64_t)K + kChunk - 1) / kChunk;
     const uint64_t gwarp = (uint64_t)blockIdx.x * (blockDim.x >> 5) + wib;
     const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
     const uint32_t lt = lanemask_lt(), gt = lanemask_gt();
-    uint32_t err = 0;
 
-    for (uint64_t c = gwarp; c < nch; c += nwarps) {
+    for (uint64_t w = gwarp; w < items; w += nwarps) {
+        uint64_t c = w;
+        int cnt;
+        uint32_t segi = 0;
+        int32_t* __restrict__ pair = P.pair;
+        if (batch) {
+            segi = doc_of_item(P, w);
+            const uint64_t local = w - __ldcg(P.rchunk_off + segi);
+            c = __ldg(&P.segs[segi].brk_base) / kChunk + local;
+            const uint64_t left = (uint64_t)__ldcg(&P.seg_out[segi].k_end) - local * kChunk;
+            cnt = (int)min((uint64_t)kChunk, left);
+            pair += __ldg(&P.segs[segi].out_base);
+        } else {
+            cnt = (int)min((uint64_t)kChunk, (uint64_t)K - c * kChunk);
+        }
         const uint64_t base = c * kChunk;
-        const int cnt = (int)min((uint64_t)kChunk, (uint64_t)K - base);
+        uint32_t err = 0;
         for (int i = lane; i < kHeads; i += 32) heads[i] = kEmpty;
         const uint2 r0 = __ldcg(P.brk + base);
         const int32_t L0 = (int32_t)r0.y >> 1;
@@ -143,7 +169,7 @@ __global__ void __launch_bounds__(256) pair_chunks(PairParams P)
                 }
                 if (partner != kEmpty) {
                     if ((partner ^ rec.x) & kCurly) err |= CJ_FLAG_BRACKETS;
-                    P.pair[partner & ~kCurly] = (int32_t)((rec.x & ~kCurly) + 1u);
+                    pair[partner & ~kCurly] = (int32_t)((rec.x & ~kCurly) + 1u);
                 }
             }
             __syncwarp();
@@ -173,9 +199,17 @@ __global__ void __launch_bounds__(256) pair_chunks(PairParams P)
                 else err |= CJ_FLAG_BRACKETS;
             }
         }
+        err = __reduce_or_sync(FULL, err);
         if (lane == 0) {
             P.cinfo[c] = make_int4(d_entry, dmin, d_exit, 0);
-            if (dmin < 0) atomicMax(&P.ctrl->neg_min_level, -dmin);
+            if (batch) {
+                if (dmin < 0) err |= CJ_FLAG_BRACKETS;
+                if (err) atomicOr(P.seg_err + segi, err);
+                if (maxd > 0) atomicMax(P.seg_depth + segi, maxd);
+            } else {
+                if (dmin < 0) atomicMax(&P.ctrl->neg_min_level, -dmin);
+                if (err) atomicOr(&P.ctrl->error_flags, err);
+            }
             if (maxd > 0) atomicMax(&P.ctrl->max_depth, maxd);
             const unsigned long long pk = tree_pack(P.epoch, dmin);
             for (int l = 1; l <= kTreeLevels; l++)
@@ -183,51 +217,69 @@ __global__ void __launch_bounds__(256) pair_chunks(PairParams P)
         }
         __syncwarp();
     }
-    err = __reduce_or_sync(FULL, err);
-    if (lane == 0 && err) atomicOr(&P.ctrl->error_flags, err);
 }
 
 __global__ void __launch_bounds__(256) pair_spine(PairParams P)
 {
     const int lane = threadIdx.x & 31;
-    const uint32_t K = P.ctrl->k_total;
-    const uint32_t S = P.ctrl->s_total;
-    const uint64_t nch = ((uint64_t)K + kChunk - 1) / kChunk;
+    const bool batch = P.rchunk_off != nullptr;
+    const uint32_t K = batch ? 0u : P.ctrl->k_total;
+    const uint64_t nch = batch ? P.n_chunks : ((uint64_t)K + kChunk - 1) / kChunk;
+    const uint64_t items = batch ? __ldcg(P.rchunk_off + P.n_bsegs) : nch;
     const uint64_t gwarp = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
-    uint32_t err = 0;
-    for (uint64_t c = gwarp; c < nch; c += nwarps) {
+    for (uint64_t w = gwarp; w < items; w += nwarps) {
+        uint32_t err = 0;
+        uint32_t segi = 0, S;
+        uint64_t c = w, c_end = nch;               // chunks of this record sequence: [.., c_end)
+        int32_t* __restrict__ pair = P.pair;
+        if (batch) {
+            segi = doc_of_item(P, w);
+            const uint64_t first = __ldg(&P.segs[segi].brk_base) / kChunk;
+            c = first + (w - __ldcg(P.rchunk_off + segi));
+            c_end = first + (__ldcg(P.rchunk_off + segi + 1) - __ldcg(P.rchunk_off + segi));
+            S = __ldcg(&P.seg_out[segi].s_end);
+            pair += __ldg(&P.segs[segi].out_base);
+        } else {
+            S = P.ctrl->s_total;
+        }
         const int4 ci = __ldcg(&P.cinfo[c]);
         const int32_t n_uo = ci.z - ci.y;          // opens still open at chunk end
         const int32_t n_uc = ci.x - ci.y;          // closes unmatched inside the chunk
-        if (n_uo < 0 || n_uc < 0 || n_uo + n_uc > kChunk) { err |= CJ_FLAG_BRACKETS; continue; }
-        for (int32_t i = lane; i < n_uo; i += 32) {
-            const int32_t d = ci.y + i;
-            const uint32_t ox = __ldcg(P.spine + c * kChunk + (kChunk - 1 - i));
-            const int64_t c2 = next_le(P, nch, c, d);
-            if (c2 < 0) { err |= CJ_FLAG_BRACKETS; continue; }
-            const int4 cj2 = __ldcg(&P.cinfo[c2]);
-            const int32_t idx = cj2.x - 1 - d;
-            if (idx < 0 || idx >= kChunk || idx >= cj2.x - cj2.y) { err |= CJ_FLAG_BRACKETS; continue; }
-            const uint32_t cx = __ldcg(P.spine + (uint64_t)c2 * kChunk + idx);
-            if ((ox ^ cx) & kCurly) err |= CJ_FLAG_BRACKETS;
-            if ((ox & ~kCurly) >= S || (cx & ~kCurly) >= S) { err |= CJ_FLAG_BRACKETS; continue; }
-            P.pair[ox & ~kCurly] = (int32_t)((cx & ~kCurly) + 1u);
+        if (n_uo < 0 || n_uc < 0 || n_uo + n_uc > kChunk) {
+            err = CJ_FLAG_BRACKETS;
+        } else {
+            for (int32_t i = lane; i < n_uo; i += 32) {
+                const int32_t d = ci.y + i;
+                const uint32_t ox = __ldcg(P.spine + c * kChunk + (kChunk - 1 - i));
+                const int64_t c2 = next_le(P, nch, c, d);
+                if (c2 < 0) { err |= CJ_FLAG_BRACKETS; continue; }
+                if ((uint64_t)c2 >= c_end) { err |= CJ_FLAG_BRACKETS; continue; }   // past the document
+                const int4 cj2 = __ldcg(&P.cinfo[c2]);
+                const int32_t idx = cj2.x - 1 - d;
+                if (idx < 0 || idx >= kChunk || idx >= cj2.x - cj2.y) { err |= CJ_FLAG_BRACKETS; continue; }
+                const uint32_t cx = __ldcg(P.spine + (uint64_t)c2 * kChunk + idx);
+                if ((ox ^ cx) & kCurly) err |= CJ_FLAG_BRACKETS;
+                if ((ox & ~kCurly) >= S || (cx & ~kCurly) >= S) { err |= CJ_FLAG_BRACKETS; continue; }
+                pair[ox & ~kCurly] = (int32_t)((cx & ~kCurly) + 1u);
+            }
         }
+        err = __reduce_or_sync(0xFFFFFFFFu, err);
+        if (lane == 0 && err) atomicOr(batch ? P.seg_err + segi : &P.ctrl->error_flags, err);
     }
-    err = __reduce_or_sync(0xFFFFFFFFu, err);
-    if (lane == 0 && err) atomicOr(&P.ctrl->error_flags, err);
 }
 
-void launch_pair(const PairParams& p, int grid, cudaStream_t stream)
+void launch_pair(const PairParams& p, int grid, cudaStream_t stream, int threads)
 {
-    const size_t smem = sizeof(uint32_t) * kHeads * 8;   // 32.8 KB: under the 48 KB default
-    pair_chunks<<<grid, 256, smem, stream>>>(p);
+    // one bucket-head table per warp: 4.1 KB each, 32.8 KB at 256 threads
+    // (threads <= 256 stays under the 48 KB default)
+    const size_t smem = sizeof(uint32_t) * kHeads * (size_t)(threads / 32);
+    pair_chunks<<<grid, threads, smem, stream>>>(p);
 }
 
-void launch_spine(const PairParams& p, int grid, cudaStream_t stream)
+void launch_spine(const PairParams& p, int grid, cudaStream_t stream, int threads)
 {
-    pair_spine<<<grid, 256, 0, stream>>>(p);
+    pair_spine<<<grid, threads, 0, stream>>>(p);
 }
 
 }  // namespace cj

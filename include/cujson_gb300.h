@@ -5,7 +5,7 @@
  * drop-in C++ headers include/cujson/cujson.h and include/cujson/cujsonlines.h
  * (which keep the reference's type layouts and function names) are thin
  * inline wrappers over these entry points; other languages bind them directly
- * (see INTEGRATION.md for the ctypes / cgo / JNI stubs).
+ * (ctypes, cgo, JNI).
  *
  * Reference interfaces replaced (file:line within AutomataLab/cuJSON):
  *   cj_parse_standard  <- cuJSONResult parse_standard_json(cuJSONInput)
@@ -159,6 +159,98 @@ cj_status cj_copy_staged_result(cj_context* ctx, int32_t* host_out, size_t out_c
  * close index for opens, else 0). */
 cj_status cj_staged_device_outputs(cj_context* ctx, const int32_t** d_positions,
                                    const int32_t** d_pair_row);
+
+/* Replays the staged run as a CUDA graph: the first call after staging (or
+ * after a tuning change) captures every memset and kernel of the run into a
+ * graph; later calls launch that graph.  Results as cj_run_staged. */
+cj_status cj_run_staged_graph(cj_context* ctx);
+
+/* ---- batches of independent documents ---------------------------------------
+ * No counterpart in the reference, which parses one document per call
+ * (parse_standard_json, cujson/parse_standard_json.cu:1584).  n_docs standard
+ * documents are parsed by one run (one scan launch over all of them, then
+ * the pairing and a layout kernel); each keeps its own string state, depth,
+ * positions and verdict, exactly as if it had been parsed alone.
+ *
+ * cj_stage_batch copies each document (host pointers, pinned for speed);
+ * cj_stage_batch_packed takes the documents back to back in one host buffer
+ * and copies them with one transfer.  lines_mode != 0: every document is a
+ * JSON-Lines buffer parsed as one chunk (as cj_parse_lines with one chunk).  Then cj_run_staged or
+ * cj_run_staged_graph; then cj_batch_info (per document: status, S, depth,
+ * and the offsets of each document's result in the batch layout, n_docs+1
+ * entries in int32 units) and cj_copy_batch_result (every document's
+ * 2*(S+2) reference layout, back to back, at those offsets).  A document
+ * whose status is not CJ_OK has a layout of unspecified content. */
+cj_status cj_stage_batch(cj_context* ctx, const uint8_t* const* docs, const size_t* sizes,
+                         size_t n_docs, int lines_mode);
+cj_status cj_stage_batch_packed(cj_context* ctx, const uint8_t* packed, const size_t* sizes,
+                                size_t n_docs, int lines_mode);
+cj_status cj_batch_info(cj_context* ctx, int32_t* status, int64_t* n_structural, int32_t* max_depth,
+                        int64_t* layout_offsets, size_t n_docs);
+cj_status cj_copy_batch_result(cj_context* ctx, int32_t* host_out, size_t out_cap);
+
+/* ---- launch shapes and the autotuner ----------------------------------------
+ * scan_ctas: persistent scan CTAs (at most one per SM fits); pair_blocks and
+ * pair_threads (64, 128 or 256): the pairing kernels' grid.  0 = default.
+ * cj_autotune_staged times `reps` graph replays of the staged input for each
+ * candidate shape, keeps the fastest in the context and reports it (and,
+ * optionally, every candidate tried with its mean milliseconds). */
+typedef struct cj_tuning {
+    int32_t scan_ctas;
+    int32_t pair_blocks;
+    int32_t pair_threads;
+    float   ms;                  /* mean replay time when measured */
+} cj_tuning;
+cj_status cj_context_set_tuning(cj_context* ctx, const cj_tuning* tuning);   /* NULL: defaults */
+cj_status cj_context_get_tuning(cj_context* ctx, cj_tuning* tuning);
+cj_status cj_autotune_staged(cj_context* ctx, int32_t reps, cj_tuning* best, cj_tuning* tried,
+                             size_t tried_cap, size_t* n_tried);
+
+/* ---- serving: a request loop with continuous batching -------------------------
+ * No counterpart in the reference.  A server owns `slots` contexts on one
+ * device and a scheduler thread.  Any host thread submits documents (standard
+ * or JSON Lines, one chunk); the scheduler batches waiting requests of one
+ * kind, oldest first, admitting them while a batch stays within
+ * max_batch_docs and the slot's share of `memory_budget` (device bytes), and
+ * keeps up to `slots` batches in flight so that the copies of one overlap
+ * the kernels of another.  Requests that arrive meanwhile join the next batch
+ * as soon as a slot frees up.  Each request is parsed as an independent
+ * document: its result is the same alone and in any mix.  `data` must stay
+ * valid (and unchanged) until the request has completed; pinned memory makes
+ * its copy asynchronous.  A document too large for a slot's share of the
+ * budget is refused at submission (CJ_ERR_TOO_LARGE). */
+typedef struct cj_server cj_server;
+typedef struct cj_server_config {
+    int32_t  device;             /* -1: current device */
+    uint32_t slots;              /* batches in flight, 1..8 (0: 2) */
+    uint32_t max_batch_docs;     /* 0: 1024 */
+    uint64_t memory_budget;      /* device bytes for requests in flight (0: 16 GiB) */
+} cj_server_config;
+typedef struct cj_server_stats {
+    uint64_t batches, docs, bytes, max_batch_docs;
+    uint64_t peak_admitted_bytes;   /* largest device-byte estimate admitted to one batch */
+    uint64_t device_bytes;          /* arena bytes the slots hold now */
+    int32_t  fault;                 /* first failure of a batch, or CJ_OK */
+} cj_server_stats;
+cj_status cj_server_create(const cj_server_config* cfg, cj_server** out);
+void      cj_server_destroy(cj_server* s);   /* finishes the requests in flight first */
+cj_status cj_server_submit(cj_server* s, const uint8_t* data, size_t size, int lines_mode,
+                           uint64_t* ticket);
+/* Waits for a request (timeout_ms < 0: no limit; CJ_ERR_TIMEOUT when it
+ * expires); info->status is the request's verdict; latency_s the time from
+ * submission to completion. */
+cj_status cj_server_wait(cj_server* s, uint64_t ticket, int64_t timeout_ms, cj_parse_info* info,
+                         double* latency_s);
+/* Copies a completed request's reference layout (2*(S+2) int32; nothing for
+ * an invalid document) and releases the request; returns its verdict. */
+cj_status cj_server_take(cj_server* s, uint64_t ticket, int32_t* host_out, size_t out_cap);
+cj_status cj_server_get_stats(cj_server* s, cj_server_stats* out);
+/* Load generator: submits docs[i] at arrival_s[i] seconds after the call
+ * (lines[i] != 0: JSON Lines; lines may be NULL), waits for all, and reports
+ * each request's verdict and latency and the time until the last completion. */
+cj_status cj_server_replay(cj_server* s, const uint8_t* const* docs, const size_t* sizes,
+                           const int32_t* lines, const double* arrival_s, size_t n, int32_t* status,
+                           double* latency_s, double* makespan_s);
 
 /* ---- measurement and host memory --------------------------------------------
  * With timing enabled, every run records CUDA events on the context stream

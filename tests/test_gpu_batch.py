@@ -1,0 +1,105 @@
+"""Batches of independent documents (one run for many documents) against the
+oracle and against single-document parses: per-document arrays bit-exact,
+per-document verdicts, graph replays and autotuned launch shapes giving the
+same results."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def check_batch(cj, oracle, docs, results):
+    assert len(results) == len(docs)
+    for i, (d, (st, res)) in enumerate(zip(docs, results)):
+        ref = oracle.parse(d)
+        if ref.flags:
+            want = cj.ERR_INVALID_UTF8 if ref.flags & oracle.ERR_UTF8 else cj.ERR_INVALID_BRACKETS
+            assert st == want, (i, st, ref.flags)
+        else:
+            assert st == cj.OK, (i, st)
+            assert res.n_structural == ref.n_structural, i
+            np.testing.assert_array_equal(res.buffer, ref.reference_layout(), err_msg=f"doc {i}")
+            assert res.max_depth == ref.max_depth, i
+
+
+def mixed_docs(cj, seed=7):
+    docs = [np.frombuffer(b, np.uint8).copy() for b in (
+        b"1", b"[]", b'{"a":"b\\"c,d"}', b"[[[", b"[1,[2]]", b"]]", b"{}", b"[{]}", b"[]",
+        b'"\\\\"', b"   ", b'{"k":[{},[]],"x":{}}', b"\xc0\x80", b'["\xed\xa0\x80"]', b"[\"\xe2\x82\xac\"]")]
+    for k, n in enumerate([1023, 1024, 1025, 4095, 65536, 131071, 131072, 131073, 300001, 1 << 20]):
+        docs.append(cj.synth_document(seed * 100 + k, n, max_depth=10))
+    bad = cj.synth_document(seed * 100 + 50, 200000)
+    assert cj.synth_corrupt(bad, cj.CORRUPT_SURROGATE, 3)
+    docs.append(bad)
+    bad2 = cj.synth_document(seed * 100 + 51, 150000)
+    assert cj.synth_corrupt(bad2, cj.CORRUPT_MISMATCHED, 3)
+    docs.append(bad2)
+    docs.append(cj.synth_deep(100000))
+    docs.append(cj.synth_backslash_string(seed, 300000))
+    return docs
+
+
+def test_batch_per_document_pointers(cj, oracle, ctx):
+    docs = mixed_docs(cj)
+    ctx.stage_batch(docs)
+    ctx.run()
+    check_batch(cj, oracle, docs, ctx.batch_results())
+
+
+def test_batch_packed_and_graph(cj, oracle, ctx):
+    docs = mixed_docs(cj, seed=8)
+    packed = np.concatenate(docs)
+    ctx.stage_batch_packed(packed, [d.size for d in docs])
+    ctx.run_graph()
+    first = ctx.batch_layout()[0].copy()
+    check_batch(cj, oracle, docs, ctx.batch_results())
+    ctx.run_graph()          # replay
+    np.testing.assert_array_equal(ctx.batch_layout()[0], first)
+    ctx.run()                # the same staged batch without the graph
+    np.testing.assert_array_equal(ctx.batch_layout()[0], first)
+
+
+def test_batch_same_alone_and_in_the_mix(cj, ctx):
+    docs = mixed_docs(cj, seed=9)
+    ctx.stage_batch(docs)
+    ctx.run()
+    mixed = ctx.batch_results()
+    for i, d in enumerate(docs):
+        st, res = ctx.try_parse(d)
+        assert st == mixed[i][0], i
+        if st == cj.OK:
+            np.testing.assert_array_equal(res.buffer, mixed[i][1].buffer)
+
+
+def test_batch_generated(cj, oracle, ctx):
+    packed, sizes, kinds = cj.batch_input(0xC0DE1004, 300, 96 << 20)
+    ctx.stage_batch_packed(packed, sizes)
+    ctx.run_graph()
+    res = ctx.batch_results()
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    docs = [packed[offs[i]:offs[i + 1]] for i in range(sizes.size)]
+    check_batch(cj, oracle, docs, res)
+    assert sum(1 for st, _ in res if st != cj.OK) == int((kinds > 0).sum())
+
+
+def test_autotune_keeps_results(cj, oracle, ctx):
+    packed, sizes, _ = cj.batch_input(0xC0DE2004, 64, 16 << 20)
+    ctx.stage_batch_packed(packed, sizes)
+    ctx.run_graph()
+    want = ctx.batch_layout()[0].copy()
+    best, tried = ctx.autotune(reps=2)
+    assert len(tried) >= 6 and best.ms > 0
+    assert min(t.ms for t in tried) == pytest.approx(best.ms)
+    ctx.run_graph()
+    np.testing.assert_array_equal(ctx.batch_layout()[0], want)
+    ctx.set_tuning()   # back to defaults for the other tests
+
+
+def test_single_document_after_batch(cj, oracle, ctx):
+    d = cj.synth_document(1234, 500000)
+    st, res = ctx.try_parse(d)
+    assert st == cj.OK
+    np.testing.assert_array_equal(res.buffer, oracle.parse(d).reference_layout())
+    ctx.stage_standard(d)
+    ctx.run_graph()
+    np.testing.assert_array_equal(ctx.staged_result().buffer, res.buffer)
