@@ -11,16 +11,26 @@ What it builds (each only when the reference tree is present):
   on a machine without a GPU and give the golden query answers under
   tests/golden/.
 
-The reference's parse path is CUDA + Thrust and needs a GPU, and the reference
-tree is not available where a GPU is, so its parse outputs are not built here.
+* refemu_std, refemu_lines -- the reference's parse path itself
+  (cujson/utils.cu, cujson/parse_standard_json.cu, cujson/parse_json_lines.cu)
+  compiled with g++ for the CPU through the CUDA host emulation in
+  oracle/refemu/ (kernels run as fibers, Thrust and the runtime replaced by
+  sequential stand-ins), driven by oracle/refemu/driver.cpp.  The only change
+  to the reference's text is mechanical and made in a temporary copy: every
+  `kernel<<<grid, block>>>(args);` launch becomes a call of the emulator's
+  launch function.  Its outputs are the golden parse vectors under
+  tests/golden/.
 
 usage: python oracle/build_ref.py [reference root]
 """
 from __future__ import annotations
 
 import os
+import re
+import shutil
 import subprocess
 import sys
+import tempfile
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
@@ -37,6 +47,90 @@ def iter_targets(ref: Path):
         "iter_ref_std": (q / "query_iterator_standard_json.cpp", 0),
         "iter_ref_lines": (q / "query_iterator.cpp", 1),
     }
+
+
+EMU = HERE / "refemu"
+LAUNCH = re.compile(r"(\w+)<<<([^<>]+?)>>>\s*\(")
+
+
+def _in_line_comment(text: str, pos: int) -> bool:
+    line_start = text.rfind("\n", 0, pos) + 1
+    return "//" in text[line_start:pos]
+
+
+def _close_paren(text: str, open_pos: int) -> int:
+    """Index of the ')' matching text[open_pos] == '(' (comments and strings skipped)."""
+    depth, i, n = 0, open_pos, len(text)
+    while i < n:
+        c = text[i]
+        if text.startswith("//", i):
+            i = text.find("\n", i)
+            if i < 0:
+                break
+            continue
+        if text.startswith("/*", i):
+            i = text.find("*/", i) + 2
+            continue
+        if c in "\"'":
+            j = i + 1
+            while j < n and text[j] != c:
+                j += 2 if text[j] == "\\" else 1
+            i = j + 1
+            continue
+        if c == "(":
+            depth += 1
+        elif c == ")":
+            depth -= 1
+            if depth == 0:
+                return i
+        i += 1
+    raise ValueError("unbalanced kernel launch")
+
+
+def rewrite_launches(text: str) -> str:
+    """`name<<<g, b>>>(args);` -> `cj_emu::launch(dim3(g), dim3(b), [&] { name(args); });`"""
+    out, pos = [], 0
+    for m in LAUNCH.finditer(text):
+        if m.start() < pos or _in_line_comment(text, m.start()):
+            continue
+        cfg = [c.strip() for c in m.group(2).split(",")]
+        if len(cfg) != 2:
+            raise ValueError(f"unexpected launch configuration: {m.group(0)}")
+        close = _close_paren(text, m.end() - 1)
+        semi = text.index(";", close)
+        out.append(text[pos:m.start()])
+        out.append(f"cj_emu::launch(dim3({cfg[0]}), dim3({cfg[1]}), [&] {{ {m.group(1)}(")
+        out.append(text[m.end():close + 1])
+        out.append("; });")
+        pos = semi + 1
+    out.append(text[pos:])
+    return "".join(out)
+
+
+def build_refemu(ref: Path, force: bool = False) -> dict:
+    src_dir = ref / "cujson"
+    deps = [EMU / "driver.cpp", EMU / "cj_cuda_emu.h", *sorted((EMU / "shim").rglob("*.h")),
+            *sorted((EMU / "shim").rglob("*.cuh")), *sorted(src_dir.glob("*.cu")), *sorted(src_dir.glob("*.h"))]
+    newest = max(p.stat().st_mtime for p in deps)
+    out = {"refemu_std": OUT / "refemu_std", "refemu_lines": OUT / "refemu_lines"}
+    if not force and all(p.exists() and p.stat().st_mtime >= newest for p in out.values()):
+        return out
+    OUT.mkdir(parents=True, exist_ok=True)
+    tmp = Path(tempfile.mkdtemp(prefix="cj_refemu_"))
+    try:
+        for f in src_dir.glob("*.h"):
+            shutil.copy(f, tmp / f.name)
+        for f in src_dir.glob("*.cu"):
+            (tmp / f.name).write_text(rewrite_launches(f.read_text()))
+        for name, lines in (("refemu_std", 0), ("refemu_lines", 1)):
+            cmd = ["g++", "-std=c++17", "-O1", "-w", f"-DCJ_REF_LINES={lines}", f"-I{EMU / 'shim'}",
+                   f"-I{tmp}", "-x", "c++", str(EMU / "driver.cpp"), "-o", str(out[name])]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"reference emulation build failed ({name}):\n{r.stderr[-4000:]}")
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    return out
 
 
 def build(ref: Path = DEFAULT_REF, force: bool = False) -> dict:
@@ -58,6 +152,7 @@ def build(ref: Path = DEFAULT_REF, force: bool = False) -> dict:
             if r.returncode != 0:
                 raise RuntimeError(f"reference iterator build failed:\n{r.stderr}")
         built[name] = exe
+    built.update(build_refemu(ref, force))
     return built
 
 

@@ -1,0 +1,2 @@
+#pragma once
+#include "cj_thrust_emu.h"
