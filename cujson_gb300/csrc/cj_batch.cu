@@ -138,8 +138,15 @@ __global__ void __launch_bounds__(1024) batch_prefix(const Segment* __restrict__
     }
 }
 
-// Each document's reference layout at off[d]: [0]=0, [1..S] positions,
-// [S+1]=S+1, [S+2..2S+1] pair row, [2S+2], [2S+3] = 0.
+// Every document's reference layout, flat over the whole batch: element g of
+// the layout buffer belongs to document d with off[d] <= g < off[d+1] and is,
+// with i = g - off[d] and S = S_d, [0]=0, [1..S] positions, [S+1]=S+1,
+// [S+2..2S+1] pair row, [2S+2], [2S+3] = 0.  A warp writes a run of
+// 32 * kLayoutRun consecutive elements, lane l the elements base + 32k + l
+// (coalesced); lane 0 finds the run's first document by binary search and
+// every lane then walks forward through the documents its elements reach.
+constexpr int kLayoutRun = 16;
+
 __global__ void __launch_bounds__(256) batch_layout(const Segment* __restrict__ segs,
                                                     const SegmentOut* __restrict__ seg_out, uint32_t n,
                                                     const int32_t* __restrict__ pos,
@@ -147,21 +154,45 @@ __global__ void __launch_bounds__(256) batch_layout(const Segment* __restrict__ 
                                                     const uint64_t* __restrict__ off,
                                                     int32_t* __restrict__ layout)
 {
-    for (uint32_t d = blockIdx.x; d < n; d += gridDim.x) {
-        const uint64_t S = min((uint64_t)__ldcg(&seg_out[d].s_end), (uint64_t)__ldg(&segs[d].len));
-        const uint64_t b = __ldg(&segs[d].out_base);
-        int32_t* L = layout + __ldcg(off + d);
-        for (uint64_t i = threadIdx.x; i < S + 2; i += blockDim.x) {
-            if (i == 0) {
-                L[0] = 0;
-                L[S + 1] = (int32_t)(S + 1);
-            } else if (i <= S) {
-                L[i] = __ldcg(pos + b + i - 1);
-                L[S + 1 + i] = __ldcg(pair + b + i - 1);
-            } else {
-                L[2 * S + 2] = 0;
-                L[2 * S + 3] = 0;
+    const int lane = threadIdx.x & 31;
+    const uint64_t total = __ldcg(off + n);
+    const uint64_t per_run = 32ull * kLayoutRun;
+    const uint64_t runs = (total + per_run - 1) / per_run;
+    const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for (uint64_t r = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < runs; r += nwarps) {
+        const uint64_t g0 = r * per_run;
+        uint32_t d = 0;
+        if (lane == 0) {
+            uint32_t lo = 0, hi = n;        // off[lo] <= g0 < off[hi]
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (__ldcg(off + mid) <= g0) lo = mid;
+                else hi = mid;
             }
+            d = lo;
+        }
+        d = __shfl_sync(FULL, d, 0);
+        uint64_t dbeg = __ldcg(off + d), dend = __ldcg(off + d + 1);
+        uint64_t S = min((uint64_t)__ldcg(&seg_out[d].s_end), (uint64_t)__ldg(&segs[d].len));
+        uint64_t b = __ldg(&segs[d].out_base);
+        for (int k = 0; k < kLayoutRun; k++) {
+            const uint64_t g = g0 + 32ull * k + lane;
+            if (g >= total) break;
+            while (g >= dend) {
+                d++;
+                dbeg = dend;
+                dend = __ldcg(off + d + 1);
+                S = min((uint64_t)__ldcg(&seg_out[d].s_end), (uint64_t)__ldg(&segs[d].len));
+                b = __ldg(&segs[d].out_base);
+            }
+            const uint64_t i = g - dbeg;
+            int32_t v;
+            if (i == 0) v = 0;
+            else if (i <= S) v = __ldcg(pos + b + i - 1);
+            else if (i == S + 1) v = (int32_t)(S + 1);
+            else if (i <= 2 * S + 1) v = __ldcg(pair + b + (i - S - 2));
+            else v = 0;
+            layout[g] = v;
         }
     }
 }
@@ -186,8 +217,7 @@ void launch_batch_layout(const Segment* segs, const SegmentOut* seg_out, uint32_
                          const int32_t* pair, const uint64_t* off, int32_t* layout, int sm_count,
                          cudaStream_t stream)
 {
-    const int grid = (int)std::min<uint32_t>(n, (uint32_t)sm_count * 8);
-    batch_layout<<<grid, 256, 0, stream>>>(segs, seg_out, n, pos, pair, off, layout);
+    batch_layout<<<sm_count * 8, 256, 0, stream>>>(segs, seg_out, n, pos, pair, off, layout);
 }
 
 }  // namespace cj

@@ -156,53 +156,62 @@ CJ_HD uint32_t mad_u32(uint32_t a, uint32_t b, uint32_t c) {
 #endif
 }
 
-// acc + (gathered nibble of m << sh): the multiply and the placement run on
-// the multiply-add pipe, only the shift on the ALU
-CJ_HD uint32_t gather4_into(uint32_t m, int sh, uint32_t acc) {
-    return mad_u32(gather4(m), 1u << sh, acc);
+// (acc << 4) | nibble of m's bits 7/15/23/31: the gathering multiply runs on
+// the multiply-add pipe, one funnel shift on the ALU both extracts the
+// nibble and appends it
+CJ_HD uint32_t gather_step(uint32_t m, uint32_t acc) {
+#ifdef __CUDA_ARCH__
+    return __funnelshift_l(m * 0x00204081u, acc, 4);
+#else
+    return (acc << 4) | ((m * 0x00204081u) >> 28);
+#endif
 }
 
 struct Classes {
-    uint32_t q, bs, st, op, cl, cur, hi;
+    uint32_t q, bs, st, op, br, cur, hi;
 };
 
 // Character classes of N*4 bytes held as N little-endian words; bit j of each
-// mask is byte j.  `hi` keeps the high bits of all bytes (non-ASCII test).
-// Each equality test is a zero-byte test on (low 7 bits ^ pattern) + 0x7F per
-// byte (the high bit of the sum is set unless the byte matched), combined with
-// the byte's own high bit; '[' and '{' (and ']' and '}') share one test on the
-// byte with bit 5 cleared.  The per-byte results (bit 7 of each byte) are
-// gathered into bit masks by multiplication (gather4_into).
+// mask is byte j: quote, backslash, structural ({ } [ ] : , and '\n' in
+// JSON-Lines mode), open ({ [), bracket (any of { } [ ]), curly ({ }) and
+// `hi` (the high bits of all bytes, the non-ASCII test).
+//
+// Per byte b (7-bit part b7 = b & 0x7F, no carry between bytes), bit 7 of
+// b7 + (0x80 - t) is [b7 >= t], so [b7 == t] = [b7 >= t] xor [b7 >= t+1]; the
+// threshold additions run on the multiply-add pipe as b7 * one + (0x80 - t)
+// (`one` is 1, passed at run time so the compiler keeps the multiply-add), and
+// one three-input logic operation per class combines two thresholds with the
+// byte's own high bit.  '[' / '{' and ']' / '}' are compared after clearing
+// bit 5 (0x5B and 0x5D), and bit 5 itself tells curly from square.
 template <bool LINES, int N>
-CJ_HD Classes classify_words(const uint32_t* w) {
-    const uint32_t H = 0x80808080u, K = 0x7F7F7F7Fu;
+CJ_HD Classes classify_words(const uint32_t* w, uint32_t one) {
+    const uint32_t H = 0x80808080u;
     Classes c;
-    c.q = c.bs = c.st = c.op = c.cl = c.cur = c.hi = 0;
+    c.q = c.bs = c.st = c.op = c.br = c.cur = c.hi = 0;
+    const uint32_t four = one << 2;
 #pragma unroll
-    for (int k = 0; k < N; k++) {
+    for (int k = N - 1; k >= 0; k--) {
         const uint32_t x = w[k];
-        const uint32_t xl = x & K, yl = x & 0x5F5F5F5Fu;
-        const uint32_t tq = (xl ^ 0x22222222u) + K;
-        const uint32_t tb = (xl ^ 0x5C5C5C5Cu) + K;
-        const uint32_t to = (yl ^ 0x5B5B5B5Bu) + K;
-        const uint32_t tc = (yl ^ 0x5D5D5D5Du) + K;
-        const uint32_t tn = (xl ^ 0x3A3A3A3Au) + K;
-        const uint32_t tm = (xl ^ 0x2C2C2C2Cu) + K;
-        uint32_t tall = to & tc & tn & tm;
-        if (LINES) tall &= (xl ^ 0x0A0A0A0Au) + K;
-        const uint32_t q = ~(tq | x) & H;
-        const uint32_t b = ~(tb | x) & H;
-        const uint32_t o = ~(to | x) & H;
-        const uint32_t cl = ~(tc | x) & H;
-        const uint32_t s = ~(tall | x) & H;
-        const uint32_t cu = (x << 2) & (o | cl);   // bit 5 (curly) -> bit 7
-        const int sh = 4 * k;
-        c.q = gather4_into(q, sh, c.q);
-        c.bs = gather4_into(b, sh, c.bs);
-        c.st = gather4_into(s, sh, c.st);
-        c.op = gather4_into(o, sh, c.op);
-        c.cl = gather4_into(cl, sh, c.cl);
-        c.cur = gather4_into(cu, sh, c.cur);
+        const uint32_t xl = x & 0x7F7F7F7Fu, yl = x & 0x5F5F5F5Fu, nx = ~x & H;
+        const uint32_t g22 = mad_u32(xl, one, 0x5E5E5E5Eu), g23 = mad_u32(xl, one, 0x5D5D5D5Du);
+        const uint32_t g2C = mad_u32(xl, one, 0x54545454u), g2D = mad_u32(xl, one, 0x53535353u);
+        const uint32_t g3A = mad_u32(xl, one, 0x46464646u), g3B = mad_u32(xl, one, 0x45454545u);
+        const uint32_t g5C = mad_u32(xl, one, 0x24242424u), g5D = mad_u32(xl, one, 0x23232323u);
+        const uint32_t h5B = mad_u32(yl, one, 0x25252525u), h5C = mad_u32(yl, one, 0x24242424u);
+        const uint32_t h5D = mad_u32(yl, one, 0x23232323u), h5E = mad_u32(yl, one, 0x22222222u);
+        const uint32_t q = (g22 ^ g23) & nx;                 // "
+        const uint32_t b = (g5C ^ g5D) & nx;                 // backslash
+        const uint32_t o = (h5B ^ h5C) & nx;                 // [ {
+        const uint32_t br = o | ((h5D ^ h5E) & nx);          // [ { ] }
+        uint32_t s = br | ((g2C ^ g2D) & nx) | ((g3A ^ g3B) & nx);   // , :
+        if (LINES) s |= (mad_u32(xl, one, 0x76767676u) ^ mad_u32(xl, one, 0x75757575u)) & nx;   // '\n'
+        const uint32_t cu = mad_u32(x, four, 0u) & br;       // bit 5 (curly) -> bit 7
+        c.q = gather_step(q, c.q);
+        c.bs = gather_step(b, c.bs);
+        c.st = gather_step(s, c.st);
+        c.op = gather_step(o, c.op);
+        c.br = gather_step(br, c.br);
+        c.cur = gather_step(cu, c.cur);
         c.hi |= x;
     }
     c.hi &= H;
@@ -210,11 +219,11 @@ CJ_HD Classes classify_words(const uint32_t* w) {
 }
 
 template <bool LINES>
-CJ_HD Classes classify16(const uint32_t w[4]) { return classify_words<LINES, 4>(w); }
+CJ_HD Classes classify16(const uint32_t w[4], uint32_t one) { return classify_words<LINES, 4>(w, one); }
 
 // Character classes of 32 bytes held as 8 little-endian words.
 template <bool LINES>
-CJ_HD Classes classify32(const uint32_t w[8]) { return classify_words<LINES, 8>(w); }
+CJ_HD Classes classify32(const uint32_t w[8], uint32_t one) { return classify_words<LINES, 8>(w, one); }
 
 // carry out of a 32-byte word entered without escape: whether its trailing
 // backslash run has odd length (not meaningful for an all-backslash word)

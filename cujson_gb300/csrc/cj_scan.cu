@@ -69,7 +69,6 @@ static_assert(kStepBytes % 16 == 0, "TMA copies need 16-byte multiples");
 struct __align__(16) Slot {
     uint32_t masks[kWarps][kStepsPerWarp][kMaskFields][32];
     Ent wtab[kWarps][4];       // per-warp transfer tables
-    Ent T[4];                  // the tile's table
     Ent wentry[kWarps];        // per-warp entry values (after the look-back)
     uint32_t we[kWarps];       // per-warp flip, then per-warp in-string inversion
     uint32_t tile;             // tile index, kNoTile when empty
@@ -169,17 +168,6 @@ __device__ __forceinline__ void mask_chunk(uint4& v, int valid) {
     }
 }
 
-// inclusive warp scan of three counters
-__device__ __forceinline__ void warp_scan3(uint32_t& a, uint32_t& b, uint32_t& c, int lane) {
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t ta = __shfl_up_sync(FULL, a, o);
-        uint32_t tb = __shfl_up_sync(FULL, b, o);
-        uint32_t tc = __shfl_up_sync(FULL, c, o);
-        if (lane >= o) { a += ta; b += tb; c += tc; }
-    }
-}
-
 struct TileGeom {
     const Segment* sp;
     uint32_t segi;
@@ -251,7 +239,7 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileGeom& g, 
         if (16 > valid) mask_chunk(lo, valid);
         if (32 > valid) mask_chunk(hi, valid - 16);
         const uint32_t w[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
-        const Classes c = classify32<LINES>(w);
+        const Classes c = classify32<LINES>(w, P.one);
 
         // UTF-8, byte-parallel, on steps that hold a non-ASCII byte
         {
@@ -261,7 +249,10 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileGeom& g, 
             const bool mine = valid > 0 && (c.hi || (pw & 0x80808000u));
             if (__any_sync(FULL, mine) && valid > 0) {
                 const bool seg_end = g.tile_off + (uint64_t)(reg_off + j * kStepBytes + my0 + kBytesPerThread) >= g.seg_len;
-                if (utf8_errors(w, pw, seg_end)) atomicOr(&P.ctrl->error_flags, CJ_FLAG_UTF8);
+                if (utf8_errors(w, pw, seg_end)) {
+                    if (P.seg_err) atomicOr(P.seg_err + g.segi, CJ_FLAG_UTF8);
+                    else atomicOr(&P.ctrl->error_flags, CJ_FLAG_UTF8);
+                }
             }
         }
 
@@ -287,7 +278,7 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileGeom& g, 
         const uint32_t lpar = par ^ (__popc(qb & lt) & 1u);
         par ^= __popc(qb) & 1u;
         const uint32_t M = prefix_xor(rq) ^ (lpar ? FULL : 0u);
-        const uint32_t br = c.op | c.cl;
+        const uint32_t br = c.br;
         n_c0 += __popc(c.st & ~M); n_ct += __popc(c.st);
         n_k0 += __popc(br & ~M);   n_kt += __popc(br);
         n_o0 += __popc(c.op & ~M); n_ot += __popc(c.op);
@@ -316,37 +307,61 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileGeom& g, 
     }
 }
 
-// Warp 0: given the exclusive prefix `excl` of the slot's tile, publish its
-// inclusive value and derive the warps' entry values.
-__device__ __forceinline__ void finish_prefix(const ScanParams& P, const TileGeom& g, Slot& sl,
-                                              Ent excl, uint32_t ep)
+__device__ __forceinline__ Ent shfl_ent(Ent e, int src) {
+    Ent r;
+    r.st = __shfl_sync(FULL, e.st, src);
+    r.s = __shfl_sync(FULL, e.s, src);
+    r.k = __shfl_sync(FULL, e.k, src);
+    r.d = __shfl_sync(FULL, e.d, src);
+    return r;
+}
+
+__device__ __forceinline__ Ent shfl_up_ent(Ent e, int o) {
+    Ent r;
+    r.st = __shfl_up_sync(FULL, e.st, o);
+    r.s = __shfl_up_sync(FULL, e.s, o);
+    r.k = __shfl_up_sync(FULL, e.k, o);
+    r.d = __shfl_up_sync(FULL, e.d, o);
+    return r;
+}
+
+// Coordinator, whole warp: given the slot's exclusive prefix `excl` and its
+// table T, publish the inclusive value (lane 0) and set every classifying
+// warp's entry value, lane w for warp w from its exclusive prefix table pre.
+__device__ __forceinline__ void finish_prefix(const ScanParams& P, const TileGeom& g, Slot& sl, Ent excl,
+                                              const Ent T[4], const Ent pre[4], uint32_t ep, int lane)
 {
-    const Ent incl = ent_apply(excl, sl.T);
-    __stcg(P.desc_incl + sl.tile, make_uint4(incl.st, incl.s, incl.k, (uint32_t)incl.d));
-    __threadfence();
-    st_release(P.desc_flag + sl.tile, (ep << 2) | kFlagIncl);
+    const Ent incl = ent_apply(excl, T);
+    if (lane == 0) {
+        // the release store orders the descriptor before the flag
+        __stcg(P.desc_incl + sl.tile, make_uint4(incl.st, incl.s, incl.k, (uint32_t)incl.d));
+        st_release(P.desc_flag + sl.tile, (ep << 2) | kFlagIncl);
+        if (g.seg_last) {
+            SegmentOut so;
+            so.s_end = incl.s;
+            so.k_end = incl.k;
+            so.depth_end = incl.d;
+            so.instr_end = incl.st & 1u;
+            P.seg_out[g.segi] = so;
+            if (incl.d != 0) {
+                if (P.seg_err) atomicOr(P.seg_err + g.segi, CJ_FLAG_BRACKETS);
+                else atomicOr(&P.ctrl->error_flags, CJ_FLAG_BRACKETS);
+            }
+        }
+        if (sl.tile + 1 == P.n_tiles) {
+            P.ctrl->s_total = incl.s;
+            P.ctrl->k_total = incl.k;
+        }
+        sl.resolved = 1;
+    }
     Ent v = excl;
     if (g.seg_first) { v.st = 0; v.d = 0; }
-    for (int w = 0; w < kWarps; w++) {
-        const uint32_t es = v.st & 3u;
-        sl.wentry[w] = v;
-        sl.we[w] = (es & 1u) ^ ((es >> 1) & sl.we[w]);   // e = instr ^ (esc & flip)
-        v = ent_apply(v, sl.wtab[w]);
+    if (lane < kWarps) {
+        const Ent e = ent_apply(v, pre);
+        const uint32_t es = e.st & 3u;
+        sl.wentry[lane] = e;
+        sl.we[lane] = (es & 1u) ^ ((es >> 1) & sl.we[lane]);   // e = instr ^ (esc & flip)
     }
-    if (g.seg_last) {
-        SegmentOut so;
-        so.s_end = incl.s;
-        so.k_end = incl.k;
-        so.depth_end = incl.d;
-        so.instr_end = incl.st & 1u;
-        P.seg_out[g.segi] = so;
-        if (incl.d != 0) atomicOr(&P.ctrl->error_flags, CJ_FLAG_BRACKETS);
-    }
-    if (sl.tile + 1 == P.n_tiles) {
-        P.ctrl->s_total = incl.s;
-        P.ctrl->k_total = incl.k;
-    }
-    sl.resolved = 1;
 }
 
 // Warp 0: decoupled look-back for the slot's tile; returns the exclusive
@@ -435,15 +450,24 @@ __device__ __forceinline__ void phase_c(const ScanParams& P, const TileGeom& g, 
         const uint32_t brm = m[1][lane] & ~Mf;
         const uint32_t opm = m[2][lane] & ~Mf;
         const uint32_t curm = m[3][lane];
-        const uint32_t own1 = (uint32_t)__popc(stm);
-        const uint32_t own2 = (uint32_t)__popc(brm);
-        const uint32_t own3 = (uint32_t)__popc(opm);
-        uint32_t i1 = own1, i2 = own2, i3 = own3;
-        warp_scan3(i1, i2, i3, lane);
-        const uint32_t n1 = __shfl_sync(FULL, i1, 31), n2 = __shfl_sync(FULL, i2, 31),
-                       n3 = __shfl_sync(FULL, i3, 31);
-        uint32_t r = s_base + i1 - own1, kr = k_base + i2 - own2;
-        int32_t depth = d_base + 2 * (int32_t)(i3 - own3) - (int32_t)(i2 - own2);
+        // the three counts (each <= 32 per lane) packed in 10-bit fields: one
+        // scan; exclusive prefixes stay <= 31 * 32 < 1024 per field
+        const uint32_t own = (uint32_t)__popc(stm) | ((uint32_t)__popc(brm) << 10) |
+                             ((uint32_t)__popc(opm) << 20);
+        uint32_t incl = own;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const uint32_t ex = incl - own;
+        const uint32_t ex31 = __shfl_sync(FULL, ex, 31), own31 = __shfl_sync(FULL, own, 31);
+        const uint32_t n1 = (ex31 & 0x3FFu) + (own31 & 0x3FFu);
+        const uint32_t n2 = ((ex31 >> 10) & 0x3FFu) + ((own31 >> 10) & 0x3FFu);
+        const uint32_t n3 = ((ex31 >> 20) & 0x3FFu) + ((own31 >> 20) & 0x3FFu);
+        const uint32_t e1 = ex & 0x3FFu, e2 = (ex >> 10) & 0x3FFu, e3 = (ex >> 20) & 0x3FFu;
+        uint32_t r = s_base + e1, kr = k_base + e2;
+        int32_t depth = d_base + 2 * (int32_t)e3 - (int32_t)e2;
         const uint64_t pos0 = pos_base + (uint64_t)j * kStepBytes;
         while (stm) {
             const int b = __ffs(stm) - 1;
@@ -493,35 +517,47 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
             const uint32_t tile = sl.tile;
             if (tile == kNoTile) break;
             const TileGeom g = tile_geom(P, tile);
-            Ent T[4];
-            tab_identity(T);
-#pragma unroll 1
-            for (int v = 0; v < kWarps; v++) tab_compose(T, sl.wtab[v], T);
+            // inclusive scan of the 16 warp tables over lanes 0..15, then the
+            // tile's table (lane 15) and each warp's exclusive prefix table
+            Ent t[4];
+            if (lane < kWarps) {
+#pragma unroll
+                for (int k = 0; k < 4; k++) t[k] = sl.wtab[lane][k];
+            } else {
+                tab_identity(t);
+            }
+#pragma unroll
+            for (int o = 1; o < kWarps; o <<= 1) {
+                Ent u[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) u[k] = shfl_up_ent(t[k], o);
+                if (lane >= o) tab_compose(u, t, t);
+            }
+            Ent T[4], pre[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                T[k] = shfl_ent(t[k], kWarps - 1);
+                pre[k] = shfl_up_ent(t[k], 1);
+            }
+            if (lane == 0) tab_identity(pre);
             if (g.seg_first) {
                 // a segment starts outside strings and escapes, at depth 0
                 const Ent t0 = T[0];
 #pragma unroll
                 for (int k = 0; k < 4; k++) { T[k] = t0; T[k].st |= 4u; }
             }
-            if (lane == 0) {
-#pragma unroll
-                for (int k = 0; k < 4; k++) sl.T[k] = T[k];
-            }
-            __syncwarp();
-            if (g.immediate) {
-                if (lane == 0) finish_prefix(P, g, sl, ent_identity(0), ep);
-            } else {
+            Ent excl = ent_identity(0);
+            if (!g.immediate) {
                 if (lane == 0) {
 #pragma unroll
                     for (int k = 0; k < 4; k++)
                         __stcg(P.desc_agg + (size_t)tile * 4 + k,
                                make_uint4(T[k].st, T[k].s, T[k].k, (uint32_t)T[k].d));
-                    __threadfence();
                     st_release(P.desc_flag + tile, (ep << 2) | kFlagAgg);
                 }
-                const Ent excl = look_back(P, tile, ep, lane);
-                if (lane == 0) finish_prefix(P, g, sl, excl, ep);
+                excl = shfl_ent(look_back(P, tile, ep, lane), 0);
             }
+            finish_prefix(P, g, sl, excl, T, pre, ep, lane);
             __syncwarp();
             bar_arrive(kBarP + s, kAll);
             s ^= 1;

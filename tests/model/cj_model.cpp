@@ -108,7 +108,7 @@ extern "C" int cjm_parse(const uint8_t* data, size_t n, int lines, const size_t*
                     }
                     w[k] = v;
                 }
-                c[t] = lines ? classify32<true>(w) : classify32<false>(w);
+                c[t] = lines ? classify32<true>(w, 1u) : classify32<false>(w, 1u);
                 {
                     // previous 4 bytes of the segment (zero before its start)
                     uint32_t pw = 0;
@@ -143,7 +143,7 @@ extern "C" int cjm_parse(const uint8_t* data, size_t n, int lines, const size_t*
                     carry = cout0[t];
                     tcout = cout0[t];
                 }
-                uint32_t br = c[t].op | c[t].cl;
+                uint32_t br = c[t].br;
                 own1[t] = __builtin_popcount(c[t].st & ~M[t]) | (__builtin_popcount(c[t].st) << 16);
                 own2[t] = __builtin_popcount(br & ~M[t]) | (__builtin_popcount(br) << 16);
                 own3[t] = __builtin_popcount(c[t].op & ~M[t]) | (__builtin_popcount(c[t].op) << 16);
@@ -197,7 +197,7 @@ extern "C" int cjm_parse(const uint8_t* data, size_t n, int lines, const size_t*
             uint32_t pre1lo = 0, pre1hi = 0, pre2lo = 0, pre2hi = 0, pre3lo = 0, pre3hi = 0;
             for (int t = 0; t < W; t++) {
                 uint32_t Mf = M[t] ^ (e ? 0xFFFFFFFFu : 0u);
-                uint32_t stm = c[t].st & ~Mf, brm = (c[t].op | c[t].cl) & ~Mf, opm = c[t].op & ~Mf;
+                uint32_t stm = c[t].st & ~Mf, brm = c[t].br & ~Mf, opm = c[t].op & ~Mf;
                 uint32_t p1lo = pre1lo, p1hi = pre1hi, p2lo = pre2lo, p2hi = pre2hi;
                 uint32_t p3lo = pre3lo, p3hi = pre3hi;
                 uint32_t sidx = entry.s + (e ? p1hi - p1lo : p1lo);
