@@ -78,7 +78,12 @@ struct __align__(16) Slot {
 struct __align__(128) Smem {
     WarpSmem w[kWarps];
     Slot slot[2];
-    uint32_t ticket;
+    // hand-offs per slot, all mbarriers (bounded waits; no warp waits on
+    // another classifying warp):
+    //   tile_ready   coordinator -> classifying warps: slot.tile is set
+    //   a_done       classifying warps (one arrival each) -> coordinator
+    //   prefix_ready coordinator -> classifying warps: entry values are set
+    unsigned long long tile_ready[2], a_done[2], prefix_ready[2];
 };
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
@@ -95,19 +100,6 @@ __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
 
 __device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
-// named barriers: 0 is __syncthreads; 1-2 "phase A done" per slot, 3-4
-// "prefix ready" per slot, 5 the classifying warps among themselves
-constexpr uint32_t kBarA = 1, kBarP = 3, kBarCompute = 5;
-constexpr uint32_t kAll = kThreads, kCompute = kWarps * 32;
-
-__device__ __forceinline__ void bar_sync(uint32_t id, uint32_t n) {
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
-}
-
-__device__ __forceinline__ void bar_arrive(uint32_t id, uint32_t n) {
-    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
 }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -147,6 +139,10 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t pari
         if (done) return true;
     }
     return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 __device__ __forceinline__ void load_table(const uint4* agg, uint32_t tile, Ent t[4]) {
@@ -506,16 +502,35 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
         for (int s = 0; s < kStages; s++) mbar_init(&S.w[warp].mbar[s], 1);
         fence_mbar_init();
     }
+    if (warp == kWarps && lane == 0) {
+        for (int s = 0; s < 2; s++) {
+            mbar_init(&S.tile_ready[s], 1);
+            mbar_init(&S.a_done[s], kWarps);
+            mbar_init(&S.prefix_ready[s], 1);
+        }
+        fence_mbar_init();
+    }
     __syncthreads();
 
     if (warp == kWarps) {
-        // ---- coordinator: publish, look back, derive entries -------------------------
+        // ---- coordinator: hand out tiles, publish, look back, derive entries ---------
+        if (lane == 0) {
+            for (int s = 0; s < 2; s++) {
+                const uint32_t t = atomicAdd(&P.ctrl->tile_ticket, 1u);
+                S.slot[s].tile = (t < P.n_tiles) ? t : kNoTile;
+                mbar_arrive(&S.tile_ready[s]);
+            }
+        }
+        __syncwarp();
+        uint32_t use = 0;          // bit s: phase parity of slot s's a_done
         int s = 0;
         while (true) {
-            bar_sync(kBarA + s, kAll);
             Slot& sl = S.slot[s];
             const uint32_t tile = sl.tile;
             if (tile == kNoTile) break;
+            if (!mbar_wait(&S.a_done[s], (use >> s) & 1u) && lane == 0)
+                atomicOr(&P.ctrl->error_flags, CJ_FLAG_TIMEOUT);
+            use ^= 1u << s;
             const TileGeom g = tile_geom(P, tile);
             // inclusive scan of the 16 warp tables over lanes 0..15, then the
             // tile's table (lane 15) and each warp's exclusive prefix table
@@ -559,7 +574,15 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
             }
             finish_prefix(P, g, sl, excl, T, pre, ep, lane);
             __syncwarp();
-            bar_arrive(kBarP + s, kAll);
+            if (lane == 0) {
+                mbar_arrive(&S.prefix_ready[s]);
+                // the slot's next tile: the classifying warps read it only
+                // after their phase C of this one
+                const uint32_t nt = atomicAdd(&P.ctrl->tile_ticket, 1u);
+                sl.tile = (nt < P.n_tiles) ? nt : kNoTile;
+                mbar_arrive(&S.tile_ready[s]);
+            }
+            __syncwarp();
             s ^= 1;
         }
         return;
@@ -568,25 +591,30 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
     // ---- classifying warps -----------------------------------------------------------
     WarpSmem& W = S.w[warp];
     const uint32_t lt = lanemask_lt();
-    uint32_t parity = 0;   // bit s: phase parity to wait for on stage s
+    // phase parities to wait for: bits 0..kStages-1 the ring stages, then two
+    // bits for the slots' tile_ready and two for their prefix_ready
+    constexpr int kTB = kStages, kPB = kStages + 2;
+    uint32_t parity = 0;
     int s = 0;
     uint32_t prev_tile = kNoTile;
     while (true) {
-        if (tid == 0) {
-            const uint32_t t = atomicAdd(&P.ctrl->tile_ticket, 1u);
-            S.slot[s].tile = (t < P.n_tiles) ? t : kNoTile;
-        }
-        bar_sync(kBarCompute, kCompute);
+        if (!mbar_wait(&S.tile_ready[s], (parity >> (kTB + s)) & 1u) && lane == 0)
+            atomicOr(&P.ctrl->error_flags, CJ_FLAG_TIMEOUT);
+        parity ^= 1u << (kTB + s);
         const uint32_t tile = S.slot[s].tile;
         if (tile != kNoTile) {
             const TileGeom g = tile_geom(P, tile);
             phase_a<LINES>(P, g, W, S.slot[s], parity, warp, lane, lt);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&S.a_done[s]);
         }
-        bar_arrive(kBarA + s, kAll);
         if (prev_tile != kNoTile) {
-            bar_sync(kBarP + (s ^ 1), kAll);
+            const int q = s ^ 1;
+            if (!mbar_wait(&S.prefix_ready[q], (parity >> (kPB + q)) & 1u) && lane == 0)
+                atomicOr(&P.ctrl->error_flags, CJ_FLAG_TIMEOUT);
+            parity ^= 1u << (kPB + q);
             const TileGeom g = tile_geom(P, prev_tile);
-            phase_c(P, g, S.slot[s ^ 1], warp, lane);
+            phase_c(P, g, S.slot[q], warp, lane);
         }
         if (tile == kNoTile) break;
         prev_tile = tile;
