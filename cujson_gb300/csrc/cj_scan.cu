@@ -194,9 +194,36 @@ __device__ __forceinline__ TileGeom tile_geom(const ScanParams& P, uint32_t tile
 }
 
 // Phase A of one warp's region: classify, validate, resolve strings, keep masks.
+// The ring runs on across tiles: step j of a tile uses stage (rstage + j) mod
+// kStages.  When the last steps of a tile free their stages and the warp's
+// next tile is already known (its slot's tile_ready phase has completed), the
+// first steps of the next tile are loaded into them ahead of time; `pf` counts
+// those steps for the next call.
+struct Ring {
+    uint32_t rstage = 0;   // stage of step 0 of the current tile
+    int pf = 0;            // steps of the current tile already in flight
+};
+
+__device__ __forceinline__ bool mbar_test(unsigned long long* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+    return done != 0;
+}
+
+__device__ __forceinline__ int region_steps(const TileGeom& g, int warp) {
+    const int reg_len = max(0, min(kWarpBytes, g.tile_len - warp * kWarpBytes));
+    return (reg_len + kStepBytes - 1) / kStepBytes;
+}
+
 template <bool LINES>
 __device__ __forceinline__ void phase_a(const ScanParams& P, const TileGeom& g, WarpSmem& W, Slot& sl,
-                                        uint32_t& parity, int warp, int lane, uint32_t lt)
+                                        uint32_t& parity, int warp, int lane, uint32_t lt, Ring& ring,
+                                        const Slot& next_slot, unsigned long long* next_ready,
+                                        uint32_t next_parity)
 {
     const int reg_off = warp * kWarpBytes;
     const int reg_len = max(0, min(kWarpBytes, g.tile_len - reg_off));
@@ -204,16 +231,25 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileGeom& g, 
     const uint8_t* reg_src = g.seg_base + g.tile_off + reg_off;
     if (lane == 0) {
         fence_proxy_async();
-        for (int j = 0; j < kStages && j < nsteps; j++)
-            tma_load(W.ring[j], reg_src + (size_t)j * kStepBytes, &W.mbar[j]);
+        uint32_t st = ring.rstage + (uint32_t)ring.pf;
+        st = st >= (uint32_t)kStages ? st - kStages : st;
+        for (int j = ring.pf; j < kStages && j < nsteps; j++) {
+            tma_load(W.ring[st], reg_src + (size_t)j * kStepBytes, &W.mbar[st]);
+            st = (st + 1 == (uint32_t)kStages) ? 0u : st + 1;
+        }
     }
+    // next tile's region, known once lane 0 has seen its slot's tile_ready
+    const uint8_t* nsrc = nullptr;
+    int nsteps_next = -1;        // -1: not looked up yet
+    int pf_next = 0;
+    uint32_t st_i = ring.rstage;
     uint32_t carry = 0, par = 0;           // escape carry / quote parity (warp uniform)
     uint32_t started = 0, wflip = 0;       // first non-all-backslash lane seen / its flip
     uint32_t prev_last = (g.tile_off + (uint64_t)reg_off > 0 && nsteps > 0)
                              ? __ldg(reinterpret_cast<const uint32_t*>(reg_src) - 1) : 0u;
     uint32_t n_c0 = 0, n_ct = 0, n_k0 = 0, n_kt = 0, n_o0 = 0, n_ot = 0;   // per lane
     for (int j = 0; j < nsteps; j++) {
-        const int st_i = j % kStages;
+        if (j > 0) st_i = (st_i + 1 == (uint32_t)kStages) ? 0u : st_i + 1;
         if (!mbar_wait(&W.mbar[st_i], (parity >> st_i) & 1u)) {
             if (lane == 0) atomicOr(&P.ctrl->error_flags, CJ_FLAG_TIMEOUT);
         }
@@ -227,9 +263,28 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileGeom& g, 
         uint4 va = *reinterpret_cast<const uint4*>(&W.ring[st_i][my0 + 16 * r0]);
         uint4 vb = *reinterpret_cast<const uint4*>(&W.ring[st_i][my0 + 16 * (r0 ^ 1)]);
         __syncwarp();
-        if (lane == 0 && j + kStages < nsteps) {
-            fence_proxy_async();
-            tma_load(W.ring[st_i], reg_src + (size_t)(j + kStages) * kStepBytes, &W.mbar[st_i]);
+        if (lane == 0) {
+            if (j + kStages < nsteps) {
+                fence_proxy_async();
+                tma_load(W.ring[st_i], reg_src + (size_t)(j + kStages) * kStepBytes, &W.mbar[st_i]);
+            } else {
+                // this stage is free for good: the next tile's step m, if known
+                const int m = j + kStages - nsteps;
+                if (nsteps_next < 0 && mbar_test(next_ready, next_parity)) {
+                    const uint32_t nt = next_slot.tile;
+                    nsteps_next = 0;
+                    if (nt != kNoTile) {
+                        const TileGeom ng = tile_geom(P, nt);
+                        nsteps_next = region_steps(ng, warp);
+                        nsrc = ng.seg_base + ng.tile_off + reg_off;
+                    }
+                }
+                if (m == pf_next && m < nsteps_next) {
+                    fence_proxy_async();
+                    tma_load(W.ring[st_i], nsrc + (size_t)m * kStepBytes, &W.mbar[st_i]);
+                    pf_next = m + 1;
+                }
+            }
         }
         uint4 lo = r0 ? vb : va, hi = r0 ? va : vb;
         if (16 > valid) mask_chunk(lo, valid);
@@ -284,6 +339,11 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileGeom& g, 
         m[2][lane] = c.op;
         m[3][lane] = c.cur;
         m[4][lane] = M;
+    }
+    {
+        uint32_t st = ring.rstage + (uint32_t)(nsteps % kStages);
+        ring.rstage = st >= (uint32_t)kStages ? st - kStages : st;
+        ring.pf = __shfl_sync(FULL, pf_next, 0);
     }
     // the warp's transfer table, relative to the state it is entered in
     const int32_t C0 = (int32_t)__reduce_add_sync(FULL, n_c0), Ct = (int32_t)__reduce_add_sync(FULL, n_ct);
@@ -595,6 +655,7 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
     // bits for the slots' tile_ready and two for their prefix_ready
     constexpr int kTB = kStages, kPB = kStages + 2;
     uint32_t parity = 0;
+    Ring ring;
     int s = 0;
     uint32_t prev_tile = kNoTile;
     while (true) {
@@ -604,7 +665,8 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
         const uint32_t tile = S.slot[s].tile;
         if (tile != kNoTile) {
             const TileGeom g = tile_geom(P, tile);
-            phase_a<LINES>(P, g, W, S.slot[s], parity, warp, lane, lt);
+            phase_a<LINES>(P, g, W, S.slot[s], parity, warp, lane, lt, ring, S.slot[s ^ 1],
+                           &S.tile_ready[s ^ 1], (parity >> (kTB + (s ^ 1))) & 1u);
             __syncwarp();
             if (lane == 0) mbar_arrive(&S.a_done[s]);
         }
