@@ -153,6 +153,27 @@ def allmax(pg, x: float) -> float:
     return float(t.item())
 
 
+def pinned_h2d_gbs(host: np.ndarray, device: int):
+    """Best of 5 plain copies of the pinned input to the device (the link's
+    bandwidth for this buffer), or None without torch."""
+    try:
+        import torch
+        src = torch.from_numpy(host)
+        dst = torch.empty(host.size, dtype=torch.uint8, device=f"cuda:{device}")
+        best = None
+        for _ in range(6):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            dst.copy_(src, non_blocking=True)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        del dst
+        return host.size / best / 1e9
+    except Exception:
+        return None
+
+
 def cpu_baseline_sample(sample_bytes: int):
     """Oracle (CPU restatement of the reference algorithm), one thread, on a
     bounded sample of the same generator; returns (GB/s, description)."""
@@ -441,6 +462,10 @@ def run_ours(args, world, rank, local, pg):
         e2e = {"value": round(N * world * args.steps / dt / 1e9, 3), "unit": UNIT,
                "h2d_bytes_per_step": N, "d2h_bytes_per_step": out_n * 4 + 64,
                "ms_per_step": round(dt / args.steps * 1e3, 3)}
+        link = pinned_h2d_gbs(pin_in.array, local)
+        if link:
+            e2e["pinned_h2d_GBps"] = round(link, 1)
+            e2e["frac_of_pinned_h2d"] = round(e2e["value"] / world / link, 3)
         pin_in.close()
         pin_out.close()
 

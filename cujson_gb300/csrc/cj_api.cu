@@ -10,6 +10,7 @@
 //   - JSON-Lines chunks are parsed in the same launch (each chunk is a segment
 //     whose string/escape state and depth restart), not one after another;
 //   - errors are returned as a status; the process never exits.
+#include <cuda.h>            // driver API types of the stream memory write entry point
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -101,6 +102,16 @@ struct cj_context {
     cudaGraphExec_t graph_exec = nullptr;
     bool graph_valid = false;
     uint64_t arena_gen = 0;             // bumped whenever a device buffer is (re)allocated
+
+    // one-shot parses of large inputs: copies on copy_stream overlap the scan,
+    // which hands out a tile only once d_ready covers its bytes
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_reset = nullptr, ev_copied = nullptr;
+    unsigned long long* d_ready = nullptr;
+    bool overlap_run = false;
+    // cuStreamWriteValue64 when the driver offers it (no kernel needs to run
+    // beside the scan to raise d_ready); else a one-thread kernel does it
+    CUresult (*write64)(CUstream, CUdeviceptr, cuuint64_t, unsigned int) = nullptr;
 
     // launch shapes (0 = default), set by cj_context_set_tuning / cj_autotune_staged
     uint32_t tune_scan_ctas = 0;
@@ -305,6 +316,7 @@ cj_status enqueue(cj_context* ctx, bool graph)
     sp.seg_out = ctx->seg_out.p;
     sp.epoch = ctx->epoch;
     sp.seg_err = ctx->batch ? ctx->seg_err.p : nullptr;
+    sp.ready = ctx->overlap_run ? ctx->d_ready : nullptr;
     uint32_t scan_grid = ctx->scan_grid;
     if (ctx->tune_scan_ctas) scan_grid = std::min(scan_grid, ctx->tune_scan_ctas);
     launch_scan(sp, ctx->lines, (int)std::min<uint32_t>(ctx->n_tiles, scan_grid), ctx->stream);
@@ -388,6 +400,129 @@ cj_status run_graph(cj_context* ctx)
     ctx->launches += (ctx->n_tiles ? 1 : 0) + 2 + (ctx->batch ? 2 : 0);
     ctx->batch_read = false;
     return CJ_OK;
+}
+
+// Raises the count of input bytes present; runs after each chunk's copy on
+// the copy stream.
+__global__ void mark_ready(unsigned long long* ready, unsigned long long bytes)
+{
+    if (threadIdx.x == 0) {
+        __threadfence_system();
+        asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(ready), "l"(bytes) : "memory");
+    }
+}
+
+constexpr size_t kOverlapMin = 64ull << 20;     // smaller inputs: one copy, then the run
+constexpr size_t kOverlapChunk = 32ull << 20;   // copy granularity of an overlapped run
+
+// Stage and run in one go, the input's copy overlapping the scan: the small
+// tables go first, then the scan is launched and the input follows in chunks
+// on the copy stream, each chunk raising d_ready.
+cj_status stage_overlapped(cj_context* ctx, const uint8_t* const* chunks, const size_t* sizes, size_t n,
+                           bool lines)
+{
+    ctx->staged = false;
+    ctx->graph_valid = false;
+    if (!chunks || !sizes || n == 0) return CJ_ERR_INVALID_ARGUMENT;
+    size_t total = 0;
+    for (size_t i = 0; i < n; i++) {
+        if (!chunks[i] || sizes[i] == 0) return CJ_ERR_INVALID_ARGUMENT;
+        total += sizes[i];
+    }
+    if (total > CJ_MAX_INPUT_BYTES) return CJ_ERR_TOO_LARGE;
+    CJ_CUDA(cudaSetDevice(ctx->device));
+    cj_status st = reserve(ctx, total, n);
+    if (st) return st;
+    ctx->h_segs.resize(n);
+    uint64_t dev_off = 0, logical = 0;
+    uint32_t tile = 0;
+    for (size_t i = 0; i < n; i++) {
+        Segment& g = ctx->h_segs[i];
+        g.dev_off = dev_off;
+        g.len = sizes[i];
+        g.logical_off = logical;
+        g.out_base = 0;
+        g.brk_base = 0;
+        g.first_tile = tile;
+        g.n_tiles = (uint32_t)((sizes[i] + kTileBytes - 1) / kTileBytes);
+        g.flags = (i > 0) ? kSegContinue : 0u;
+        g.pad = 0;
+        dev_off += round_up(sizes[i], kPadBytes);
+        logical += sizes[i];
+        tile += g.n_tiles;
+    }
+    CJ_CUDA(cudaMemcpyAsync(ctx->segs.p, ctx->h_segs.data(), n * sizeof(Segment), cudaMemcpyHostToDevice,
+                            ctx->stream));
+    if (n > 1) {
+        ctx->h_tile_seg.resize(tile);
+        for (size_t i = 0; i < n; i++)
+            for (uint32_t t = 0; t < ctx->h_segs[i].n_tiles; t++)
+                ctx->h_tile_seg[ctx->h_segs[i].first_tile + t] = (uint32_t)i;
+        CJ_CUDA(cudaMemcpyAsync(ctx->tile_seg.p, ctx->h_tile_seg.data(), tile * sizeof(uint32_t),
+                                cudaMemcpyHostToDevice, ctx->stream));
+    }
+    CJ_CUDA(cudaMemsetAsync(ctx->d_ready, 0, sizeof(unsigned long long), ctx->stream));
+    CJ_CUDA(cudaEventRecord(ctx->ev_reset, ctx->stream));
+    ctx->n_bytes = total;
+    ctx->n_segs = (uint32_t)n;
+    ctx->n_tiles = tile;
+    ctx->lines = lines;
+    ctx->batch = false;
+    ctx->staged = true;
+    ctx->overlap_run = true;
+    st = enqueue(ctx, false);
+    ctx->overlap_run = false;
+    if (st) return st;
+    CJ_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_reset, 0));
+    for (size_t i = 0; i < n; i++) {
+        const Segment& g = ctx->h_segs[i];
+        for (uint64_t o = 0; o < g.len; o += kOverlapChunk) {
+            const uint64_t c = std::min<uint64_t>(kOverlapChunk, g.len - o);
+            CJ_CUDA(cudaMemcpyAsync(ctx->in.p + g.dev_off + o, chunks[i] + o, c, cudaMemcpyHostToDevice,
+                                    ctx->copy_stream));
+            const uint64_t upto = (o + c == g.len) ? round_up(g.len, kPadBytes) : o + c;
+            if (ctx->write64) {
+                // default flags: the write follows a barrier that orders the copy before it
+                if (ctx->write64((CUstream)ctx->copy_stream, (CUdeviceptr)ctx->d_ready, g.dev_off + upto,
+                                 CU_STREAM_WRITE_VALUE_DEFAULT) != CUDA_SUCCESS)
+                    return CJ_ERR_CUDA;
+            } else {
+                mark_ready<<<1, 32, 0, ctx->copy_stream>>>(ctx->d_ready, g.dev_off + upto);
+                ctx->launches += 1;
+            }
+        }
+    }
+    CJ_CUDA(cudaGetLastError());
+    CJ_CUDA(cudaEventRecord(ctx->ev_copied, ctx->copy_stream));
+    CJ_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_copied, 0));
+    return CJ_OK;
+}
+
+bool is_pinned(const void* p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+// One-shot staging and run: overlapped for large pinned inputs (a copy from
+// pageable memory goes through the driver's staging and may synchronise with
+// other work), else copy then run.
+cj_status stage_run(cj_context* ctx, const uint8_t* const* chunks, const size_t* sizes, size_t n, bool lines)
+{
+    size_t total = 0;
+    bool pinned = chunks != nullptr;
+    for (size_t i = 0; sizes && i < n; i++) {
+        total += sizes[i];
+        if (pinned && (!chunks[i] || !is_pinned(chunks[i]))) pinned = false;
+    }
+    if (total >= kOverlapMin && pinned) return stage_overlapped(ctx, chunks, sizes, n, lines);
+    cj_status st = stage(ctx, chunks, sizes, n, lines);
+    if (!st) st = run(ctx);
+    return st;
 }
 
 cj_status read_info(cj_context* ctx, cj_parse_info* info)
@@ -664,9 +799,26 @@ cj_status cj_context_create(int device, cj_context** out)
     }
     ctx->scan_grid = (uint32_t)(per_sm * ctx->sm_count);
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_reset, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_copied, cudaEventDisableTiming) != cudaSuccess ||
+        cudaMalloc((void**)&ctx->d_ready, sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc((void**)&ctx->d_ctrl, sizeof(Ctrl)) != cudaSuccess) {
         cj_context_destroy(ctx);
         return CJ_ERR_CUDA;
+    }
+    {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuStreamWriteValue64", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess && fn) {
+            auto w = reinterpret_cast<CUresult (*)(CUstream, CUdeviceptr, cuuint64_t, unsigned int)>(fn);
+            if (w((CUstream)ctx->copy_stream, (CUdeviceptr)ctx->d_ready, 0, CU_STREAM_WRITE_VALUE_DEFAULT) ==
+                    CUDA_SUCCESS &&
+                cudaStreamSynchronize(ctx->copy_stream) == cudaSuccess)
+                ctx->write64 = w;
+        }
+        cudaGetLastError();
     }
     *out = ctx;
     return CJ_OK;
@@ -684,6 +836,11 @@ void cj_context_destroy(cj_context* ctx)
     release(ctx->seg_err); release(ctx->seg_depth); release(ctx->rchunk_off);
     release(ctx->layout_off); release(ctx->layout); release(ctx->pack); release(ctx->pack_off);
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    if (ctx->d_ready) cudaFree(ctx->d_ready);
+    if (ctx->ev_reset) cudaEventDestroy(ctx->ev_reset);
+    if (ctx->ev_copied) cudaEventDestroy(ctx->ev_copied);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->d_ctrl) cudaFree(ctx->d_ctrl);
     if (ctx->h_ctrl) cudaFreeHost(ctx->h_ctrl);
     if (ctx->h_seg_out) cudaFreeHost(ctx->h_seg_out);
@@ -770,8 +927,7 @@ cj_status cj_parse_standard(cj_context* ctx, const uint8_t* data, size_t size, c
     if (!ctx || !out || !data || size == 0) return finish(CJ_ERR_INVALID_ARGUMENT);
     const uint8_t* chunks[1] = {data};
     size_t sizes[1] = {size};
-    cj_status st = stage(ctx, chunks, sizes, 1, false);
-    if (!st) st = run(ctx);
+    cj_status st = stage_run(ctx, chunks, sizes, 1, false);
     cj_parse_info info;
     if (!st) st = read_info(ctx, &info);
     if (!st && info.status != CJ_OK) st = (cj_status)info.status;
@@ -785,8 +941,7 @@ cj_status cj_parse_lines(cj_context* ctx, const uint8_t* const* chunks, const si
 {
     if (out) memset(out, 0, sizeof(*out));
     if (!ctx || !out) return finish(CJ_ERR_INVALID_ARGUMENT);
-    cj_status st = stage(ctx, chunks, chunk_sizes, n_chunks, true);
-    if (!st) st = run(ctx);
+    cj_status st = stage_run(ctx, chunks, chunk_sizes, n_chunks, true);
     cj_parse_info info;
     if (!st) st = read_info(ctx, &info);
     if (!st && info.status != CJ_OK) st = (cj_status)info.status;
@@ -809,8 +964,7 @@ cj_status cj_parse_into(cj_context* ctx, const uint8_t* data, size_t size, int l
     if (!ctx || !data || size == 0 || !host_out) return finish(CJ_ERR_INVALID_ARGUMENT);
     const uint8_t* chunks[1] = {data};
     size_t sizes[1] = {size};
-    cj_status st = stage(ctx, chunks, sizes, 1, lines_mode != 0);
-    if (!st) st = run(ctx);
+    cj_status st = stage_run(ctx, chunks, sizes, 1, lines_mode != 0);
     cj_parse_info local;
     if (!info) info = &local;
     if (!st) st = read_info(ctx, info);

@@ -52,7 +52,9 @@ namespace {
 constexpr int kStages = 3;                // TMA ring depth per warp
 constexpr int kMaskFields = 5;            // st, br, op, cur, M per lane per step
 constexpr uint32_t kSpinLimit = 1u << 22; // look-back polls before giving up
+constexpr int kLookPerLane = 4;           // predecessors per lane and look-back round
 constexpr uint32_t kWaitLimit = 1u << 20; // mbarrier polls before giving up
+constexpr uint32_t kInputWaitLimit = 1u << 22;   // polls (>= 256 ns each) for input bytes
 constexpr uint32_t FULL = 0xFFFFFFFFu;
 constexpr uint32_t kNoTile = 0xFFFFFFFFu;
 
@@ -95,6 +97,12 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
     uint32_t v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
 
@@ -293,7 +301,7 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileGeom& g, 
         const Classes c = classify32<LINES>(w, P.one);
 
         // UTF-8, byte-parallel, on steps that hold a non-ASCII byte
-        {
+        if (__any_sync(FULL, c.hi != 0u) || (prev_last & 0x80808000u)) {
             uint32_t pw = __shfl_up_sync(FULL, w[7], 1);
             if (lane == 0) pw = prev_last;
             prev_last = __shfl_sync(FULL, w[7], 31);
@@ -305,22 +313,36 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileGeom& g, 
                     else atomicOr(&P.ctrl->error_flags, CJ_FLAG_UTF8);
                 }
             }
+        } else {
+            // an all-ASCII step after a word without lead bytes: nothing to check
+            prev_last = __shfl_sync(FULL, w[7], 31);
         }
 
         // escapes: carry from the nearest earlier lane that is not all backslashes
-        const uint32_t cout0 = escape_cout(c.bs);
-        const bool all_bs = (c.bs == FULL);
-        const uint32_t nonall = __ballot_sync(FULL, !all_bs);
-        const uint32_t prior = nonall & lt;
-        const uint32_t cin_lane = __shfl_sync(FULL, cout0, prior ? 31 - __clz(prior) : 0);
-        const uint32_t lane_carry = prior ? cin_lane : carry;
-        const uint32_t flipc = all_bs ? 0u : ((c.q >> (__ffs(~c.bs) - 1)) & 1u);
-        const uint32_t first_flip = __shfl_sync(FULL, flipc, nonall ? __ffs(nonall) - 1 : 0);
-        const uint32_t last_cout = __shfl_sync(FULL, cout0, nonall ? 31 - __clz(nonall) : 0);
-        if (nonall) {
-            if (!started) wflip = first_flip;
-            started = 1;
-            carry = last_cout;
+        uint32_t lane_carry;
+        if (!__any_sync(FULL, (int32_t)c.bs < 0)) {
+            // no lane ends in a backslash: only lane 0 can receive a carry
+            lane_carry = (lane == 0) ? carry : 0u;
+            if (!started) {
+                wflip = __shfl_sync(FULL, (c.q >> (__ffs(~c.bs) - 1)) & 1u, 0);
+                started = 1;
+            }
+            carry = 0;
+        } else {
+            const uint32_t cout0 = escape_cout(c.bs);
+            const bool all_bs = (c.bs == FULL);
+            const uint32_t nonall = __ballot_sync(FULL, !all_bs);
+            const uint32_t prior = nonall & lt;
+            const uint32_t cin_lane = __shfl_sync(FULL, cout0, prior ? 31 - __clz(prior) : 0);
+            lane_carry = prior ? cin_lane : carry;
+            const uint32_t flipc = all_bs ? 0u : ((c.q >> (__ffs(~c.bs) - 1)) & 1u);
+            const uint32_t first_flip = __shfl_sync(FULL, flipc, nonall ? __ffs(nonall) - 1 : 0);
+            const uint32_t last_cout = __shfl_sync(FULL, cout0, nonall ? 31 - __clz(nonall) : 0);
+            if (nonall) {
+                if (!started) wflip = first_flip;
+                started = 1;
+                carry = last_cout;
+            }
         }
         uint32_t dummy;
         const uint32_t esc = escaped32(c.bs, lane_carry, &dummy);
@@ -424,23 +446,41 @@ __device__ __forceinline__ void finish_prefix(const ScanParams& P, const TileGeo
 // prefix (valid in lane 0).
 __device__ __forceinline__ Ent look_back(const ScanParams& P, uint32_t tile, uint32_t ep, int lane)
 {
-    Ent excl = ent_identity(0);
+    // Each round inspects kLookBack = 32 * kLookPerLane predecessors; lane l
+    // covers indices l*kLookPerLane .. +kLookPerLane-1 (index i is tile
+    // pred_hi - i).  Flags first, then -- once no predecessor before the
+    // nearest inclusive one is still unpublished -- the aggregate tables below
+    // it and that inclusive value, all loaded in parallel.
+    constexpr int R = kLookPerLane;
     Ent acc[4];
     tab_identity(acc);
     int64_t pred_hi = (int64_t)tile - 1;
     uint32_t spins = 0;
     while (true) {
-        const int64_t p = pred_hi - lane;
-        uint32_t status = kFlagIncl;
-        if (p >= 0) {
-            uint32_t f = ld_acquire(P.desc_flag + p);
-            status = ((f >> 2) == ep) ? (f & 3u) : 0u;
+        uint32_t st_bits = 0;           // 2 bits per index: status
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int64_t p = pred_hi - (lane * R + r);
+            uint32_t status = kFlagIncl;
+            if (p >= 0) {
+                const uint32_t f = ld_acquire(P.desc_flag + p);
+                status = ((f >> 2) == ep) ? (f & 3u) : 0u;
+            }
+            st_bits |= status << (2 * r);
         }
-        const uint32_t incl = __ballot_sync(FULL, status == kFlagIncl);
-        const uint32_t notr = __ballot_sync(FULL, status == 0u);
-        const int n = incl ? __ffs(incl) - 1 : 32;
-        const uint32_t below = (n == 32) ? FULL : ((1u << n) - 1u);
-        if (notr & below) {
+        int r_incl = R, r_notr = R;
+#pragma unroll
+        for (int r = R - 1; r >= 0; r--) {
+            const uint32_t stt = (st_bits >> (2 * r)) & 3u;
+            if (stt == kFlagIncl) r_incl = r;
+            if (stt == 0u) r_notr = r;
+        }
+        const uint32_t incl = __ballot_sync(FULL, r_incl < R);
+        const int nl = incl ? __ffs(incl) - 1 : 32;                  // lane holding the nearest inclusive
+        const int n_incl = __shfl_sync(FULL, r_incl, nl & 31);
+        const int lim = (nl == 32) ? R * 32 : nl * R + n_incl;       // indices below use aggregates
+        const bool blocked = (lane * R + r_notr) < lim && r_notr < R;
+        if (__any_sync(FULL, blocked)) {
             if (++spins > kSpinLimit) {
                 if (lane == 0) atomicOr(&P.ctrl->error_flags, CJ_FLAG_TIMEOUT);
                 return ent_identity(0);
@@ -448,9 +488,23 @@ __device__ __forceinline__ Ent look_back(const ScanParams& P, uint32_t tile, uin
             __nanosleep(32);
             continue;
         }
+        // this lane's tables, farthest first, and the inclusive value
+        uint4 iv = make_uint4(0, 0, 0, 0);
+        if (lane == nl) {
+            const int64_t pi = pred_hi - (lane * R + n_incl);
+            if (pi >= 0) iv = __ldcg(P.desc_incl + pi);     // before tile 0: the zero value
+        }
         Ent t[4];
-        if (lane < n) load_table(P.desc_agg, (uint32_t)p, t);
-        else tab_identity(t);
+        tab_identity(t);
+#pragma unroll
+        for (int r = R - 1; r >= 0; r--) {
+            const int i = lane * R + r;
+            if (i < lim) {
+                Ent u[4];
+                load_table(P.desc_agg, (uint32_t)(pred_hi - i), u);
+                tab_compose(t, u, t);
+            }
+        }
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             Ent u[4];
@@ -464,19 +518,16 @@ __device__ __forceinline__ Ent look_back(const ScanParams& P, uint32_t tile, uin
             if (lane + o < 32) tab_compose(u, t, t);
         }
         if (incl) {
-            uint4 iv = make_uint4(0, 0, 0, 0);
-            if (lane == n) iv = __ldcg(P.desc_incl + p);
-            iv.x = __shfl_sync(FULL, iv.x, n);
-            iv.y = __shfl_sync(FULL, iv.y, n);
-            iv.z = __shfl_sync(FULL, iv.z, n);
-            iv.w = __shfl_sync(FULL, iv.w, n);
+            iv.x = __shfl_sync(FULL, iv.x, nl);
+            iv.y = __shfl_sync(FULL, iv.y, nl);
+            iv.z = __shfl_sync(FULL, iv.z, nl);
+            iv.w = __shfl_sync(FULL, iv.w, nl);
             Ent v;
             v.st = iv.x; v.s = iv.y; v.k = iv.z; v.d = (int32_t)iv.w;
-            excl = ent_apply(ent_apply(v, t), acc);
-            return excl;
+            return ent_apply(ent_apply(v, t), acc);
         }
         tab_compose(t, acc, acc);
-        pred_hi -= 32;
+        pred_hi -= 32 * R;
     }
 }
 
@@ -550,6 +601,29 @@ __device__ __forceinline__ void phase_c(const ScanParams& P, const TileGeom& g, 
 
 size_t scan_smem_bytes() { return sizeof(Smem); }
 
+// Coordinator lane 0: the next tile from the ticket counter, once its input
+// bytes are in device memory (bounded wait; the timeout flag on expiry).
+__device__ __forceinline__ uint32_t next_tile(const ScanParams& P)
+{
+    const uint32_t t = atomicAdd(&P.ctrl->tile_ticket, 1u);
+    if (t >= P.n_tiles) return kNoTile;
+    if (P.ready) {
+        const TileGeom g = tile_geom(P, t);
+        const uint64_t padded = (g.seg_len + kPadBytes - 1) / kPadBytes * kPadBytes;
+        const uint64_t end = g.tile_off + (uint64_t)kTileBytes;
+        const uint64_t need = (uint64_t)(g.seg_base - P.in) + (end < padded ? end : padded);
+        uint32_t spins = 0;
+        while (ld_acquire64(P.ready) < need) {
+            if (++spins > kInputWaitLimit) {
+                atomicOr(&P.ctrl->error_flags, CJ_FLAG_TIMEOUT);
+                break;
+            }
+            __nanosleep(256);
+        }
+    }
+    return t;
+}
+
 template <bool LINES>
 __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
 {
@@ -567,6 +641,7 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
             mbar_init(&S.tile_ready[s], 1);
             mbar_init(&S.a_done[s], kWarps);
             mbar_init(&S.prefix_ready[s], 1);
+            S.slot[s].tile = kNoTile;
         }
         fence_mbar_init();
     }
@@ -576,8 +651,7 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
         // ---- coordinator: hand out tiles, publish, look back, derive entries ---------
         if (lane == 0) {
             for (int s = 0; s < 2; s++) {
-                const uint32_t t = atomicAdd(&P.ctrl->tile_ticket, 1u);
-                S.slot[s].tile = (t < P.n_tiles) ? t : kNoTile;
+                S.slot[s].tile = next_tile(P);
                 mbar_arrive(&S.tile_ready[s]);
             }
         }
@@ -638,8 +712,7 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
                 mbar_arrive(&S.prefix_ready[s]);
                 // the slot's next tile: the classifying warps read it only
                 // after their phase C of this one
-                const uint32_t nt = atomicAdd(&P.ctrl->tile_ticket, 1u);
-                sl.tile = (nt < P.n_tiles) ? nt : kNoTile;
+                sl.tile = next_tile(P);
                 mbar_arrive(&S.tile_ready[s]);
             }
             __syncwarp();
@@ -659,10 +732,12 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
     int s = 0;
     uint32_t prev_tile = kNoTile;
     while (true) {
-        if (!mbar_wait(&S.tile_ready[s], (parity >> (kTB + s)) & 1u) && lane == 0)
-            atomicOr(&P.ctrl->error_flags, CJ_FLAG_TIMEOUT);
+        // a wait that expired (lane 0 decides for the warp) ends the warp's
+        // work: the slot's contents are then not trusted
+        const bool got_tile = __shfl_sync(FULL, mbar_wait(&S.tile_ready[s], (parity >> (kTB + s)) & 1u), 0);
+        if (!got_tile && lane == 0) atomicOr(&P.ctrl->error_flags, CJ_FLAG_TIMEOUT);
         parity ^= 1u << (kTB + s);
-        const uint32_t tile = S.slot[s].tile;
+        const uint32_t tile = got_tile ? S.slot[s].tile : kNoTile;
         if (tile != kNoTile) {
             const TileGeom g = tile_geom(P, tile);
             phase_a<LINES>(P, g, W, S.slot[s], parity, warp, lane, lt, ring, S.slot[s ^ 1],
@@ -672,11 +747,15 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
         }
         if (prev_tile != kNoTile) {
             const int q = s ^ 1;
-            if (!mbar_wait(&S.prefix_ready[q], (parity >> (kPB + q)) & 1u) && lane == 0)
-                atomicOr(&P.ctrl->error_flags, CJ_FLAG_TIMEOUT);
+            const bool got_prefix =
+                __shfl_sync(FULL, mbar_wait(&S.prefix_ready[q], (parity >> (kPB + q)) & 1u), 0);
             parity ^= 1u << (kPB + q);
-            const TileGeom g = tile_geom(P, prev_tile);
-            phase_c(P, g, S.slot[q], warp, lane);
+            if (got_prefix) {
+                const TileGeom g = tile_geom(P, prev_tile);
+                phase_c(P, g, S.slot[q], warp, lane);
+            } else if (lane == 0) {
+                atomicOr(&P.ctrl->error_flags, CJ_FLAG_TIMEOUT);   // no entry value: no writes
+            }
         }
         if (tile == kNoTile) break;
         prev_tile = tile;

@@ -83,3 +83,33 @@ def test_config4_batch_full(cj, oracle, ctx):
             continue
         assert status[i] == cj.OK and ref.valid, i
         np.testing.assert_array_equal(layout[off[i]:off[i + 1]], ref.reference_layout(), err_msg=f"doc {i}")
+
+
+def test_overlapped_copy_pinned(cj, oracle, ctx):
+    """One-shot parses of pinned inputs of 64 MiB and more copy the input on a
+    second stream while the scan runs; results equal the oracle's and the
+    staged (copy-then-run) path's."""
+    doc = cj.synth_document(0x0E71A9, (80 << 20) + 12345, max_depth=12)
+    pin = cj.PinnedBuffer(doc.size)
+    pin.array[:] = doc
+    ref = oracle.parse(doc)
+    res = ctx.parse_standard_json(pin.array)
+    np.testing.assert_array_equal(res.buffer, ref.reference_layout())
+    out = np.zeros(2 * ref.n_structural + 4, np.int32)
+    info = ctx.parse_into(pin.array, out)
+    assert info.status == cj.OK
+    np.testing.assert_array_equal(out, ref.reference_layout())
+    ctx.stage_standard(doc)
+    ctx.run()
+    np.testing.assert_array_equal(ctx.staged_result().buffer, res.buffer)
+    pin.close()
+    lines, _ = cj.synth_lines(0x0E71AA, 96 << 20)
+    pl = cj.PinnedBuffer(lines.size)
+    pl.array[:] = lines
+    sizes = cj.plan_lines_count(lines, 3)
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    res = ctx.parse_json_lines([pl.array[offs[i]:offs[i + 1]] for i in range(3)])
+    ref = oracle.parse(lines, lines=True, chunk_sizes=sizes)
+    np.testing.assert_array_equal(res.positions, ref.positions)
+    np.testing.assert_array_equal(res.pair_row, ref.pair_row)
+    pl.close()
