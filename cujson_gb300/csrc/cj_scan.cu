@@ -52,7 +52,7 @@ namespace {
 constexpr int kStages = 3;                // TMA ring depth per warp
 constexpr int kMaskFields = 5;            // st, br, op, cur, M per lane per step
 constexpr uint32_t kSpinLimit = 1u << 22; // look-back polls before giving up
-constexpr int kLookPerLane = 4;           // predecessors per lane and look-back round
+constexpr int kLookPerLane = 2;           // predecessors per lane and look-back round
 constexpr uint32_t kWaitLimit = 1u << 20; // mbarrier polls before giving up
 constexpr uint32_t kInputWaitLimit = 1u << 22;   // polls (>= 256 ns each) for input bytes
 constexpr uint32_t FULL = 0xFFFFFFFFu;
@@ -202,36 +202,9 @@ __device__ __forceinline__ TileGeom tile_geom(const ScanParams& P, uint32_t tile
 }
 
 // Phase A of one warp's region: classify, validate, resolve strings, keep masks.
-// The ring runs on across tiles: step j of a tile uses stage (rstage + j) mod
-// kStages.  When the last steps of a tile free their stages and the warp's
-// next tile is already known (its slot's tile_ready phase has completed), the
-// first steps of the next tile are loaded into them ahead of time; `pf` counts
-// those steps for the next call.
-struct Ring {
-    uint32_t rstage = 0;   // stage of step 0 of the current tile
-    int pf = 0;            // steps of the current tile already in flight
-};
-
-__device__ __forceinline__ bool mbar_test(unsigned long long* bar, uint32_t parity) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done) : "r"(smem_u32(bar)), "r"(parity) : "memory");
-    return done != 0;
-}
-
-__device__ __forceinline__ int region_steps(const TileGeom& g, int warp) {
-    const int reg_len = max(0, min(kWarpBytes, g.tile_len - warp * kWarpBytes));
-    return (reg_len + kStepBytes - 1) / kStepBytes;
-}
-
 template <bool LINES>
 __device__ __forceinline__ void phase_a(const ScanParams& P, const TileGeom& g, WarpSmem& W, Slot& sl,
-                                        uint32_t& parity, int warp, int lane, uint32_t lt, Ring& ring,
-                                        const Slot& next_slot, unsigned long long* next_ready,
-                                        uint32_t next_parity)
+                                        uint32_t& parity, int warp, int lane, uint32_t lt)
 {
     const int reg_off = warp * kWarpBytes;
     const int reg_len = max(0, min(kWarpBytes, g.tile_len - reg_off));
@@ -239,25 +212,16 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileGeom& g, 
     const uint8_t* reg_src = g.seg_base + g.tile_off + reg_off;
     if (lane == 0) {
         fence_proxy_async();
-        uint32_t st = ring.rstage + (uint32_t)ring.pf;
-        st = st >= (uint32_t)kStages ? st - kStages : st;
-        for (int j = ring.pf; j < kStages && j < nsteps; j++) {
-            tma_load(W.ring[st], reg_src + (size_t)j * kStepBytes, &W.mbar[st]);
-            st = (st + 1 == (uint32_t)kStages) ? 0u : st + 1;
-        }
+        for (int j = 0; j < kStages && j < nsteps; j++)
+            tma_load(W.ring[j], reg_src + (size_t)j * kStepBytes, &W.mbar[j]);
     }
-    // next tile's region, known once lane 0 has seen its slot's tile_ready
-    const uint8_t* nsrc = nullptr;
-    int nsteps_next = -1;        // -1: not looked up yet
-    int pf_next = 0;
-    uint32_t st_i = ring.rstage;
     uint32_t carry = 0, par = 0;           // escape carry / quote parity (warp uniform)
     uint32_t started = 0, wflip = 0;       // first non-all-backslash lane seen / its flip
     uint32_t prev_last = (g.tile_off + (uint64_t)reg_off > 0 && nsteps > 0)
                              ? __ldg(reinterpret_cast<const uint32_t*>(reg_src) - 1) : 0u;
     uint32_t n_c0 = 0, n_ct = 0, n_k0 = 0, n_kt = 0, n_o0 = 0, n_ot = 0;   // per lane
     for (int j = 0; j < nsteps; j++) {
-        if (j > 0) st_i = (st_i + 1 == (uint32_t)kStages) ? 0u : st_i + 1;
+        const int st_i = j % kStages;
         if (!mbar_wait(&W.mbar[st_i], (parity >> st_i) & 1u)) {
             if (lane == 0) atomicOr(&P.ctrl->error_flags, CJ_FLAG_TIMEOUT);
         }
@@ -271,28 +235,9 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileGeom& g, 
         uint4 va = *reinterpret_cast<const uint4*>(&W.ring[st_i][my0 + 16 * r0]);
         uint4 vb = *reinterpret_cast<const uint4*>(&W.ring[st_i][my0 + 16 * (r0 ^ 1)]);
         __syncwarp();
-        if (lane == 0) {
-            if (j + kStages < nsteps) {
-                fence_proxy_async();
-                tma_load(W.ring[st_i], reg_src + (size_t)(j + kStages) * kStepBytes, &W.mbar[st_i]);
-            } else {
-                // this stage is free for good: the next tile's step m, if known
-                const int m = j + kStages - nsteps;
-                if (nsteps_next < 0 && mbar_test(next_ready, next_parity)) {
-                    const uint32_t nt = next_slot.tile;
-                    nsteps_next = 0;
-                    if (nt != kNoTile) {
-                        const TileGeom ng = tile_geom(P, nt);
-                        nsteps_next = region_steps(ng, warp);
-                        nsrc = ng.seg_base + ng.tile_off + reg_off;
-                    }
-                }
-                if (m == pf_next && m < nsteps_next) {
-                    fence_proxy_async();
-                    tma_load(W.ring[st_i], nsrc + (size_t)m * kStepBytes, &W.mbar[st_i]);
-                    pf_next = m + 1;
-                }
-            }
+        if (lane == 0 && j + kStages < nsteps) {
+            fence_proxy_async();
+            tma_load(W.ring[st_i], reg_src + (size_t)(j + kStages) * kStepBytes, &W.mbar[st_i]);
         }
         uint4 lo = r0 ? vb : va, hi = r0 ? va : vb;
         if (16 > valid) mask_chunk(lo, valid);
@@ -361,11 +306,6 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileGeom& g, 
         m[2][lane] = c.op;
         m[3][lane] = c.cur;
         m[4][lane] = M;
-    }
-    {
-        uint32_t st = ring.rstage + (uint32_t)(nsteps % kStages);
-        ring.rstage = st >= (uint32_t)kStages ? st - kStages : st;
-        ring.pf = __shfl_sync(FULL, pf_next, 0);
     }
     // the warp's transfer table, relative to the state it is entered in
     const int32_t C0 = (int32_t)__reduce_add_sync(FULL, n_c0), Ct = (int32_t)__reduce_add_sync(FULL, n_ct);
@@ -650,10 +590,8 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
     if (warp == kWarps) {
         // ---- coordinator: hand out tiles, publish, look back, derive entries ---------
         if (lane == 0) {
-            for (int s = 0; s < 2; s++) {
-                S.slot[s].tile = next_tile(P);
-                mbar_arrive(&S.tile_ready[s]);
-            }
+            S.slot[0].tile = next_tile(P);
+            mbar_arrive(&S.tile_ready[0]);
         }
         __syncwarp();
         uint32_t use = 0;          // bit s: phase parity of slot s's a_done
@@ -665,6 +603,14 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
             if (!mbar_wait(&S.a_done[s], (use >> s) & 1u) && lane == 0)
                 atomicOr(&P.ctrl->error_flags, CJ_FLAG_TIMEOUT);
             use ^= 1u << s;
+            // the warps go on to phase C of the other slot's tile and then
+            // start that slot's next one: hand it out now, just in time, so
+            // that tiles are taken in the order their phase A begins and a
+            // look-back rarely waits on a predecessor that has not started
+            if (lane == 0) {
+                S.slot[s ^ 1].tile = next_tile(P);
+                mbar_arrive(&S.tile_ready[s ^ 1]);
+            }
             const TileGeom g = tile_geom(P, tile);
             // inclusive scan of the 16 warp tables over lanes 0..15, then the
             // tile's table (lane 15) and each warp's exclusive prefix table
@@ -708,13 +654,7 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
             }
             finish_prefix(P, g, sl, excl, T, pre, ep, lane);
             __syncwarp();
-            if (lane == 0) {
-                mbar_arrive(&S.prefix_ready[s]);
-                // the slot's next tile: the classifying warps read it only
-                // after their phase C of this one
-                sl.tile = next_tile(P);
-                mbar_arrive(&S.tile_ready[s]);
-            }
+            if (lane == 0) mbar_arrive(&S.prefix_ready[s]);
             __syncwarp();
             s ^= 1;
         }
@@ -728,7 +668,6 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
     // bits for the slots' tile_ready and two for their prefix_ready
     constexpr int kTB = kStages, kPB = kStages + 2;
     uint32_t parity = 0;
-    Ring ring;
     int s = 0;
     uint32_t prev_tile = kNoTile;
     while (true) {
@@ -740,8 +679,7 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
         const uint32_t tile = got_tile ? S.slot[s].tile : kNoTile;
         if (tile != kNoTile) {
             const TileGeom g = tile_geom(P, tile);
-            phase_a<LINES>(P, g, W, S.slot[s], parity, warp, lane, lt, ring, S.slot[s ^ 1],
-                           &S.tile_ready[s ^ 1], (parity >> (kTB + (s ^ 1))) & 1u);
+            phase_a<LINES>(P, g, W, S.slot[s], parity, warp, lane, lt);
             __syncwarp();
             if (lane == 0) mbar_arrive(&S.a_done[s]);
         }
