@@ -112,6 +112,7 @@ _SIGNATURES = {
                                       ctypes.c_size_t]),
     "cj_run_staged": (ctypes.c_int, [ctypes.c_void_p]),
     "cj_run_staged_graph": (ctypes.c_int, [ctypes.c_void_p]),
+    "cj_run_staged_starved": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(ParseInfo)]),
     "cj_server_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
     "cj_server_destroy": (None, [ctypes.c_void_p]),
     "cj_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,

@@ -109,6 +109,7 @@ struct cj_context {
     cudaEvent_t ev_reset = nullptr, ev_copied = nullptr;
     unsigned long long* d_ready = nullptr;
     bool overlap_run = false;
+    uint32_t input_wait_limit = 0;      // 0: the kernel's default
     // cuStreamWriteValue64 when the driver offers it (no kernel needs to run
     // beside the scan to raise d_ready); else a one-thread kernel does it
     CUresult (*write64)(CUstream, CUdeviceptr, cuuint64_t, unsigned int) = nullptr;
@@ -317,6 +318,7 @@ cj_status enqueue(cj_context* ctx, bool graph)
     sp.epoch = ctx->epoch;
     sp.seg_err = ctx->batch ? ctx->seg_err.p : nullptr;
     sp.ready = ctx->overlap_run ? ctx->d_ready : nullptr;
+    sp.input_wait_limit = ctx->input_wait_limit;
     uint32_t scan_grid = ctx->scan_grid;
     if (ctx->tune_scan_ctas) scan_grid = std::min(scan_grid, ctx->tune_scan_ctas);
     launch_scan(sp, ctx->lines, (int)std::min<uint32_t>(ctx->n_tiles, scan_grid), ctx->stream);
@@ -1141,6 +1143,25 @@ cj_status cj_autotune_staged(cj_context* ctx, int32_t reps, cj_tuning* best, cj_
     cj_context_set_tuning(ctx, &win);
     if (best) *best = win;
     return finish(CJ_OK);
+}
+
+cj_status cj_run_staged_starved(cj_context* ctx, uint32_t polls, cj_parse_info* info)
+{
+    if (!ctx || polls == 0) return finish(CJ_ERR_INVALID_ARGUMENT);
+    if (!ctx->staged || ctx->batch) return finish(CJ_ERR_NOT_STAGED);
+    if (cudaSetDevice(ctx->device) != cudaSuccess ||
+        cudaMemsetAsync(ctx->d_ready, 0, sizeof(unsigned long long), ctx->stream) != cudaSuccess)
+        return finish(CJ_ERR_CUDA);
+    ctx->overlap_run = true;
+    ctx->input_wait_limit = polls;
+    cj_status st = enqueue(ctx, false);
+    ctx->overlap_run = false;
+    ctx->input_wait_limit = 0;
+    cj_parse_info local;
+    if (!info) info = &local;
+    if (!st) st = read_info(ctx, info);
+    if (!st) st = (cj_status)info->status;
+    return finish(st);
 }
 
 const char* cj_status_string(int status)

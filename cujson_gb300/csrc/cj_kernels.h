@@ -30,6 +30,7 @@ struct ScanParams {
     // memory, raised by the host's copies while the scan runs; a tile is
     // handed out once its bytes are there.  nullptr: all input is present.
     const unsigned long long* ready;
+    uint32_t input_wait_limit;  // polls before a wait for input gives up (0: default)
 };
 
 struct PairParams {

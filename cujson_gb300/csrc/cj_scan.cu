@@ -552,9 +552,10 @@ __device__ __forceinline__ uint32_t next_tile(const ScanParams& P)
         const uint64_t padded = (g.seg_len + kPadBytes - 1) / kPadBytes * kPadBytes;
         const uint64_t end = g.tile_off + (uint64_t)kTileBytes;
         const uint64_t need = (uint64_t)(g.seg_base - P.in) + (end < padded ? end : padded);
+        const uint32_t limit = P.input_wait_limit ? P.input_wait_limit : kInputWaitLimit;
         uint32_t spins = 0;
         while (ld_acquire64(P.ready) < need) {
-            if (++spins > kInputWaitLimit) {
+            if (++spins > limit) {
                 atomicOr(&P.ctrl->error_flags, CJ_FLAG_TIMEOUT);
                 break;
             }

@@ -165,6 +165,13 @@ cj_status cj_staged_device_outputs(cj_context* ctx, const int32_t** d_positions,
  * graph; later calls launch that graph.  Results as cj_run_staged. */
 cj_status cj_run_staged_graph(cj_context* ctx);
 
+/* Failure-detection check (no reference counterpart): runs the staged input
+ * while the device count of input bytes present stays at zero, so the scan's
+ * bounded wait for input gives up after `polls` polls per tile; the kernel
+ * sets its timeout flag, finishes, and the context stays usable.  Returns the
+ * run's verdict: CJ_ERR_TIMEOUT. */
+cj_status cj_run_staged_starved(cj_context* ctx, uint32_t polls, cj_parse_info* info);
+
 /* ---- batches of independent documents ---------------------------------------
  * No counterpart in the reference, which parses one document per call
  * (parse_standard_json, cujson/parse_standard_json.cu:1584).  n_docs standard

@@ -137,3 +137,18 @@ def test_staged_and_into(cj, ctx, oracle):
 def test_empty_input_rejected(ctx):
     st, _ = ctx.try_parse(b"")
     assert st == 1
+
+
+def test_input_wait_timeout_reported(cj, ctx, oracle):
+    """A bounded wait that runs out: the scan waits for input bytes that a
+    counter nobody raises never reports; the kernel gives up after a few polls,
+    finishes with its timeout flag, and the context parses normally afterwards."""
+    import ctypes
+    d = cj.synth_document(4242, 300001)
+    ctx.stage_standard(d)
+    info = cj.ParseInfo()
+    st = cj.lib().cj_run_staged_starved(ctx.handle, 64, ctypes.byref(info))
+    assert st == cj.ERR_TIMEOUT and info.error_flags & 0x4
+    st2, res = ctx.try_parse(d)
+    assert st2 == cj.OK
+    np.testing.assert_array_equal(res.buffer, oracle.parse(d).reference_layout())
