@@ -55,6 +55,7 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-documents measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--no-query", action="store_true", help="skip the device query measurement")
     return ap.parse_args()
 
 
@@ -402,6 +403,78 @@ def run_serve(args, local):
     }
 
 
+QUERY_SEED = 0xC0DE5004
+
+
+def run_query(args, local):
+    """The reference's real-world query -- count the event records whose
+    "type" is "PushEvent" -- on the device over a resident JSON-Lines result,
+    end to end from a pinned file (parse + query), and the reference's host
+    record loop (oracle restatement, one core) on a bounded sample."""
+    import cujson_gb300 as cj
+    size = cj.MAX_INPUT_BYTES
+    pin = cj.PinnedBuffer(size)
+    t_gen = time.perf_counter()
+    doc, nrec, npush = cj.synth_events(QUERY_SEED, size)
+    pin.array[:] = doc
+    t_gen = time.perf_counter() - t_gen
+    sizes = cj.plan_lines_count(doc, 4)
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    chunks = [pin.array[offs[i]:offs[i + 1]] for i in range(len(sizes))]
+    ctx = cj.Context(local)
+    res = ctx.parse_json_lines(chunks)
+    S = res.n_structural
+    del res
+    key, val = b"type", b"PushEvent"
+    for _ in range(args.warmup):
+        n = ctx.query_count(key, val)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        n = ctx.query_count(key, val)
+    q_s = (time.perf_counter() - t0) / args.steps
+    for _ in range(max(1, args.warmup)):
+        ctx.stage_lines(pin.array, sizes)
+        ctx.run()
+        ctx.query_count(key, val)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.stage_lines(pin.array, sizes)
+        ctx.run()
+        n2 = ctx.query_count(key, val)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    ctx.close()
+    pin.close()
+    out = {
+        "workload": f"event-log JSON Lines, {size} B in 4 chunks, {nrec} records (seed {QUERY_SEED:#x}); "
+                    f"count the records whose \"type\" is \"PushEvent\"",
+        "records": nrec, "structurals": S, "matches": n, "matches_generator": npush,
+        "correct": n == npush and n2 == npush,
+        "query_ms": round(q_s * 1e3, 4), "records_per_s": round(nrec / q_s, 1),
+        "input_GBps": round(size / q_s / 1e9, 2),
+        "e2e_parse_plus_query_ms": round(e2e_s * 1e3, 3),
+        "e2e_GBps": round(size / e2e_s / 1e9, 2),
+        "generation_s": round(t_gen, 1),
+    }
+    if not args.no_cpu_baseline:
+        from oracle import cj_oracle
+        sample = min(size, args.cpu_sample)
+        sdoc, srec, _ = cj.synth_events(QUERY_SEED, sample)
+        ref = cj_oracle.parse(sdoc, lines=True)
+        t0 = time.perf_counter()
+        reps = 0
+        while True:
+            cj_oracle.query_lines(sdoc, ref, key, val)
+            reps += 1
+            if time.perf_counter() - t0 > 2.0:
+                break
+        cpu_s = (time.perf_counter() - t0) / reps
+        out["cpu_records_per_s"] = round(srec / cpu_s, 1)
+        out["cpu_sample"] = (f"{sample} B event-log sample, {srec} records, reference record loop "
+                             f"(gotoArrayIndex / checkKeyValue / gotoNextSibling) restated in C, 1 core")
+        out["speedup_vs_cpu_loop"] = round(out["records_per_s"] / out["cpu_records_per_s"], 1)
+    return out
+
+
 def run_ours(args, world, rank, local, pg):
     import cujson_gb300 as cj
     peak, peak_kind = measured_peaks()
@@ -473,6 +546,7 @@ def run_ours(args, world, rank, local, pg):
         return
     batch = None if args.no_batch else run_batch(args, local)
     serve = None if args.no_serve else run_serve(args, local)
+    query = None if args.no_query else run_query(args, local)
     cpu = None
     if not args.no_cpu_baseline:
         v, desc = cpu_baseline_sample(args.cpu_sample)
@@ -493,7 +567,7 @@ def run_ours(args, world, rank, local, pg):
                                "spine": round(spine_ms / runs, 4)},
         "parse_roofline_frac": round(B / (span_max / args.steps / 1e3) / 1e9 / peak, 4),
         "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": ck,
-        "batch": batch, "serving": serve,
+        "batch": batch, "serving": serve, "query": query,
     }
     print(json.dumps(line), flush=True)
 

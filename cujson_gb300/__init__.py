@@ -36,6 +36,7 @@ ERR_TIMEOUT = 7
 ERR_NO_DEVICE = 8
 ERR_CAPACITY = 9
 ERR_NOT_STAGED = 10
+ERR_UNSUPPORTED = 11
 
 FLAG_UTF8 = 0x01
 FLAG_BRACKETS = 0x02
@@ -112,6 +113,10 @@ _SIGNATURES = {
                                       ctypes.c_size_t]),
     "cj_run_staged": (ctypes.c_int, [ctypes.c_void_p]),
     "cj_run_staged_graph": (ctypes.c_int, [ctypes.c_void_p]),
+    "cj_query_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t, ctypes.c_char_p,
+                                      ctypes.c_size_t, ctypes.POINTER(ctypes.c_int64)]),
+    "cj_query_values": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t, ctypes.c_void_p,
+                                       ctypes.c_size_t, ctypes.POINTER(ctypes.c_int64)]),
     "cj_run_staged_starved": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(ParseInfo)]),
     "cj_server_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
     "cj_server_destroy": (None, [ctypes.c_void_p]),
@@ -160,6 +165,8 @@ _SIGNATURES = {
     "cj_synth_default_params": (None, [ctypes.POINTER(SynthParams)]),
     "cj_synth_document": (ctypes.c_size_t, [ctypes.c_uint64, ctypes.c_size_t,
                                             ctypes.POINTER(SynthParams), ctypes.c_void_p]),
+    "cj_synth_events": (ctypes.c_size_t, [ctypes.c_uint64, ctypes.c_size_t, ctypes.c_void_p,
+                                         ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
     "cj_synth_lines": (ctypes.c_size_t, [ctypes.c_uint64, ctypes.c_size_t, ctypes.POINTER(SynthParams),
                                          ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
     "cj_synth_deep": (ctypes.c_size_t, [ctypes.c_size_t, ctypes.c_void_p]),
@@ -343,6 +350,26 @@ class Context:
         buf = np.zeros(2 * S + 4, dtype=np.int32)
         _check(lib().cj_copy_staged_result(self._h, buf.ctypes.data, buf.size), "copy")
         return ParseResult(buf, S, int(inf.max_depth))
+
+    # ---- queries on the device over the staged JSON-Lines result --------------------
+    def query_count(self, key: bytes, value: bytes) -> int:
+        """Records whose `key` has the value `value` (checkKeyValue semantics)."""
+        n = ctypes.c_int64()
+        _check(lib().cj_query_count(self._h, key, len(key), value, len(value), ctypes.byref(n)), "query_count")
+        return n.value
+
+    def query_values(self, key: bytes, cap: Optional[int] = None) -> np.ndarray:
+        """int64[m, 3]: record offset, value offset, value length, in document
+        order, for the records that have `key`.  Without `cap`, a first pass
+        counts them."""
+        n = ctypes.c_int64()
+        if cap is None:
+            _check(lib().cj_query_values(self._h, key, len(key), None, 0, ctypes.byref(n)), "query_values")
+            cap = n.value
+        out = np.zeros((max(cap, 1), 3), np.int64)
+        _check(lib().cj_query_values(self._h, key, len(key), out.ctypes.data if cap else None, cap,
+                                     ctypes.byref(n)), "query_values")
+        return out[: n.value]
 
     def run_graph(self) -> None:
         _check(lib().cj_run_staged_graph(self._h), "run_graph")
@@ -676,6 +703,16 @@ def synth_lines(seed: int, size: int, **kw):
     if n != size:
         raise ValueError("synth_lines failed")
     return out, int(nrec.value)
+
+
+def synth_events(seed: int, size: int):
+    """Event-log JSON Lines of exactly `size` bytes: (bytes, records, PushEvent records)."""
+    out = np.empty(size, dtype=np.uint8)
+    nrec, npush = ctypes.c_uint64(), ctypes.c_uint64()
+    n = lib().cj_synth_events(seed, size, out.ctypes.data, ctypes.byref(nrec), ctypes.byref(npush))
+    if n != size:
+        raise ValueError("synth_events failed")
+    return out, int(nrec.value), int(npush.value)
 
 
 def synth_deep(depth: int) -> np.ndarray:

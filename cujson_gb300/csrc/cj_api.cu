@@ -114,6 +114,10 @@ struct cj_context {
     // beside the scan to raise d_ready); else a one-thread kernel does it
     CUresult (*write64)(CUstream, CUdeviceptr, cuuint64_t, unsigned int) = nullptr;
 
+    // queries over a staged JSON-Lines result
+    DevBuf<unsigned long long> q_count;
+    DevBuf<long long> q_out;
+
     // launch shapes (0 = default), set by cj_context_set_tuning / cj_autotune_staged
     uint32_t tune_scan_ctas = 0;
     uint32_t tune_pair_blocks = 0;
@@ -837,6 +841,7 @@ void cj_context_destroy(cj_context* ctx)
     release(ctx->spine); release(ctx->cinfo); release(ctx->tree);
     release(ctx->seg_err); release(ctx->seg_depth); release(ctx->rchunk_off);
     release(ctx->layout_off); release(ctx->layout); release(ctx->pack); release(ctx->pack_off);
+    release(ctx->q_count); release(ctx->q_out);
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
     if (ctx->d_ready) cudaFree(ctx->d_ready);
@@ -1164,6 +1169,65 @@ cj_status cj_run_staged_starved(cj_context* ctx, uint32_t polls, cj_parse_info* 
     return finish(st);
 }
 
+namespace {
+
+cj_status run_query(cj_context* ctx, const char* key, size_t key_len, const char* value, long value_len,
+                    int64_t* out, size_t cap, int64_t* n)
+{
+    if (!ctx || !key || !n || (value_len > 0 && !value)) return CJ_ERR_INVALID_ARGUMENT;
+    if (key_len > 256 || value_len > 256) return CJ_ERR_INVALID_ARGUMENT;
+    if (!ctx->staged || ctx->batch || !ctx->lines) return CJ_ERR_NOT_STAGED;
+    cj_parse_info info;
+    cj_status st = read_info(ctx, &info);       // the staged run has finished
+    if (st) return st;
+    if (info.status != CJ_OK) return (cj_status)info.status;
+    if ((st = ensure(ctx, ctx->q_count, 2))) return st;
+    if (out && cap && (st = ensure(ctx, ctx->q_out, 3 * cap))) return st;
+    CJ_CUDA(cudaMemsetAsync(ctx->q_count.p, 0, 2 * sizeof(unsigned long long), ctx->stream));
+    if (info.n_structural > 0) {
+        CJ_CUDA(launch_query(ctx->in.p, ctx->segs.p, ctx->n_segs, ctx->pos.p, ctx->pair.p,
+                             (uint32_t)info.n_structural, key, (int)key_len, value, (int)value_len,
+                             (int64_t)ctx->n_bytes, ctx->q_count.p, (out && cap) ? ctx->q_out.p : nullptr,
+                             (out && cap) ? cap : 0, ctx->sm_count, ctx->stream));
+        ctx->launches += 1;
+    }
+    unsigned long long cnt[2] = {0, 0};
+    CJ_CUDA(cudaMemcpyAsync(cnt, ctx->q_count.p, sizeof(cnt), cudaMemcpyDeviceToHost, ctx->stream));
+    CJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (cnt[1]) return CJ_ERR_UNSUPPORTED;
+    *n = (int64_t)cnt[0];
+    const unsigned long long m_all = cnt[0];
+    if (out && cap) {
+        const size_t m = std::min<size_t>(cap, (size_t)m_all);
+        CJ_CUDA(cudaMemcpyAsync(out, ctx->q_out.p, 3 * m * sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream));
+        CJ_CUDA(cudaStreamSynchronize(ctx->stream));
+        // records in document order
+        std::vector<size_t> idx(m);
+        for (size_t i = 0; i < m; i++) idx[i] = i;
+        std::sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return out[3 * a] < out[3 * b]; });
+        std::vector<int64_t> tmp(3 * m);
+        for (size_t i = 0; i < m; i++)
+            for (int k = 0; k < 3; k++) tmp[3 * i + k] = out[3 * idx[i] + k];
+        std::copy(tmp.begin(), tmp.end(), out);
+        if (m_all > cap) return CJ_ERR_CAPACITY;
+    }
+    return CJ_OK;
+}
+
+}  // namespace
+
+cj_status cj_query_count(cj_context* ctx, const char* key, size_t key_len, const char* value,
+                         size_t value_len, int64_t* count)
+{
+    return finish(run_query(ctx, key, key_len, value ? value : "", (long)value_len, nullptr, 0, count));
+}
+
+cj_status cj_query_values(cj_context* ctx, const char* key, size_t key_len, int64_t* out, size_t cap,
+                          int64_t* n_records)
+{
+    return finish(run_query(ctx, key, key_len, nullptr, -1, out, cap, n_records));
+}
+
 const char* cj_status_string(int status)
 {
     switch (status) {
@@ -1178,6 +1242,7 @@ const char* cj_status_string(int status)
     case CJ_ERR_NO_DEVICE: return "no CUDA device";
     case CJ_ERR_CAPACITY: return "output buffer too small";
     case CJ_ERR_NOT_STAGED: return "no staged input";
+    case CJ_ERR_UNSUPPORTED: return "query over records that span lines";
     default: return "unknown status";
     }
 }

@@ -70,6 +70,12 @@ const void* scan_kernel_ptr();     // for occupancy queries
 void launch_pair(const PairParams& p, int grid, cudaStream_t stream, int threads = 256);
 void launch_spine(const PairParams& p, int grid, cudaStream_t stream, int threads = 256);
 
+// key/value queries over a staged JSON-Lines result (cj_query.cu)
+cudaError_t launch_query(const uint8_t* in, const Segment* segs, uint32_t n_segs, const int32_t* pos,
+                         const int32_t* pair, uint32_t S, const char* key, int key_len, const char* value,
+                         int value_len, int64_t n_bytes, unsigned long long* count, long long* out,
+                         unsigned long long cap, int sm_count, cudaStream_t stream);
+
 // batches of independent documents (cj_batch.cu)
 void launch_batch_scatter(const uint8_t* packed, const uint64_t* src_off, const uint64_t* word_off,
                           const Segment* segs, uint32_t n, uint64_t total_words, uint8_t* in, int sm_count,

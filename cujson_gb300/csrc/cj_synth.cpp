@@ -222,6 +222,162 @@ void fill_block(uint64_t seed, const cj_synth_params& p, size_t budget, uint8_t*
     memset(dst + used, ' ', budget - used);
 }
 
+// Event-log records: one object per line shaped like a public activity feed
+// (an id, an event "type", actor / repo / payload objects, a timestamp) -- the
+// record shape the reference's real-world query runs over (counting the
+// records whose "type" is "PushEvent").  Values are random; what the shape
+// exercises is the query: nested objects that hold a "type" member of their
+// own, "type" placed after them in some records, absent in some, near-miss
+// values, spacing after ',' and ':' in some records, and blank lines.
+struct EventGen {
+    std::mt19937_64 rng;
+    std::string out;
+    explicit EventGen(uint64_t seed) : rng(seed) {}
+
+    double unit() { return (rng() >> 11) * (1.0 / 9007199254740992.0); }
+    int64_t uni(int64_t lo, int64_t hi) { return lo + (int64_t)(rng() % (uint64_t)(hi - lo + 1)); }
+
+    void word(int lo, int hi) {
+        static const char a[] = "abcdefghijklmnopqrstuvwxyz0123456789-";
+        int n = (int)uni(lo, hi);
+        for (int i = 0; i < n; i++) out.push_back(a[rng() % 37]);
+    }
+    void hex(int n) {
+        static const char h[] = "0123456789abcdef";
+        for (int i = 0; i < n; i++) out.push_back(h[rng() & 15]);
+    }
+    void num(int64_t lo, int64_t hi) { out += std::to_string(uni(lo, hi)); }
+    void text(int lo, int hi) {        // free text with escapes and a few UTF-8 characters
+        static const char a[] = "abcdefghijklmnopqrstuvwxyz ABCDEFGHIJ .,:;{}[]-_/#0123456789";
+        int n = (int)uni(lo, hi);
+        for (int i = 0; i < n; i++) {
+            double r = unit();
+            if (r < 0.02) out += "\\n";
+            else if (r < 0.03) out += "\\\"";
+            else if (r < 0.035) out += "\xc3\xa9";
+            else out.push_back(a[rng() % (sizeof(a) - 1)]);
+        }
+    }
+
+    const char* sep;   // "," or ", "
+    const char* col;   // ":" or ": "
+    void key(const char* k) {
+        out.push_back('"');
+        out += k;
+        out.push_back('"');
+        out += col;
+    }
+    void str_member(const char* k, bool first = false) {
+        if (!first) out += sep;
+        key(k);
+    }
+
+    void user(const char* k) {         // {"id":..,"login":"..","type":"User",..}
+        out += sep;
+        key(k);
+        out += "{";
+        key("id"); num(1, 99999999);
+        out += sep; key("login"); out += '"'; word(3, 16); out += '"';
+        out += sep; key("gravatar_id"); out += "\"\"";
+        if (unit() < 0.5) { out += sep; key("type"); out += unit() < 0.9 ? "\"User\"" : "\"Organization\""; }
+        out += sep; key("url"); out += "\"https://api.example.invalid/users/"; word(3, 16); out += '"';
+        out += "}";
+    }
+    void repo() {
+        out += sep; key("repo"); out += "{";
+        key("id"); num(1, 99999999);
+        out += sep; key("name"); out += '"'; word(3, 12); out += '/'; word(2, 20); out += '"';
+        out += sep; key("url"); out += "\"https://api.example.invalid/repos/"; word(3, 12); out += '"';
+        out += "}";
+    }
+    void payload(int kind) {
+        out += sep; key("payload"); out += "{";
+        if (kind == 0) {               // pushes: commits with messages
+            int n = (int)uni(1, 6);
+            key("push_id"); num(1, 999999999);
+            out += sep; key("size"); out += std::to_string(n);
+            out += sep; key("distinct_size"); out += std::to_string(n);
+            out += sep; key("ref"); out += "\"refs/heads/"; word(3, 12); out += '"';
+            out += sep; key("head"); out += '"'; hex(40); out += '"';
+            out += sep; key("before"); out += '"'; hex(40); out += '"';
+            out += sep; key("commits"); out += "[";
+            for (int i = 0; i < n; i++) {
+                if (i) out += sep;
+                out += "{"; key("sha"); out += '"'; hex(40); out += '"';
+                out += sep; key("author"); out += "{"; key("email"); out += '"'; word(3, 10); out += "@example.invalid\"";
+                out += sep; key("name"); out += '"'; word(3, 14); out += "\"}";
+                out += sep; key("message"); out += '"'; text(8, 160); out += '"';
+                out += sep; key("distinct"); out += (rng() & 1) ? "true" : "false";
+                out += "}";
+            }
+            out += "]";
+        } else if (kind == 1) {        // branch / tag creation
+            key("ref"); out += '"'; word(3, 12); out += '"';
+            out += sep; key("ref_type"); out += (rng() & 1) ? "\"branch\"" : "\"tag\"";
+            out += sep; key("master_branch"); out += "\"main\"";
+            out += sep; key("description"); out += unit() < 0.3 ? std::string("null") : std::string("\"x\"");
+        } else if (kind == 2) {        // issues and comments, with nested users that have a "type"
+            key("action"); out += "\"created\"";
+            out += sep; key("issue"); out += "{";
+            key("number"); num(1, 99999);
+            out += sep; key("title"); out += '"'; text(4, 60); out += '"';
+            user("user");
+            out += sep; key("labels"); out += "[";
+            int n = (int)uni(0, 3);
+            for (int i = 0; i < n; i++) {
+                if (i) out += sep;
+                out += "{"; key("name"); out += '"'; word(3, 10); out += "\"}";
+            }
+            out += "]";
+            out += sep; key("body"); out += '"'; text(0, 300); out += '"';
+            out += "}";
+        } else {                       // one-word actions
+            key("action"); out += "\"started\"";
+        }
+        out += "}";
+    }
+
+    // One record; returns 1 if its top-level "type" is exactly PushEvent.
+    int record() {
+        static const char* types[] = {"PushEvent", "CreateEvent", "WatchEvent", "IssueCommentEvent",
+                                      "PullRequestEvent", "IssuesEvent", "ForkEvent", "DeleteEvent",
+                                      "GollumEvent", "ReleaseEvent", "MemberEvent", "PublicEvent"};
+        static const double cum[] = {0.50, 0.62, 0.72, 0.80, 0.85, 0.89, 0.92, 0.95, 0.96, 0.97, 0.98, 1.0};
+        const bool spaced = unit() < 0.2;
+        sep = spaced ? ", " : ",";
+        col = spaced ? ": " : ":";
+        double r = unit();
+        int t = 0;
+        while (cum[t] < r) t++;
+        const int pk = t == 0 ? 0 : t == 1 || t == 7 ? 1 : t == 3 || t == 5 ? 2 : 3;
+        // where "type" goes: 0 second (usual), 1 after the nested objects, 2 absent
+        double w = unit();
+        const int place = w < 0.94 ? 0 : w < 0.99 ? 1 : 2;
+        // the value written: the type name, or (1%) a near miss
+        std::string tv = std::string("\"") + types[t] + "\"";
+        double m = unit();
+        if (m < 0.0025) tv = "\"PushEventX\"";
+        else if (m < 0.005) tv = "\"pushEvent\"";
+        else if (m < 0.0075) tv = "null";
+        else if (m < 0.01) tv = "{\"type\":\"PushEvent\"}";
+        const int hit = place != 2 && tv == "\"PushEvent\"";
+        out += "{";
+        key("id"); out += '"'; num(1000000000, 9999999999); out += '"';
+        if (place == 0) { out += sep; key("type"); out += tv; }
+        user("actor");
+        repo();
+        payload(pk);
+        if (place == 1) { out += sep; key("type"); out += tv; }
+        out += sep; key("public"); out += (unit() < 0.98) ? "true" : "false";
+        out += sep; key("created_at"); out += "\"2015-01-";
+        out += std::to_string(10 + uni(0, 18)); out += "T"; out += std::to_string(10 + uni(0, 13));
+        out += ":00:00Z\"";
+        if (unit() < 0.2) user("org");
+        out += "}";
+        return hit;
+    }
+};
+
 void run_parallel(size_t nblocks, unsigned threads, const std::function<void(size_t)>& fn)
 {
     if (threads == 0) threads = std::max(1u, std::thread::hardware_concurrency());
@@ -342,6 +498,48 @@ size_t cj_synth_lines(uint64_t seed, size_t size, const cj_synth_params* pp, uin
         for (auto c : counts) t += c;
         *n_records = t;
     }
+    return size;
+}
+
+// Event-log JSON Lines (EventGen above), exactly `size` bytes, blocks of 4 MiB
+// generated in parallel; blank lines between some records; the tail of every
+// block is spaces and a newline.  Returns bytes written; the record count and
+// the count of records whose top-level "type" is "PushEvent" through the
+// pointers.
+size_t cj_synth_events(uint64_t seed, size_t size, uint8_t* out, uint64_t* n_records, uint64_t* n_push)
+{
+    if (!out || size < 4) return 0;
+    const size_t bb = 4u << 20;
+    const size_t nblocks = std::max<size_t>(1, size / bb);
+    std::vector<uint64_t> counts(nblocks, 0), hits(nblocks, 0);
+    run_parallel(nblocks, 0, [&](size_t b) {
+        const size_t start = b * bb, budget = (b + 1 == nblocks) ? size - start : bb;
+        EventGen g(seed * 0xA0761D6478BD642Full + b + 11);
+        g.out.reserve(budget + 8192);
+        size_t used = 0;
+        uint64_t cnt = 0, hit = 0;
+        while (true) {
+            const size_t mark = g.out.size();
+            const int h = g.record();
+            g.out.push_back('\n');
+            if (g.unit() < 0.002) g.out.push_back('\n');
+            if (g.out.size() > budget) { g.out.resize(mark); break; }
+            used = g.out.size();
+            cnt++;
+            hit += h;
+        }
+        memcpy(out + start, g.out.data(), used);
+        if (budget > used) {
+            memset(out + start + used, ' ', budget - used);
+            out[start + budget - 1] = '\n';
+        }
+        counts[b] = cnt;
+        hits[b] = hit;
+    });
+    uint64_t c = 0, h = 0;
+    for (size_t b = 0; b < nblocks; b++) { c += counts[b]; h += hits[b]; }
+    if (n_records) *n_records = c;
+    if (n_push) *n_push = h;
     return size;
 }
 

@@ -51,7 +51,8 @@ typedef enum cj_status {
     CJ_ERR_TIMEOUT = 7,           /* a bounded device-side wait expired */
     CJ_ERR_NO_DEVICE = 8,
     CJ_ERR_CAPACITY = 9,          /* caller-provided output buffer too small */
-    CJ_ERR_NOT_STAGED = 10        /* cj_run_staged without a staged input */
+    CJ_ERR_NOT_STAGED = 10,       /* cj_run_staged without a staged input */
+    CJ_ERR_UNSUPPORTED = 11       /* a query over records that span lines (not JSON Lines) */
 } cj_status;
 
 /* detail bits in cj_parse_info.error_flags */
@@ -171,6 +172,27 @@ cj_status cj_run_staged_graph(cj_context* ctx);
  * sets its timeout flag, finishes, and the context stays usable.  Returns the
  * run's verdict: CJ_ERR_TIMEOUT. */
 cj_status cj_run_staged_starved(cj_context* ctx, uint32_t polls, cj_parse_info* info);
+
+/* ---- queries on the device over a staged JSON-Lines result -------------------
+ * The reference answers such queries on the host with its iterator, one record
+ * at a time (cuJSONLinesIterator::checkKeyValue / findKey / getValue,
+ * cujson/query/query_iterator.cpp:614, :447, :512; the loop of
+ * real_world_use_case/main.cu:70-86).  Here one device thread takes one line
+ * of the input last staged with cj_stage_lines (or parsed with cj_parse_lines)
+ * and run, and applies the iterator's rules to every record of the line (a
+ * '{' at the start of the result or after a top-level ',' or newline): the
+ * first top-level member whose key equals `key` decides.
+ * cj_query_count counts the records whose value for `key` is `value`
+ * (checkKeyValue); cj_query_values returns, for every record that has `key`,
+ * 3 int64 -- the record's byte offset, the value's byte offset and length as
+ * getValue slices it -- in document order, and CJ_ERR_CAPACITY when more than
+ * `cap` records have the key (`*n_records` is the full count then).  Keys and
+ * values are at most 256 bytes; a result whose records span lines is refused
+ * with CJ_ERR_UNSUPPORTED; a result that is not valid returns its verdict. */
+cj_status cj_query_count(cj_context* ctx, const char* key, size_t key_len, const char* value,
+                         size_t value_len, int64_t* count);
+cj_status cj_query_values(cj_context* ctx, const char* key, size_t key_len, int64_t* out, size_t cap,
+                          int64_t* n_records);
 
 /* ---- batches of independent documents ---------------------------------------
  * No counterpart in the reference, which parses one document per call
@@ -316,6 +338,7 @@ void   cj_synth_default_params(cj_synth_params* p);
 size_t cj_synth_document(uint64_t seed, size_t size, const cj_synth_params* p, uint8_t* out);
 size_t cj_synth_lines(uint64_t seed, size_t size, const cj_synth_params* p, uint8_t* out,
                       uint64_t* n_records);
+size_t cj_synth_events(uint64_t seed, size_t size, uint8_t* out, uint64_t* n_records, uint64_t* n_push);
 size_t cj_synth_deep(size_t depth, uint8_t* out);
 size_t cj_synth_backslash_string(uint64_t seed, size_t body, uint8_t* out);
 int    cj_synth_corrupt(uint8_t* doc, size_t n, int kind, uint64_t seed);

@@ -10,7 +10,7 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 LIB = BUILD / "libcj_oracle.so"
-SRC = [HERE / "cj_oracle.c"]
+SRC = [HERE / "cj_oracle.c", HERE / "cj_oracle_query.c"]
 
 
 def build(force: bool = False) -> Path:

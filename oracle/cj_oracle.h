@@ -77,6 +77,19 @@ int cjo_utf8_valid(const uint8_t* buf, size_t n);
  */
 int cjo_utf8_refcompat(const uint8_t* buf, size_t n);
 
+/*
+ * The reference's real-world query loop over a JSON-Lines result
+ * (cj_oracle_query.c): visit every record the way gotoArrayIndex(0) +
+ * gotoNextSibling(1) do, apply findKey(key) and getValue, and count the records
+ * that have `key` (check_value == 0) or whose value for it equals `value`
+ * (checkKeyValue).  `positions` / `pair_row` as cjo_parse writes them for the
+ * whole file.  Writes up to `cap` triples (record byte offset, value byte
+ * offset, value length) to `out` in visiting order; returns the count.
+ */
+int64_t cjo_query_lines(const uint8_t* buf, size_t n, const int32_t* positions, const int32_t* pair_row,
+                        size_t S, const uint8_t* key, size_t key_len, const uint8_t* value, size_t value_len,
+                        int check_value, int64_t* out, size_t cap);
+
 #ifdef __cplusplus
 }
 #endif

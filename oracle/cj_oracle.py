@@ -38,6 +38,10 @@ def lib():
                                 ctypes.POINTER(_Stats)]
         L.cjo_utf8_valid.restype = ctypes.c_int
         L.cjo_utf8_valid.argtypes = [ctypes.c_void_p, ctypes.c_size_t]
+        L.cjo_query_lines.restype = ctypes.c_int64
+        L.cjo_query_lines.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t, ctypes.c_char_p,
+                                      ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]
         L.cjo_utf8_refcompat.restype = ctypes.c_int
         L.cjo_utf8_refcompat.argtypes = [ctypes.c_void_p, ctypes.c_size_t]
         _lib = L
@@ -102,3 +106,18 @@ def utf8_valid(data) -> bool:
 def utf8_refcompat(data) -> bool:
     buf = _as_u8(data)
     return bool(lib().cjo_utf8_refcompat(buf.ctypes.data if buf.size else None, buf.size))
+
+
+def query_lines(data, res: OracleResult, key: bytes, value: Optional[bytes] = None, cap: int = 0):
+    """The reference's record loop (gotoArrayIndex(0), checkKeyValue / findKey +
+    getValue, gotoNextSibling(1)) over a JSON-Lines result: the count of
+    matching records and, with `cap`, int64[min(count, cap), 3] of (record byte
+    offset, value byte offset, value length) in visiting order."""
+    buf = _as_u8(data)
+    out = np.zeros((max(cap, 1), 3), np.int64)
+    pos = np.ascontiguousarray(res.positions, np.int32)
+    pair = np.ascontiguousarray(res.pair_row, np.int32)
+    n = lib().cjo_query_lines(buf.ctypes.data if buf.size else None, buf.size, pos.ctypes.data, pair.ctypes.data,
+                              res.n_structural, key, len(key), value or b"", len(value or b""),
+                              int(value is not None), out.ctypes.data if cap else None, cap)
+    return int(n), out[:min(int(n), cap)]
