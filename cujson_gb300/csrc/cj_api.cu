@@ -541,6 +541,7 @@ cj_status read_info(cj_context* ctx, cj_parse_info* info)
     const Ctrl& c = *ctx->h_ctrl;
     uint32_t flags = c.error_flags;
     if (c.neg_min_level > 0) flags |= CJ_FLAG_BRACKETS;
+    if (flags & CJ_FLAG_TIMEOUT) flags |= (c.gave_up & 0xFFu) << 16;
     cj_status verdict = CJ_OK;
     if (flags & CJ_FLAG_TIMEOUT) verdict = CJ_ERR_TIMEOUT;
     else if (flags & CJ_FLAG_UTF8) verdict = CJ_ERR_INVALID_UTF8;

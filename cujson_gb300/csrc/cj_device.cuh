@@ -71,7 +71,7 @@ struct Ctrl {
     int32_t  neg_min_level;   // max(-level) over brackets; > 0 means a close below depth 0
     int32_t  max_depth;
     uint32_t n_tiles_done;
-    uint32_t pad;
+    uint32_t gave_up;         // the first bounded wait that expired (scan kernel's wait codes), 0 if none
 };
 
 // ---- look-back descriptors -------------------------------------------------

@@ -51,9 +51,10 @@ namespace {
 
 constexpr int kStages = 3;                // TMA ring depth per warp
 constexpr int kMaskFields = 5;            // st, br, op, cur, M per lane per step
-constexpr uint32_t kSpinLimit = 1u << 22; // look-back polls before giving up
+constexpr uint32_t kSpinLimit = 1u << 20; // look-back polls before giving up
 constexpr int kLookPerLane = 2;           // predecessors per lane and look-back round
-constexpr uint32_t kWaitLimit = 1u << 20; // mbarrier polls before giving up
+constexpr uint32_t kWaitLimit = 1u << 20; // mbarrier polls (each suspends <= kPollNs) before giving up
+constexpr uint32_t kPollNs = 1000;
 constexpr uint32_t kInputWaitLimit = 1u << 22;   // polls (>= 256 ns each) for input bytes
 constexpr uint32_t FULL = 0xFFFFFFFFu;
 constexpr uint32_t kNoTile = 0xFFFFFFFFu;
@@ -135,16 +136,34 @@ __device__ __forceinline__ void tma_load(void* dst, const void* src, unsigned lo
         ::"r"(smem_u32(dst)), "l"(src), "r"((uint32_t)kStepBytes), "r"(smem_u32(bar)) : "memory");
 }
 
-// bounded wait for phase `parity` of `bar`; false if the limit was hit
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t parity) {
+// the run has been given up (some bounded wait expired): every other wait
+// then ends at once, so that a stall costs one wait's limit, not one per tile
+__device__ __noinline__ bool aborted(const Ctrl* ctrl) {
+    return (*reinterpret_cast<const volatile uint32_t*>(&ctrl->error_flags) & CJ_FLAG_TIMEOUT) != 0u;
+}
+
+// where a bounded wait gave up (Ctrl::gave_up; the first one is kept)
+enum : uint32_t { kGaveTileReady = 1, kGaveADone, kGavePrefixReady, kGaveLookBack, kGaveCopy, kGaveInput };
+
+__device__ __noinline__ void give_up(Ctrl* ctrl, uint32_t where) {
+    atomicCAS(&ctrl->gave_up, 0u, where);
+    atomicOr(&ctrl->error_flags, CJ_FLAG_TIMEOUT);
+}
+
+// bounded wait for phase `parity` of `bar`; false if the limit was hit or (with
+// `ctrl`) the run was given up.  Waits for a warp's own bulk copies pass no
+// `ctrl`: a copy in flight is always waited for, so no CTA exits with one
+// still writing into its shared memory.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t parity, const Ctrl* ctrl) {
     for (uint32_t i = 0; i < kWaitLimit; i++) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
             "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+            : "=r"(done) : "r"(smem_u32(bar)), "r"(parity), "n"(kPollNs) : "memory");
         if (done) return true;
+        if (ctrl && (i & 255u) == 255u && aborted(ctrl)) return false;
     }
     return false;
 }
@@ -222,8 +241,8 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileGeom& g, 
     uint32_t n_c0 = 0, n_ct = 0, n_k0 = 0, n_kt = 0, n_o0 = 0, n_ot = 0;   // per lane
     for (int j = 0; j < nsteps; j++) {
         const int st_i = j % kStages;
-        if (!mbar_wait(&W.mbar[st_i], (parity >> st_i) & 1u)) {
-            if (lane == 0) atomicOr(&P.ctrl->error_flags, CJ_FLAG_TIMEOUT);
+        if (!mbar_wait(&W.mbar[st_i], (parity >> st_i) & 1u, nullptr)) {
+            if (lane == 0) give_up(P.ctrl, kGaveCopy);
         }
         parity ^= 1u << st_i;
         const int step_len = min(kStepBytes, reg_len - j * kStepBytes);
@@ -421,8 +440,8 @@ __device__ __forceinline__ Ent look_back(const ScanParams& P, uint32_t tile, uin
         const int lim = (nl == 32) ? R * 32 : nl * R + n_incl;       // indices below use aggregates
         const bool blocked = (lane * R + r_notr) < lim && r_notr < R;
         if (__any_sync(FULL, blocked)) {
-            if (++spins > kSpinLimit) {
-                if (lane == 0) atomicOr(&P.ctrl->error_flags, CJ_FLAG_TIMEOUT);
+            if (++spins > kSpinLimit || ((spins & 255u) == 0u && aborted(P.ctrl))) {
+                if (lane == 0) give_up(P.ctrl, kGaveLookBack);
                 return ent_identity(0);
             }
             __nanosleep(32);
@@ -555,8 +574,8 @@ __device__ __forceinline__ uint32_t next_tile(const ScanParams& P)
         const uint32_t limit = P.input_wait_limit ? P.input_wait_limit : kInputWaitLimit;
         uint32_t spins = 0;
         while (ld_acquire64(P.ready) < need) {
-            if (++spins > limit) {
-                atomicOr(&P.ctrl->error_flags, CJ_FLAG_TIMEOUT);
+            if (++spins > limit || ((spins & 255u) == 0u && aborted(P.ctrl))) {
+                give_up(P.ctrl, kGaveInput);
                 break;
             }
             __nanosleep(256);
@@ -601,8 +620,7 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
             Slot& sl = S.slot[s];
             const uint32_t tile = sl.tile;
             if (tile == kNoTile) break;
-            if (!mbar_wait(&S.a_done[s], (use >> s) & 1u) && lane == 0)
-                atomicOr(&P.ctrl->error_flags, CJ_FLAG_TIMEOUT);
+            if (!mbar_wait(&S.a_done[s], (use >> s) & 1u, P.ctrl) && lane == 0) give_up(P.ctrl, kGaveADone);
             use ^= 1u << s;
             // the warps go on to phase C of the other slot's tile and then
             // start that slot's next one: hand it out now, just in time, so
@@ -674,8 +692,9 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
     while (true) {
         // a wait that expired (lane 0 decides for the warp) ends the warp's
         // work: the slot's contents are then not trusted
-        const bool got_tile = __shfl_sync(FULL, mbar_wait(&S.tile_ready[s], (parity >> (kTB + s)) & 1u), 0);
-        if (!got_tile && lane == 0) atomicOr(&P.ctrl->error_flags, CJ_FLAG_TIMEOUT);
+        const bool got_tile =
+            __shfl_sync(FULL, mbar_wait(&S.tile_ready[s], (parity >> (kTB + s)) & 1u, P.ctrl), 0);
+        if (!got_tile && lane == 0) give_up(P.ctrl, kGaveTileReady);
         parity ^= 1u << (kTB + s);
         const uint32_t tile = got_tile ? S.slot[s].tile : kNoTile;
         if (tile != kNoTile) {
@@ -687,13 +706,13 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
         if (prev_tile != kNoTile) {
             const int q = s ^ 1;
             const bool got_prefix =
-                __shfl_sync(FULL, mbar_wait(&S.prefix_ready[q], (parity >> (kPB + q)) & 1u), 0);
+                __shfl_sync(FULL, mbar_wait(&S.prefix_ready[q], (parity >> (kPB + q)) & 1u, P.ctrl), 0);
             parity ^= 1u << (kPB + q);
             if (got_prefix) {
                 const TileGeom g = tile_geom(P, prev_tile);
                 phase_c(P, g, S.slot[q], warp, lane);
             } else if (lane == 0) {
-                atomicOr(&P.ctrl->error_flags, CJ_FLAG_TIMEOUT);   // no entry value: no writes
+                give_up(P.ctrl, kGavePrefixReady);   // no entry value: no writes
             }
         }
         if (tile == kNoTile) break;

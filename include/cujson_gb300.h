@@ -60,6 +60,11 @@ typedef enum cj_status {
 #define CJ_FLAG_BRACKETS    0x02u
 #define CJ_FLAG_TIMEOUT     0x04u
 #define CJ_FLAG_OVERFLOW    0x08u
+/* with CJ_FLAG_TIMEOUT: bits 16-23 say which bounded wait of the scan kernel
+ * expired first (1 tile hand-out, 2 end of a tile's phase A, 3 a tile's entry
+ * value, 4 look-back, 5 input copy to shared memory, 6 input bytes from the
+ * host) */
+#define CJ_TIMEOUT_WAIT(flags) (((flags) >> 16) & 0xFFu)
 
 /* Largest input in bytes: positions are int32 (reference, cujson_types.h:26). */
 #define CJ_MAX_INPUT_BYTES 2147483646ull

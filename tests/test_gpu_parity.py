@@ -149,6 +149,7 @@ def test_input_wait_timeout_reported(cj, ctx, oracle):
     info = cj.ParseInfo()
     st = cj.lib().cj_run_staged_starved(ctx.handle, 64, ctypes.byref(info))
     assert st == cj.ERR_TIMEOUT and info.error_flags & 0x4
+    assert (info.error_flags >> 16) & 0xFF == 6      # the wait for input bytes expired
     st2, res = ctx.try_parse(d)
     assert st2 == cj.OK
     np.testing.assert_array_equal(res.buffer, oracle.parse(d).reference_layout())
