@@ -56,6 +56,8 @@ def parse_args():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-documents measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-query", action="store_true", help="skip the device query measurement")
+    ap.add_argument("--query-bytes", type=int, default=0,
+                    help="event-log bytes of the query measurement (default: the 2 GB JSON-Lines limit)")
     return ap.parse_args()
 
 
@@ -412,7 +414,7 @@ def run_query(args, local):
     end to end from a pinned file (parse + query), and the reference's host
     record loop (oracle restatement, one core) on a bounded sample."""
     import cujson_gb300 as cj
-    size = cj.MAX_INPUT_BYTES
+    size = args.query_bytes or cj.MAX_INPUT_BYTES
     pin = cj.PinnedBuffer(size)
     t_gen = time.perf_counter()
     doc, nrec, npush = cj.synth_events(QUERY_SEED, size)
