@@ -156,6 +156,26 @@ def build(ref: Path = DEFAULT_REF, force: bool = False) -> dict:
     return built
 
 
+def build_simdjson(ref: Path = DEFAULT_REF, force: bool = False):
+    """oracle/_ref/simdjson_bench: oracle/simdjson_driver.cpp with the simdjson
+    amalgamation the reference ships (paper_reproduced/related_works/simdjson/),
+    compiled where it lies; None when the reference tree is absent.  Built on
+    request only (timing a related CPU parser, not a checker)."""
+    sj = ref / "paper_reproduced" / "related_works" / "simdjson"
+    if not (sj / "simdjson.cpp").is_file():
+        return None
+    OUT.mkdir(parents=True, exist_ok=True)
+    exe = OUT / "simdjson_bench"
+    drv = HERE / "simdjson_driver.cpp"
+    if force or not exe.exists() or exe.stat().st_mtime < drv.stat().st_mtime:
+        cmd = ["g++", "-std=c++17", "-O3", "-DNDEBUG", "-w", f"-I{sj}", str(drv), str(sj / "simdjson.cpp"),
+               "-o", str(exe), "-pthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"simdjson build failed:\n{r.stderr[-3000:]}")
+    return exe
+
+
 if __name__ == "__main__":
     ref = Path(sys.argv[1]) if len(sys.argv) > 1 else DEFAULT_REF
     for k, v in build(ref, force=True).items():
