@@ -1182,9 +1182,9 @@ cj_status run_query(cj_context* ctx, const char* key, size_t key_len, const char
     cj_status st = read_info(ctx, &info);       // the staged run has finished
     if (st) return st;
     if (info.status != CJ_OK) return (cj_status)info.status;
-    if ((st = ensure(ctx, ctx->q_count, 2))) return st;
+    if ((st = ensure(ctx, ctx->q_count, 3))) return st;
     if (out && cap && (st = ensure(ctx, ctx->q_out, 3 * cap))) return st;
-    CJ_CUDA(cudaMemsetAsync(ctx->q_count.p, 0, 2 * sizeof(unsigned long long), ctx->stream));
+    CJ_CUDA(cudaMemsetAsync(ctx->q_count.p, 0, 3 * sizeof(unsigned long long), ctx->stream));
     if (info.n_structural > 0) {
         CJ_CUDA(launch_query(ctx->in.p, ctx->segs.p, ctx->n_segs, ctx->pos.p, ctx->pair.p,
                              (uint32_t)info.n_structural, key, (int)key_len, value, (int)value_len,

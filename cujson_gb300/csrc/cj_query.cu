@@ -55,7 +55,7 @@ struct QueryParams {
     uint8_t key[kMaxQuery];
     uint8_t value[kMaxQuery];
     int key_len, value_len;       // value_len < 0: no value comparison (extract only)
-    unsigned long long* count;    // [0] matches, [1] set when a record spans lines
+    unsigned long long* count;    // [0] matches, [1] set when a record spans lines, [2] tile ticket
     long long* out;               // 3 per match: record byte offset, value offset, value length
     unsigned long long cap;       // matches that fit `out`
 };
@@ -264,7 +264,9 @@ __global__ void __launch_bounds__(kQThreads, 6) query_tiles(QueryParams Q)
     uint32_t mine = 0;
     SegCursor cur;
     const uint64_t n_tiles = ((uint64_t)Q.S + kQTile - 1) / kQTile;
-    for (uint64_t tile = gwarp; tile < n_tiles; tile += n_warps) {
+    // the first tile of each warp by its index, the rest from a ticket counter,
+    // so that warps with slow records take fewer tiles
+    for (uint64_t tile = gwarp; tile < n_tiles;) {
         const int64_t base = (int64_t)tile * kQTile;
         if (lane == 0) {
             sh.n_lines[w] = base == 0 ? 1u : 0u;   // entry 0 starts the first line
@@ -320,6 +322,9 @@ __global__ void __launch_bounds__(kQThreads, 6) query_tiles(QueryParams Q)
             }
         }
         __syncwarp();
+        unsigned long long next = 0;
+        if (lane == 0) next = n_warps + atomicAdd(Q.count + 2, 1ull);
+        tile = __shfl_sync(0xffffffffu, next, 0);
     }
     if (!Q.out) {
         // one count per block
