@@ -190,8 +190,10 @@ cj_status cj_run_staged_starved(cj_context* ctx, uint32_t polls, cj_parse_info* 
  * cj_query_count counts the records whose value for `key` is `value`
  * (checkKeyValue); cj_query_values returns, for every record that has `key`,
  * 3 int64 -- the record's byte offset, the value's byte offset and length as
- * getValue slices it -- in document order, and CJ_ERR_CAPACITY when more than
- * `cap` records have the key (`*n_records` is the full count then).  Keys and
+ * getValue slices it -- in document order; with `out` NULL or `cap` 0 it only
+ * counts them.  CJ_ERR_CAPACITY when more than `cap` records have the key:
+ * `*n_records` is the full count and `out` holds `cap` of the triples (in
+ * document order, not necessarily the first ones).  Keys and
  * values are at most 256 bytes; a result whose records span lines is refused
  * with CJ_ERR_UNSUPPORTED; a result that is not valid returns its verdict. */
 cj_status cj_query_count(cj_context* ctx, const char* key, size_t key_len, const char* value,
