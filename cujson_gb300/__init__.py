@@ -161,6 +161,7 @@ _SIGNATURES = {
                                            ctypes.POINTER(ctypes.c_size_t)]),
     "cj_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "cj_last_status": (ctypes.c_int, []),
+    "cj_last_error": (ctypes.c_char_p, []),
     "cj_set_last_status": (None, [ctypes.c_int]),
     "cj_synth_default_params": (None, [ctypes.POINTER(SynthParams)]),
     "cj_synth_document": (ctypes.c_size_t, [ctypes.c_uint64, ctypes.c_size_t,

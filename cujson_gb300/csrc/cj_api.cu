@@ -1250,5 +1250,6 @@ const char* cj_status_string(int status)
 
 int cj_last_status(void) { return g_last_status; }
 void cj_set_last_status(int status) { g_last_status = status; }
+const char* cj_last_error(void) { return cj_status_string(g_last_status); }
 
 }  // extern "C"

@@ -324,6 +324,10 @@ const char* cj_status_string(int status);
  * callers expect). */
 int cj_last_status(void);
 void cj_set_last_status(int status);
+/* The same as a message (cj_status_string(cj_last_status())): where the
+ * reference printed a reason and called exit(0) (parse_standard_json.cu,
+ * parse_json_lines.cu on invalid input), a caller reads it here. */
+const char* cj_last_error(void);
 
 /* ---- synthetic inputs -------------------------------------------------------
  * Seeded generators standing in for the reference's evaluation datasets (not
