@@ -36,7 +36,6 @@ ERR_TIMEOUT = 7
 ERR_NO_DEVICE = 8
 ERR_CAPACITY = 9
 ERR_NOT_STAGED = 10
-ERR_UNSUPPORTED = 11
 
 FLAG_UTF8 = 0x01
 FLAG_BRACKETS = 0x02

@@ -1186,16 +1186,17 @@ cj_status run_query(cj_context* ctx, const char* key, size_t key_len, const char
     if (out && cap && (st = ensure(ctx, ctx->q_out, 3 * cap))) return st;
     CJ_CUDA(cudaMemsetAsync(ctx->q_count.p, 0, 3 * sizeof(unsigned long long), ctx->stream));
     if (info.n_structural > 0) {
-        CJ_CUDA(launch_query(ctx->in.p, ctx->segs.p, ctx->n_segs, ctx->pos.p, ctx->pair.p,
-                             (uint32_t)info.n_structural, key, (int)key_len, value, (int)value_len,
-                             (int64_t)ctx->n_bytes, ctx->q_count.p, (out && cap) ? ctx->q_out.p : nullptr,
-                             (out && cap) ? cap : 0, ctx->sm_count, ctx->stream));
+        CJ_CUDA(launch_query(ctx->in.p, ctx->segs.p, ctx->n_segs, ctx->pos.p, ctx->pair.p, ctx->brk.p,
+                             (uint32_t)info.n_structural, (uint32_t)info.n_brackets, key, (int)key_len, value,
+                             (int)value_len, (int64_t)ctx->n_bytes, ctx->q_count.p,
+                             (out && cap) ? ctx->q_out.p : nullptr, (out && cap) ? cap : 0, ctx->sm_count,
+                             ctx->stream));
         ctx->launches += 1;
     }
     unsigned long long cnt[2] = {0, 0};
     CJ_CUDA(cudaMemcpyAsync(cnt, ctx->q_count.p, sizeof(cnt), cudaMemcpyDeviceToHost, ctx->stream));
     CJ_CUDA(cudaStreamSynchronize(ctx->stream));
-    if (cnt[1]) return CJ_ERR_UNSUPPORTED;
+    if (cnt[1]) return CJ_ERR_INVALID_BRACKETS;       // a malformed result (not reached for a valid one)
     *n = (int64_t)cnt[0];
     const unsigned long long m_all = cnt[0];
     if (out && cap) {
@@ -1243,7 +1244,6 @@ const char* cj_status_string(int status)
     case CJ_ERR_NO_DEVICE: return "no CUDA device";
     case CJ_ERR_CAPACITY: return "output buffer too small";
     case CJ_ERR_NOT_STAGED: return "no staged input";
-    case CJ_ERR_UNSUPPORTED: return "query over records that span lines";
     default: return "unknown status";
     }
 }

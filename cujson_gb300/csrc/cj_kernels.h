@@ -72,9 +72,9 @@ void launch_spine(const PairParams& p, int grid, cudaStream_t stream, int thread
 
 // key/value queries over a staged JSON-Lines result (cj_query.cu)
 cudaError_t launch_query(const uint8_t* in, const Segment* segs, uint32_t n_segs, const int32_t* pos,
-                         const int32_t* pair, uint32_t S, const char* key, int key_len, const char* value,
-                         int value_len, int64_t n_bytes, unsigned long long* count, long long* out,
-                         unsigned long long cap, int sm_count, cudaStream_t stream);
+                         const int32_t* pair, const uint2* brk, uint32_t S, uint32_t K, const char* key,
+                         int key_len, const char* value, int value_len, int64_t n_bytes, unsigned long long* count,
+                         long long* out, unsigned long long cap, int sm_count, cudaStream_t stream);
 
 // batches of independent documents (cj_batch.cu)
 void launch_batch_scatter(const uint8_t* packed, const uint64_t* src_off, const uint64_t* word_off,

@@ -9,14 +9,15 @@
 // follow a top-level separator (a ',' entry, or a newline entry, which the
 // iterator's getChar reports as ','); every other top-level item is skipped.
 //
-// Here one persistent kernel does it; each warp takes tiles of 1024 entries on
-// its own (no block-wide barrier, so a slow record holds up only its warp).
-// First the warp reads the tile's structural positions coalesced, eight
-// independent loads per lane at a time, and compacts in shared memory every
-// entry that starts a line (index 0, or the entry after a newline entry).
-// Then each lane takes a line, walks its top-level items up to the next
-// newline entry, jumping containers with the pair row, and queries each record
-// it meets with the iterator's rules, on 0-based byte offsets where a byte
+// Here the records come from the parse itself: the scan kernel leaves one
+// bracket record per bracket (structural index, nesting level, open flag,
+// brace or square) on the device, and the iterator's records are exactly the
+// '{' opens at level 0 whose previous entry is a ',' or a newline entry (or
+// that are entry 0) -- a separator just before a level-0 open is itself at
+// level 0.  One persistent kernel, warp by warp: a warp reads a tile of 512
+// bracket records coalesced, compacts the level-0 brace opens in shared
+// memory, and each lane then checks a candidate's previous entry and queries
+// the record with the iterator's rules, on 0-based byte offsets where a byte
 // outside the file reads as 0:
 //   key of the ':' at s:  from the first non-space after the previous
 //       structural (a) to the last non-space before the ':' (b), the slice
@@ -25,12 +26,9 @@
 //       close; else from jumpValueForward(':') to jumpValueBackward(next
 //       structural): spaces skipped, one quote dropped at each end;
 //   slices clamp to the file, an empty or negative length is "".
-// The first member whose key equals the query key decides (findKey).
-//
-// A line whose walk meets a close bracket it did not open started inside a
-// container: a record spans lines (not JSON Lines).  The iterator's walk jumps
-// such records whole, which a line-parallel walk cannot follow, so the kernel
-// raises a flag and the query is refused rather than answered differently.
+// The first member whose key equals the query key decides (findKey).  The
+// depth comes from the parse, so records that span lines are found exactly as
+// the iterator's walk finds them.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -50,12 +48,14 @@ struct QueryParams {
     uint32_t n_segs;
     const int32_t* pos;
     const int32_t* pair;
+    const uint2* brk;             // bracket records: x = structural index | kCurly, y = level << 1 | open
     uint32_t S;
+    uint32_t K;                   // bracket records
     int64_t n_bytes;              // file length (all chunks)
     uint8_t key[kMaxQuery];
     uint8_t value[kMaxQuery];
     int key_len, value_len;       // value_len < 0: no value comparison (extract only)
-    unsigned long long* count;    // [0] matches, [1] set when a record spans lines, [2] tile ticket
+    unsigned long long* count;    // [0] matches, [1] set on a malformed result, [2] tile ticket
     long long* out;               // 3 per match: record byte offset, value offset, value length
     unsigned long long cap;       // matches that fit `out`
 };
@@ -179,24 +179,17 @@ __device__ bool query_record(const QueryParams& Q, SegCursor& cur, int64_t r, in
 
 constexpr int kQThreads = 256;
 constexpr int kQWarps = kQThreads / 32;
-constexpr int kQPerLane = 32;
-constexpr int kQTile = 32 * kQPerLane;            // structural entries per warp tile
+constexpr int kQPerLane = 16;
+constexpr int kQTile = 32 * kQPerLane;            // bracket records per warp tile
 constexpr int kQStage = 32;                       // matches staged per warp tile (extract mode)
 
 struct QueryShared {
-    uint16_t lines[kQWarps][kQTile];              // line starts, offsets in the warp's tile
+    uint32_t recs[kQWarps][kQTile];               // candidate records: structural index of the '{'
     long long staged[kQWarps][3 * kQStage];       // extract mode: matches of the warp's tile
-    uint32_t n_lines[kQWarps];
+    uint32_t n_recs[kQWarps];
     uint32_t n_staged[kQWarps];
     uint32_t warp_sum[kQWarps];
 };
-
-// device address of the byte at 0-based file offset b (inside the file)
-__device__ __forceinline__ const uint8_t* byte_ptr(const QueryParams& Q, SegCursor& c, int64_t b)
-{
-    if (b < c.lo || b >= c.hi) seek(Q, c, b);
-    return c.base + (b - c.lo);
-}
 
 // A match: counted per lane (count mode), or staged in shared memory and
 // written out once per warp tile (extract mode; a full stage falls back to a
@@ -223,36 +216,23 @@ __device__ __forceinline__ void record_match(const QueryParams& Q, QueryShared& 
     }
 }
 
-// Walk the line that starts at entry t: query every record that opens it or
-// follows a top-level ','.
-__device__ void walk_line(const QueryParams& Q, QueryShared& sh, uint32_t w, uint32_t& mine, int64_t t)
+// The level-0 '{' at entry u: a record if it is entry 0 or follows a ',' or a
+// newline entry; query it.
+__device__ __forceinline__ void query_candidate(const QueryParams& Q, QueryShared& sh, uint32_t w, uint32_t& mine,
+                                                int64_t u)
 {
     SegCursor cur;
-    bool item_start = true;
-    for (int64_t u = t; u < (int64_t)Q.S; u++) {
-        const uint8_t b = entry(Q, cur, u);
-        if (b == '\n') break;
-        if (b == '}' || b == ']') {                // closes what this line did not open
-            atomicOr(Q.count + 1, 1ull);
-            break;
-        }
-        if (b == '{' || b == '[') {
-            const int64_t c = (int64_t)__ldg(Q.pair + u) - 1;
-            if (c <= u || c >= (int64_t)Q.S) {       // not a valid result
-                atomicOr(Q.count + 1, 2ull);
-                break;
-            }
-            if (b == '{' && item_start) {
-                long long vs, vl;
-                if (query_record(Q, cur, u, c, vs, vl))
-                    record_match(Q, sh, w, mine, (long long)__ldg(Q.pos + u) - 1, vs, vl);
-            }
-            u = c;
-            item_start = false;
-            continue;
-        }
-        item_start = b == ',';
+    if (u > 0) {
+        const uint8_t prev = entry(Q, cur, u - 1);
+        if (prev != ',' && prev != '\n') return;
     }
+    const int64_t c = (int64_t)__ldg(Q.pair + u) - 1;
+    if (c <= u || c >= (int64_t)Q.S) {           // not a valid result
+        atomicOr(Q.count + 1, 1ull);
+        return;
+    }
+    long long vs, vl;
+    if (query_record(Q, cur, u, c, vs, vl)) record_match(Q, sh, w, mine, (long long)__ldg(Q.pos + u) - 1, vs, vl);
 }
 
 __global__ void __launch_bounds__(kQThreads, 6) query_tiles(QueryParams Q)
@@ -262,57 +242,49 @@ __global__ void __launch_bounds__(kQThreads, 6) query_tiles(QueryParams Q)
     const uint64_t gwarp = (uint64_t)blockIdx.x * kQWarps + w;
     const uint64_t n_warps = (uint64_t)gridDim.x * kQWarps;
     uint32_t mine = 0;
-    SegCursor cur;
-    const uint64_t n_tiles = ((uint64_t)Q.S + kQTile - 1) / kQTile;
+    const uint64_t n_tiles = ((uint64_t)Q.K + kQTile - 1) / kQTile;
     // the first tile of each warp by its index, the rest from a ticket counter,
     // so that warps with slow records take fewer tiles
     for (uint64_t tile = gwarp; tile < n_tiles;) {
-        const int64_t base = (int64_t)tile * kQTile;
+        const uint64_t base = tile * kQTile;
         if (lane == 0) {
-            sh.n_lines[w] = base == 0 ? 1u : 0u;   // entry 0 starts the first line
-            sh.lines[w][0] = 0;
+            sh.n_recs[w] = 0;
             sh.n_staged[w] = 0;
         }
         __syncwarp();
-        // entries t in [base-1, base+kQTile-1): a newline at t starts a line at t+1
+        // level-0 brace opens among the tile's bracket records
 #pragma unroll 1
         for (int j0 = 0; j0 < kQPerLane; j0 += 8) {
-            int32_t p[8];
+            uint2 r[8];
 #pragma unroll
             for (int j = 0; j < 8; j++) {
-                const int64_t t = base - 1 + (int64_t)(j0 + j) * 32 + lane;
-                p[j] = (t >= 0 && t + 1 < (int64_t)Q.S) ? __ldg(Q.pos + t) : 0;
+                const uint64_t t = base + (uint64_t)(j0 + j) * 32 + lane;
+                r[j] = t < Q.K ? __ldg(Q.brk + t) : make_uint2(0u, 0u);
             }
-            const uint8_t* a[8];
-#pragma unroll
-            for (int j = 0; j < 8; j++) a[j] = p[j] > 0 ? byte_ptr(Q, cur, (int64_t)p[j] - 1) : nullptr;
-            uint8_t b[8];
-#pragma unroll
-            for (int j = 0; j < 8; j++) b[j] = a[j] ? __ldg(a[j]) : 0;
 #pragma unroll
             for (int j = 0; j < 8; j++) {
-                const bool nl = b[j] == '\n';
-                const uint32_t m = __ballot_sync(0xffffffffu, nl);
+                const bool rec = (r[j].y == 1u) && (r[j].x & kCurly);       // open, level 0, brace
+                const uint32_t m = __ballot_sync(0xffffffffu, rec);
                 if (!m) continue;
                 uint32_t b0 = 0;
                 if (lane == 0) {
-                    b0 = sh.n_lines[w];
-                    sh.n_lines[w] = b0 + __popc(m);
+                    b0 = sh.n_recs[w];
+                    sh.n_recs[w] = b0 + __popc(m);
                 }
                 b0 = __shfl_sync(0xffffffffu, b0, 0);
-                if (nl) sh.lines[w][b0 + __popc(m & ((1u << lane) - 1))] = (uint16_t)((j0 + j) * 32 + lane);
+                if (rec) sh.recs[w][b0 + __popc(m & ((1u << lane) - 1))] = r[j].x & ~kCurly;
             }
         }
         __syncwarp();
-        const uint32_t n_lines = sh.n_lines[w];
-        for (uint32_t k = lane; k < n_lines; k += 32) walk_line(Q, sh, w, mine, base + sh.lines[w][k]);
+        const uint32_t n = sh.n_recs[w];
+        for (uint32_t k = lane; k < n; k += 32) query_candidate(Q, sh, w, mine, (int64_t)sh.recs[w][k]);
         if (Q.out) {
             __syncwarp();
-            const uint32_t n = min(sh.n_staged[w], (uint32_t)kQStage);
+            const uint32_t ns = min(sh.n_staged[w], (uint32_t)kQStage);
             unsigned long long slot = 0;
-            if (lane == 0 && n) slot = atomicAdd(Q.count, (unsigned long long)n);
+            if (lane == 0 && ns) slot = atomicAdd(Q.count, (unsigned long long)ns);
             slot = __shfl_sync(0xffffffffu, slot, 0);
-            for (uint32_t k = lane; k < n; k += 32) {
+            for (uint32_t k = lane; k < ns; k += 32) {
                 const unsigned long long m = slot + k;
                 if (m < Q.cap) {
                     Q.out[3 * m] = sh.staged[w][3 * k];
@@ -342,7 +314,8 @@ __global__ void __launch_bounds__(kQThreads, 6) query_tiles(QueryParams Q)
 }
 
 cudaError_t launch_query(const uint8_t* in, const Segment* segs, uint32_t n_segs, const int32_t* pos,
-                         const int32_t* pair, uint32_t S, const char* key, int key_len, const char* value,
+                         const int32_t* pair, const uint2* brk, uint32_t S, uint32_t K, const char* key,
+                         int key_len, const char* value,
                          int value_len, int64_t n_bytes, unsigned long long* count, long long* out,
                          unsigned long long cap, int sm_count, cudaStream_t stream)
 {
@@ -353,7 +326,9 @@ cudaError_t launch_query(const uint8_t* in, const Segment* segs, uint32_t n_segs
     Q.n_segs = n_segs;
     Q.pos = pos;
     Q.pair = pair;
+    Q.brk = brk;
     Q.S = S;
+    Q.K = K;
     Q.n_bytes = n_bytes;
     for (int k = 0; k < key_len; k++) Q.key[k] = (uint8_t)key[k];
     for (int k = 0; k < value_len; k++) Q.value[k] = (uint8_t)value[k];
@@ -362,9 +337,9 @@ cudaError_t launch_query(const uint8_t* in, const Segment* segs, uint32_t n_segs
     Q.count = count;
     Q.out = out;
     Q.cap = cap;
-    const uint64_t tiles = ((uint64_t)S + kQTile - 1) / kQTile;
+    const uint64_t tiles = ((uint64_t)K + kQTile - 1) / kQTile;
     const uint64_t blocks = (tiles + kQWarps - 1) / kQWarps;
-    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(blocks, (uint64_t)sm_count * 8));
+    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(blocks, (uint64_t)sm_count * 6));
     query_tiles<<<grid, kQThreads, 0, stream>>>(Q);
     return cudaGetLastError();
 }

@@ -51,8 +51,7 @@ typedef enum cj_status {
     CJ_ERR_TIMEOUT = 7,           /* a bounded device-side wait expired */
     CJ_ERR_NO_DEVICE = 8,
     CJ_ERR_CAPACITY = 9,          /* caller-provided output buffer too small */
-    CJ_ERR_NOT_STAGED = 10,       /* cj_run_staged without a staged input */
-    CJ_ERR_UNSUPPORTED = 11       /* a query over records that span lines (not JSON Lines) */
+    CJ_ERR_NOT_STAGED = 10        /* cj_run_staged without a staged input */
 } cj_status;
 
 /* detail bits in cj_parse_info.error_flags */
@@ -182,20 +181,20 @@ cj_status cj_run_staged_starved(cj_context* ctx, uint32_t polls, cj_parse_info* 
  * The reference answers such queries on the host with its iterator, one record
  * at a time (cuJSONLinesIterator::checkKeyValue / findKey / getValue,
  * cujson/query/query_iterator.cpp:614, :447, :512; the loop of
- * real_world_use_case/main.cu:70-86).  Here one device thread takes one line
- * of the input last staged with cj_stage_lines (or parsed with cj_parse_lines)
- * and run, and applies the iterator's rules to every record of the line (a
- * '{' at the start of the result or after a top-level ',' or newline): the
- * first top-level member whose key equals `key` decides.
+ * real_world_use_case/main.cu:70-86, whose gotoNextSibling visits every '{'
+ * that opens the result or follows a top-level ',' or newline).  Here the
+ * device finds those records among the parse's bracket records (the level-0
+ * brace opens) of the input last staged with cj_stage_lines (or parsed with
+ * cj_parse_lines) and run, and applies the iterator's rules to each: the first
+ * top-level member whose key equals `key` decides.
  * cj_query_count counts the records whose value for `key` is `value`
  * (checkKeyValue); cj_query_values returns, for every record that has `key`,
  * 3 int64 -- the record's byte offset, the value's byte offset and length as
  * getValue slices it -- in document order; with `out` NULL or `cap` 0 it only
  * counts them.  CJ_ERR_CAPACITY when more than `cap` records have the key:
  * `*n_records` is the full count and `out` holds `cap` of the triples (in
- * document order, not necessarily the first ones).  Keys and
- * values are at most 256 bytes; a result whose records span lines is refused
- * with CJ_ERR_UNSUPPORTED; a result that is not valid returns its verdict. */
+ * document order, not necessarily the first ones).  Keys and values are at
+ * most 256 bytes; a result that is not valid returns its verdict. */
 cj_status cj_query_count(cj_context* ctx, const char* key, size_t key_len, const char* value,
                          size_t value_len, int64_t* count);
 cj_status cj_query_values(cj_context* ctx, const char* key, size_t key_len, int64_t* out, size_t cap,

@@ -54,6 +54,17 @@ HAND = {
         b'12\n'
         b'{"type":"PushEvent"}'
     ),
+    # records and values that span lines: the iterator jumps records whole,
+    # so a '{' after a newline inside a record is not a record
+    "hand_multiline": (
+        b'{"type":\n"PushEvent","a":1}\n'
+        b'{"x":{"type":"PushEvent"},\n"type":"PushEvent"}\n'
+        b'{"a":[\n{"type":"PushEvent"}\n],"type":"WatchEvent"}\n'
+        b'[{"type":"PushEvent"},\n{"type":"X"}]\n'
+        b'{"type" :\n "PushEvent" }\n'
+        b'{"type":"PushEvent"}\n'
+        b'{\n"id":7,\n"type":"PushEvent"\n}\n'
+    ),
     "hand_keys": (
         b'{"":1,"type":null}\n'
         b'{"t":"PushEvent","tt":{"":"x"}}\n'

@@ -72,18 +72,17 @@ def test_random_keys_config3_shape(cj, oracle, ctx):
     np.testing.assert_array_equal(got, want[:n])
 
 
-def test_capacity_and_refusals(cj, ctx):
+def test_capacity_multiline_and_refusals(cj, ctx):
     doc = np.frombuffer(b'{"type":"A"}\n{"type":"B"}\n{"type":"A"}\n', np.uint8)
     ctx.parse_json_lines([doc])
     assert ctx.query_count(b"type", b"A") == 2
     with pytest.raises(cj.CujsonError) as e:
         ctx.query_values(b"type", cap=2)
     assert e.value.status == cj.ERR_CAPACITY
-    # a record that spans lines is not JSON Lines: refused, not answered differently
-    ctx.parse_json_lines([np.frombuffer(b'{"type":\n"A"}\n{"type":"A"}\n', np.uint8)])
-    with pytest.raises(cj.CujsonError) as e:
-        ctx.query_count(b"type", b"A")
-    assert e.value.status == cj.ERR_UNSUPPORTED
+    # records that span lines are jumped whole, as the iterator's walk does
+    ml = np.frombuffer(b'{"type":"A",\n"b":{"type":"A"}}\n{"c":[\n{"type":"A"}]}\n{"type":"A"}\n', np.uint8)
+    ctx.parse_json_lines([ml])
+    assert ctx.query_count(b"type", b"A") == 2
     # standard JSON and batches are not JSON-Lines results
     ctx.parse_standard_json(np.frombuffer(b'[{"type":"A"}]', np.uint8))
     with pytest.raises(cj.CujsonError) as e:
