@@ -56,6 +56,7 @@ def parse_args():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-documents measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-query", action="store_true", help="skip the device query measurement")
+    ap.add_argument("--no-configs", action="store_true", help="skip configs 1 and 3")
     ap.add_argument("--query-bytes", type=int, default=0,
                     help="event-log bytes of the query measurement (default: the 2 GB JSON-Lines limit)")
     return ap.parse_args()
@@ -405,6 +406,43 @@ def run_serve(args, local):
     }
 
 
+def run_other_configs(args, local, peak):
+    """Device-resident parse of the other single-input configurations (config 1:
+    64 MiB standard JSON; config 3: 2 GB JSON Lines in 4 chunks), the same
+    kernels and the same timing as the headline line."""
+    import cujson_gb300 as cj
+    out = []
+    for config in (1, 3):
+        data, info = cj.config_input(config)
+        ctx = cj.Context(local)
+        if info["kind"] == "lines":
+            sizes = cj.plan_lines_count(data, 4)
+            ctx.stage_lines(data, sizes)
+        else:
+            ctx.stage_standard(data)
+        for _ in range(max(3, args.warmup)):
+            ctx.run()
+        inf = ctx.info()
+        assert inf.status == 0
+        S = int(inf.n_structural)
+        ctx.timing(True)
+        for _ in range(args.steps):
+            ctx.run()
+        scan_ms, pair_ms, spine_ms, runs = ctx.phase_ms()
+        span = ctx.span_ms() / args.steps
+        ctx.timing(False)
+        N = data.size
+        B = N + 8 * S
+        out.append({
+            "config": config, "workload": f"{info['kind']} {N} B (seed {cj.CONFIG_SEED_BASE + config:#x})",
+            "structurals": S, "GBps": round(N / (span / 1e3) / 1e9, 1), "ms_per_parse": round(span, 4),
+            "scan_ms": round(scan_ms / runs, 4), "scan_roofline_frac": round(B / (scan_ms / runs / 1e3) / 1e9 / peak, 4),
+            "l2": "input larger than L2" if N > (129 << 20) else "input 64 MiB < 129 MB L2 (no flush: warm-L2 figure)",
+        })
+        ctx.close()
+    return out
+
+
 QUERY_SEED = 0xC0DE5004
 
 
@@ -549,6 +587,7 @@ def run_ours(args, world, rank, local, pg):
     batch = None if args.no_batch else run_batch(args, local)
     serve = None if args.no_serve else run_serve(args, local)
     query = None if args.no_query else run_query(args, local)
+    others = None if args.no_configs else run_other_configs(args, local, peak)
     cpu = None
     if not args.no_cpu_baseline:
         v, desc = cpu_baseline_sample(args.cpu_sample)
@@ -569,7 +608,7 @@ def run_ours(args, world, rank, local, pg):
                                "spine": round(spine_ms / runs, 4)},
         "parse_roofline_frac": round(B / (span_max / args.steps / 1e3) / 1e9 / peak, 4),
         "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": ck,
-        "batch": batch, "serving": serve, "query": query,
+        "batch": batch, "serving": serve, "query": query, "other_configs": others,
     }
     print(json.dumps(line), flush=True)
 
