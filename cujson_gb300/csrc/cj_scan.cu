@@ -278,8 +278,9 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileGeom& g, 
                 }
             }
         } else {
-            // an all-ASCII step after a word without lead bytes: nothing to check
-            prev_last = __shfl_sync(FULL, w[7], 31);
+            // an all-ASCII step after a word without lead bytes: nothing to
+            // check, and the step's last word has no high bit either
+            prev_last = 0u;
         }
 
         // escapes: carry from the nearest earlier lane that is not all backslashes
