@@ -433,11 +433,29 @@ def run_other_configs(args, local, peak):
         ctx.timing(False)
         N = data.size
         B = N + 8 * S
+        e2e = None
+        if not args.no_e2e and info["kind"] == "lines":
+            # end to end through the C ABI: pinned input (one chunk; its copy
+            # overlaps the scan), parse, D2H of the reference layout
+            pin_in = cj.PinnedBuffer(N)
+            pin_in.array[:] = data
+            pin_out = cj.PinnedBuffer((2 * S + 4) * 4, dtype=np.int32)
+            ctx.parse_into(pin_in.array, pin_out.array, lines=True)
+            t0 = time.perf_counter()
+            for _ in range(3):
+                inf2 = ctx.parse_into(pin_in.array, pin_out.array, lines=True)
+            dt = (time.perf_counter() - t0) / 3
+            assert inf2.status == 0 and int(inf2.n_structural) == S
+            e2e = {"GBps": round(N / dt / 1e9, 1), "ms": round(dt * 1e3, 2), "h2d_bytes": N,
+                   "d2h_bytes": (2 * S + 4) * 4}
+            pin_in.close()
+            pin_out.close()
         out.append({
             "config": config, "workload": f"{info['kind']} {N} B (seed {cj.CONFIG_SEED_BASE + config:#x})",
             "structurals": S, "GBps": round(N / (span / 1e3) / 1e9, 1), "ms_per_parse": round(span, 4),
             "scan_ms": round(scan_ms / runs, 4), "scan_roofline_frac": round(B / (scan_ms / runs / 1e3) / 1e9 / peak, 4),
             "l2": "input larger than L2" if N > (129 << 20) else "input 64 MiB < 129 MB L2 (no flush: warm-L2 figure)",
+            "e2e": e2e,
         })
         ctx.close()
     return out
