@@ -93,3 +93,49 @@ def test_capacity_multiline_and_refusals(cj, ctx):
     with pytest.raises(cj.CujsonError) as e:
         ctx.query_count(b"k" * 257, b"A")
     assert e.value.status == cj.ERR_INVALID_ARGUMENT
+
+
+@pytest.mark.parametrize("seed", [11, 12, 13, 14, 15])
+def test_random_documents_and_keys(cj, oracle, ctx, seed):
+    """Random-key JSON Lines (the config-3 generator, several chunkings) and
+    event logs: keys drawn from the documents' records -- the records' own
+    top-level keys and nested keys -- counted and extracted on the device and
+    by the oracle, bit for bit."""
+    rng = np.random.default_rng(seed)
+    if seed % 2:
+        doc, _ = cj.synth_lines(seed, 3 << 20, max_depth=4)
+    else:
+        doc, _, _ = cj.synth_events(seed, 3 << 20)
+    n_chunks = int(rng.integers(1, 5))
+    sizes = cj.plan_lines_count(doc, n_chunks)
+    staged(ctx, doc, sizes)
+    ref = oracle.parse(doc, lines=True, chunk_sizes=sizes)
+    text = doc.tobytes()
+    # candidate keys: every quoted token followed by ':' in a few sampled lines
+    keys = set()
+    starts = np.flatnonzero(doc == ord("\n")) + 1
+    for st in rng.choice(starts[:-1], size=min(8, starts.size - 1), replace=False):
+        line = text[st:text.index(b"\n", st)]
+        i = 0
+        while len(keys) < 24:
+            a = line.find(b'"', i)
+            if a < 0:
+                break
+            b = line.find(b'"', a + 1)
+            if b < 0:
+                break
+            if line[b + 1:b + 2] == b":" and b - a - 1 <= 64 and b"\\" not in line[a + 1:b]:
+                keys.add(line[a + 1:b])
+            i = b + 1
+    assert keys
+    for key in sorted(keys):
+        n, want = oracle.query_lines(doc, ref, key, None, cap=1 << 18)
+        got = ctx.query_values(key)
+        assert got.shape[0] == n, key
+        np.testing.assert_array_equal(got, want[:n], err_msg=str(key))
+        if n:
+            # count the records whose value equals the first match's value
+            s, l = int(want[0, 1]), int(want[0, 2])
+            value = text[s:s + l][:256]
+            if len(text[s:s + l]) <= 256:
+                assert ctx.query_count(key, value) == oracle.query_lines(doc, ref, key, value)[0], key
