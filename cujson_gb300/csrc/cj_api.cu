@@ -419,7 +419,7 @@ __global__ void mark_ready(unsigned long long* ready, unsigned long long bytes)
 }
 
 constexpr size_t kOverlapMin = 64ull << 20;     // smaller inputs: one copy, then the run
-constexpr size_t kOverlapChunk = 32ull << 20;   // copy granularity of an overlapped run
+constexpr size_t kOverlapChunk = 64ull << 20;   // copy granularity of an overlapped run (16 / 32 / 64 / 128 MiB measured: 64 best)
 
 // Stage and run in one go, the input's copy overlapping the scan: the small
 // tables go first, then the scan is launched and the input follows in chunks
@@ -582,6 +582,11 @@ cj_status to_result(cj_context* ctx, const cj_parse_info& info, cj_result* out)
     CJ_CUDA(cudaMallocHost((void**)&buf, (size_t)(2 * S + 4) * sizeof(int32_t)));
     cj_status st = copy_result(ctx, S, buf, (size_t)(2 * S + 4));
     if (st) { cudaFreeHost(buf); return st; }
+    int64_t* seg_sizes = (int64_t*)malloc(sizeof(int64_t) * (ctx->n_segs ? ctx->n_segs : 1));
+    if (!seg_sizes) {
+        cudaFreeHost(buf);
+        return CJ_ERR_OUT_OF_MEMORY;
+    }
     out->structural = buf;
     out->pair_pos = buf + S + 1;
     out->n_structural = S;
@@ -589,7 +594,7 @@ cj_status to_result(cj_context* ctx, const cj_parse_info& info, cj_result* out)
     out->max_depth = info.max_depth;
     out->status = CJ_OK;
     out->n_segments = ctx->n_segs;
-    out->segment_sizes = (int64_t*)malloc(sizeof(int64_t) * ctx->n_segs);
+    out->segment_sizes = seg_sizes;
     uint32_t prev = 0;
     for (uint32_t i = 0; i < ctx->n_segs; i++) {
         out->segment_sizes[i] = (int64_t)(ctx->h_seg_out[i].s_end - prev);
