@@ -112,6 +112,10 @@ _SIGNATURES = {
                                       ctypes.c_size_t]),
     "cj_run_staged": (ctypes.c_int, [ctypes.c_void_p]),
     "cj_run_staged_graph": (ctypes.c_int, [ctypes.c_void_p]),
+    "cj_batch_padded_offsets": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
+                                               ctypes.POINTER(ctypes.c_size_t)]),
+    "cj_parse_batch_padded": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                             ctypes.c_int]),
     "cj_query_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t, ctypes.c_char_p,
                                       ctypes.c_size_t, ctypes.POINTER(ctypes.c_int64)]),
     "cj_query_values": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t, ctypes.c_void_p,
@@ -393,6 +397,15 @@ class Context:
         self._batch_n = int(sz.size)
         _check(lib().cj_stage_batch_packed(self._h, buf.ctypes.data, sz.ctypes.data, int(sz.size),
                                            int(lines)), "stage_batch_packed")
+
+    def parse_batch_padded(self, padded, sizes: Sequence[int], lines: bool = False) -> None:
+        """Parse documents laid out by batch_padded_offsets (pinned for the
+        overlap of copy and parse); read results with batch_info / batch_layout."""
+        buf = _u8(padded)
+        sz = np.ascontiguousarray(np.asarray(sizes, dtype=np.uint64))
+        self._batch_n = int(sz.size)
+        _check(lib().cj_parse_batch_padded(self._h, buf.ctypes.data, sz.ctypes.data, int(sz.size), int(lines)),
+               "parse_batch_padded")
 
     def batch_info(self):
         """(status int32[n], n_structural int64[n], max_depth int32[n], offsets int64[n+1])."""
@@ -703,6 +716,16 @@ def synth_lines(seed: int, size: int, **kw):
     if n != size:
         raise ValueError("synth_lines failed")
     return out, int(nrec.value)
+
+
+def batch_padded_offsets(sizes: Sequence[int]):
+    """(offsets uint64[n], total bytes): the 1 KiB-aligned layout of a batch."""
+    sz = np.ascontiguousarray(np.asarray(sizes, dtype=np.uint64))
+    off = np.zeros(max(1, sz.size), np.uint64)
+    tot = ctypes.c_size_t()
+    _check(lib().cj_batch_padded_offsets(sz.ctypes.data, sz.size, off.ctypes.data, ctypes.byref(tot)),
+           "batch_padded_offsets")
+    return off[:sz.size], int(tot.value)
 
 
 def synth_events(seed: int, size: int):

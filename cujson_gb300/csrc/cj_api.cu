@@ -657,7 +657,7 @@ cj_status reserve_batch(cj_context* ctx, uint64_t in_bytes, uint64_t out_cap, ui
 
 // `docs` (one host pointer per document) or `packed` (documents back to back)
 cj_status stage_batch(cj_context* ctx, const uint8_t* const* docs, const uint8_t* packed,
-                      const size_t* sizes, size_t n, bool lines)
+                      const size_t* sizes, size_t n, bool lines, bool tables_only = false)
 {
     // a captured graph stays valid for a new batch of the same document sizes
     // in the same buffers
@@ -667,7 +667,7 @@ cj_status stage_batch(cj_context* ctx, const uint8_t* const* docs, const uint8_t
     const uint64_t gen0 = ctx->arena_gen;
     ctx->staged = false;
     ctx->graph_valid = false;
-    if (!sizes || n == 0 || n > 0xFFFFFFFEu || (!docs && !packed)) return CJ_ERR_INVALID_ARGUMENT;
+    if (!sizes || n == 0 || n > 0xFFFFFFFEu || (!docs && !packed && !tables_only)) return CJ_ERR_INVALID_ARGUMENT;
     uint64_t in_bytes = 0, out_cap = 0, brk_cap = 0, tiles = 0, layout_cap = 0, total = 0;
     for (size_t i = 0; i < n; i++) {
         if (sizes[i] == 0 || (docs && !docs[i])) return CJ_ERR_INVALID_ARGUMENT;
@@ -682,7 +682,7 @@ cj_status stage_batch(cj_context* ctx, const uint8_t* const* docs, const uint8_t
     if (tiles >= 0xFFFFFFFFull) return CJ_ERR_TOO_LARGE;
     CJ_CUDA(cudaSetDevice(ctx->device));
     cj_status st = reserve_batch(ctx, in_bytes, out_cap, brk_cap, tiles + 1, n, layout_cap,
-                                 packed ? total : 0);
+                                 (packed && !tables_only) ? total : 0);
     if (st) return st;
 
     ctx->h_segs.resize(n);
@@ -706,7 +706,9 @@ cj_status stage_batch(cj_context* ctx, const uint8_t* const* docs, const uint8_t
         brk_base += round_up(sizes[i], kChunk);
         tile += g.n_tiles;
     }
-    if (packed) {
+    if (tables_only) {
+        // the caller copies the data (cj_parse_batch_padded)
+    } else if (packed) {
         // one copy of the packed documents, then a kernel moves each one to
         // its aligned place
         ctx->h_pack_off.assign(2 * (n + 1), 0);
@@ -731,7 +733,7 @@ cj_status stage_batch(cj_context* ctx, const uint8_t* const* docs, const uint8_t
                             ctx->stream));
     CJ_CUDA(cudaMemcpyAsync(ctx->tile_seg.p, ctx->h_tile_seg.data(), tiles * sizeof(uint32_t),
                             cudaMemcpyHostToDevice, ctx->stream));
-    if (packed) {
+    if (packed && !tables_only) {
         launch_batch_scatter(ctx->pack.p, ctx->pack_off.p, ctx->pack_off.p + n + 1, ctx->segs.p, (uint32_t)n,
                              ctx->h_pack_off[2 * n + 1], ctx->in.p, ctx->sm_count, ctx->stream);
         ctx->launches += 1;
@@ -745,8 +747,43 @@ cj_status stage_batch(cj_context* ctx, const uint8_t* const* docs, const uint8_t
     ctx->lines = lines;
     ctx->batch = true;
     ctx->batch_read = false;
-    ctx->graph_valid = same && ctx->arena_gen == gen0;
+    ctx->graph_valid = same && ctx->arena_gen == gen0 && !tables_only;
     ctx->staged = true;
+    return CJ_OK;
+}
+
+// A batch whose host buffer already has the device layout (every document at
+// its 1 KiB-aligned offset, cj_batch_padded_offsets): the run starts at once
+// and the copy follows on the copy stream in chunks; the scan hands out a tile
+// once the bytes counter covers it (as in stage_overlapped).  Without the
+// driver's stream write the copy simply precedes the run.
+cj_status parse_batch_padded(cj_context* ctx, const uint8_t* padded, const size_t* sizes, size_t n, bool lines)
+{
+    if (!padded) return CJ_ERR_INVALID_ARGUMENT;
+    cj_status st = stage_batch(ctx, nullptr, nullptr, sizes, n, lines, true);
+    if (st) return st;
+    const Segment& last = ctx->h_segs[n - 1];
+    const uint64_t bytes = last.dev_off + round_up(last.len, kPadBytes);
+    if (!ctx->write64) {
+        CJ_CUDA(cudaMemcpyAsync(ctx->in.p, padded, bytes, cudaMemcpyHostToDevice, ctx->stream));
+        return run(ctx);
+    }
+    CJ_CUDA(cudaMemsetAsync(ctx->d_ready, 0, sizeof(unsigned long long), ctx->stream));
+    CJ_CUDA(cudaEventRecord(ctx->ev_reset, ctx->stream));
+    ctx->overlap_run = true;
+    st = enqueue(ctx, false);
+    ctx->overlap_run = false;
+    if (st) return st;
+    CJ_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_reset, 0));
+    for (uint64_t o = 0; o < bytes; o += kOverlapChunk) {
+        const uint64_t c = std::min<uint64_t>(kOverlapChunk, bytes - o);
+        CJ_CUDA(cudaMemcpyAsync(ctx->in.p + o, padded + o, c, cudaMemcpyHostToDevice, ctx->copy_stream));
+        if (ctx->write64((CUstream)ctx->copy_stream, (CUdeviceptr)ctx->d_ready, o + c,
+                         CU_STREAM_WRITE_VALUE_DEFAULT) != CUDA_SUCCESS)
+            return CJ_ERR_CUDA;
+    }
+    CJ_CUDA(cudaEventRecord(ctx->ev_copied, ctx->copy_stream));
+    CJ_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_copied, 0));
     return CJ_OK;
 }
 
@@ -1043,6 +1080,25 @@ cj_status cj_stage_batch_packed(cj_context* ctx, const uint8_t* packed, const si
 {
     if (!ctx || !packed) return finish(CJ_ERR_INVALID_ARGUMENT);
     return finish(stage_batch(ctx, nullptr, packed, sizes, n_docs, lines_mode != 0));
+}
+
+cj_status cj_batch_padded_offsets(const size_t* sizes, size_t n_docs, size_t* offsets, size_t* total)
+{
+    if (!sizes || !total || (n_docs && !offsets)) return CJ_ERR_INVALID_ARGUMENT;
+    size_t o = 0;
+    for (size_t i = 0; i < n_docs; i++) {
+        offsets[i] = o;
+        o += round_up(sizes[i], kPadBytes);
+    }
+    *total = o;
+    return CJ_OK;
+}
+
+cj_status cj_parse_batch_padded(cj_context* ctx, const uint8_t* padded, const size_t* sizes, size_t n_docs,
+                                int lines_mode)
+{
+    if (!ctx) return finish(CJ_ERR_INVALID_ARGUMENT);
+    return finish(parse_batch_padded(ctx, padded, sizes, n_docs, lines_mode != 0));
 }
 
 cj_status cj_batch_info(cj_context* ctx, int32_t* status, int64_t* n_structural, int32_t* max_depth,

@@ -220,6 +220,15 @@ cj_status cj_stage_batch(cj_context* ctx, const uint8_t* const* docs, const size
                          size_t n_docs, int lines_mode);
 cj_status cj_stage_batch_packed(cj_context* ctx, const uint8_t* packed, const size_t* sizes,
                                 size_t n_docs, int lines_mode);
+/* A batch whose host buffer already has the device layout: document i at
+ * offsets[i] from cj_batch_padded_offsets (1 KiB-aligned, back to back),
+ * `*total` bytes in all.  cj_parse_batch_padded launches the run at once and
+ * copies the buffer (pinned for the overlap) in chunks behind it: the scan
+ * takes a tile as soon as its bytes have arrived, so copy and parse overlap.
+ * Results as after cj_run_staged (cj_batch_info, cj_copy_batch_result). */
+cj_status cj_batch_padded_offsets(const size_t* sizes, size_t n_docs, size_t* offsets, size_t* total);
+cj_status cj_parse_batch_padded(cj_context* ctx, const uint8_t* padded, const size_t* sizes, size_t n_docs,
+                                int lines_mode);
 cj_status cj_batch_info(cj_context* ctx, int32_t* status, int64_t* n_structural, int32_t* max_depth,
                         int64_t* layout_offsets, size_t n_docs);
 cj_status cj_copy_batch_result(cj_context* ctx, int32_t* host_out, size_t out_cap);

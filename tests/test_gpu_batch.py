@@ -103,3 +103,50 @@ def test_single_document_after_batch(cj, oracle, ctx):
     ctx.stage_standard(d)
     ctx.run_graph()
     np.testing.assert_array_equal(ctx.staged_result().buffer, res.buffer)
+
+
+def padded_copy(cj, docs_or_packed, sizes, pinned=True):
+    """The documents laid out at batch_padded_offsets (a pinned buffer)."""
+    off, total = cj.batch_padded_offsets(sizes)
+    buf = cj.PinnedBuffer(max(total, 1)) if pinned else None
+    arr = buf.array if pinned else np.zeros(max(total, 1), np.uint8)
+    src = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    for i in range(len(sizes)):
+        d = docs_or_packed[i] if isinstance(docs_or_packed, list) else docs_or_packed[src[i]:src[i + 1]]
+        arr[int(off[i]):int(off[i]) + d.size] = d
+    return buf, arr
+
+
+def test_padded_batch_overlapped(cj, oracle, ctx):
+    """A batch already in the device layout, copied in chunks while the scan
+    runs: every document's result and verdict as the oracle's, and the same
+    as the packed path's."""
+    docs = mixed_docs(cj, seed=10)
+    sizes = [d.size for d in docs]
+    buf, arr = padded_copy(cj, docs, sizes)
+    ctx.parse_batch_padded(arr, sizes)
+    check_batch(cj, oracle, docs, ctx.batch_results())
+    first = ctx.batch_layout()[0].copy()
+    ctx.stage_batch_packed(np.concatenate(docs), sizes)
+    ctx.run()
+    np.testing.assert_array_equal(ctx.batch_layout()[0], first)
+    buf.close()
+
+
+def test_padded_batch_full_size(cj, ctx):
+    """Config 4 (4096 documents, 2 GiB, 1 % invalid UTF-8, 1 % bad brackets)
+    through the overlapped padded path: identical to the packed graph path."""
+    packed, sizes, kinds = cj.batch_input(cj.CONFIG_SEED_BASE + 4, 4096, 2 << 30)
+    ctx.stage_batch_packed(packed, sizes)
+    ctx.run_graph()
+    want, wst, wS, wd, woff = ctx.batch_layout()
+    want = want.copy()
+    buf, arr = padded_copy(cj, packed, sizes)
+    ctx.parse_batch_padded(arr, sizes)
+    got, st, S, d, off = ctx.batch_layout()
+    np.testing.assert_array_equal(st, wst)
+    np.testing.assert_array_equal(S, wS)
+    np.testing.assert_array_equal(off, woff)
+    np.testing.assert_array_equal(got[:int(off[-1])], want[:int(woff[-1])])
+    assert int((st != cj.OK).sum()) == int((kinds > 0).sum())
+    buf.close()
