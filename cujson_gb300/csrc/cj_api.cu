@@ -305,7 +305,6 @@ cj_status enqueue(cj_context* ctx, bool graph)
     }
 
     ScanParams sp{};
-    sp.one = 1;
     sp.in = ctx->in.p;
     sp.segs = ctx->segs.p;
     sp.tile_seg = (ctx->n_segs > 1) ? ctx->tile_seg.p : nullptr;

@@ -21,12 +21,13 @@ namespace cj {
 // by itself; a tile is the kWarps regions of one CTA, and the cross-tile carry
 // (decoupled look-back) runs once per tile.
 constexpr int kWarps = 16;                                // classifying warps per CTA
-constexpr int kThreads = (kWarps + 1) * 32;               // + one coordinator warp
+constexpr int kCoords = 2;                                // coordinator warps (alternate tiles)
+constexpr int kThreads = (kWarps + kCoords) * 32;
 constexpr int kBytesPerThread = 32;
 constexpr int kStepBytes = 32 * kBytesPerThread;          // 1 KiB, one TMA copy
-constexpr int kStepsPerWarp = 8;
-constexpr int kWarpBytes = kStepBytes * kStepsPerWarp;    // 8 KiB per warp region
-constexpr int kTileBytes = kWarpBytes * kWarps;           // 128 KiB per tile
+constexpr int kStepsPerWarp = 7;
+constexpr int kWarpBytes = kStepBytes * kStepsPerWarp;    // 7 KiB per warp region
+constexpr int kTileBytes = kWarpBytes * kWarps;           // 112 KiB per tile
 constexpr int kPadBytes = kStepBytes;                     // segment padding granule
 
 // Pairing: one warp matches a chunk of this many bracket records.
@@ -140,90 +141,92 @@ CJ_HD uint32_t eq_bytes(uint32_t w, uint32_t pat) {
     return ~(((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x) & 0x80808080u;
 }
 
-// bits 7/15/23/31 of m -> bits 0..3 (multiplication gathers them into the top
-// nibble without carries because the partial products never overlap)
-CJ_HD uint32_t gather4(uint32_t m) { return (m * 0x00204081u) >> 28; }
-
-// a * b + c on the multiply-add pipe (keeps the integer ALU pipe, which bounds
-// the classification, free for the logic operations)
-CJ_HD uint32_t mad_u32(uint32_t a, uint32_t b, uint32_t c) {
+// byte selection of the 8 bytes {x, y} (x = bytes 0-3): result byte i is the
+// byte numbered by nibble i of s (0-7)
+CJ_HD uint32_t byte_perm(uint32_t x, uint32_t y, uint32_t s) {
 #ifdef __CUDA_ARCH__
-    uint32_t d;
-    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
-    return d;
+    return __byte_perm(x, y, s);
 #else
-    return a * b + c;
+    const uint64_t v = ((uint64_t)y << 32) | x;
+    uint32_t r = 0;
+    for (int i = 0; i < 4; i++) r |= (uint32_t)((v >> (8 * ((s >> (4 * i)) & 7u))) & 0xFFu) << (8 * i);
+    return r;
 #endif
 }
 
-// (acc << 4) | nibble of m's bits 7/15/23/31: the gathering multiply runs on
-// the multiply-add pipe, one funnel shift on the ALU both extracts the
-// nibble and appends it
-CJ_HD uint32_t gather_step(uint32_t m, uint32_t acc) {
-#ifdef __CUDA_ARCH__
-    return __funnelshift_l(m * 0x00204081u, acc, 4);
-#else
-    return (acc << 4) | ((m * 0x00204081u) >> 28);
-#endif
+// 4x4 byte transpose: afterwards byte i of a, b, c, d is byte 0, 1, 2, 3 of
+// the old i-th word (columns of the rows a, b, c, d)
+CJ_HD void transpose_bytes4(uint32_t& a, uint32_t& b, uint32_t& c, uint32_t& d) {
+    const uint32_t ab_lo = byte_perm(a, b, 0x5140u), ab_hi = byte_perm(a, b, 0x7362u);   // a0 b0 a1 b1 / a2 b2 a3 b3
+    const uint32_t cd_lo = byte_perm(c, d, 0x5140u), cd_hi = byte_perm(c, d, 0x7362u);
+    a = byte_perm(ab_lo, cd_lo, 0x5410u);
+    b = byte_perm(ab_lo, cd_lo, 0x7632u);
+    c = byte_perm(ab_hi, cd_hi, 0x5410u);
+    d = byte_perm(ab_hi, cd_hi, 0x7632u);
+}
+
+// exchange the bits of a at positions p + s with the bits of b at positions p,
+// for every p set in m (a delta swap between two registers)
+CJ_HD void swap_bits(uint32_t& a, uint32_t& b, int s, uint32_t m) {
+    const uint32_t t = ((a >> s) ^ b) & m;
+    b ^= t;
+    a ^= t << s;
+}
+
+// Bit planes of 32 bytes held as 8 little-endian words: afterwards bit j of
+// p[k] is bit k of byte j.  First a byte transpose leaves byte b of word r
+// holding byte 8b + r (r = 0..7), so the bit at position 8b + k of word r is
+// bit k of byte 8b + r; three delta-swap rounds then exchange the three bits
+// of the word number r with the three low bits of the position (k), giving
+// word k, position 8b + r.
+CJ_HD void bit_planes32(const uint32_t w[8], uint32_t p[8]) {
+    uint32_t v0 = w[0], v1 = w[2], v2 = w[4], v3 = w[6];   // bytes 8b + 0..3
+    uint32_t v4 = w[1], v5 = w[3], v6 = w[5], v7 = w[7];   // bytes 8b + 4..7
+    transpose_bytes4(v0, v1, v2, v3);
+    transpose_bytes4(v4, v5, v6, v7);
+    swap_bits(v0, v1, 1, 0x55555555u); swap_bits(v2, v3, 1, 0x55555555u);
+    swap_bits(v4, v5, 1, 0x55555555u); swap_bits(v6, v7, 1, 0x55555555u);
+    swap_bits(v0, v2, 2, 0x33333333u); swap_bits(v1, v3, 2, 0x33333333u);
+    swap_bits(v4, v6, 2, 0x33333333u); swap_bits(v5, v7, 2, 0x33333333u);
+    swap_bits(v0, v4, 4, 0x0F0F0F0Fu); swap_bits(v1, v5, 4, 0x0F0F0F0Fu);
+    swap_bits(v2, v6, 4, 0x0F0F0F0Fu); swap_bits(v3, v7, 4, 0x0F0F0F0Fu);
+    p[0] = v0; p[1] = v1; p[2] = v2; p[3] = v3; p[4] = v4; p[5] = v5; p[6] = v6; p[7] = v7;
 }
 
 struct Classes {
     uint32_t q, bs, st, op, br, cur, hi;
 };
 
-// Character classes of N*4 bytes held as N little-endian words; bit j of each
+// Character classes of 32 bytes held as 8 little-endian words; bit j of each
 // mask is byte j: quote, backslash, structural ({ } [ ] : , and '\n' in
 // JSON-Lines mode), open ({ [), bracket (any of { } [ ]), curly ({ }) and
-// `hi` (the high bits of all bytes, the non-ASCII test).
+// `hi` (bytes >= 0x80, the non-ASCII test).
 //
-// Per byte b (7-bit part b7 = b & 0x7F, no carry between bytes), bit 7 of
-// b7 + (0x80 - t) is [b7 >= t], so [b7 == t] = [b7 >= t] xor [b7 >= t+1]; the
-// threshold additions run on the multiply-add pipe as b7 * one + (0x80 - t)
-// (`one` is 1, passed at run time so the compiler keeps the multiply-add), and
-// one three-input logic operation per class combines two thresholds with the
-// byte's own high bit.  '[' / '{' and ']' / '}' are compared after clearing
-// bit 5 (0x5B and 0x5D), and bit 5 itself tells curly from square.
-template <bool LINES, int N>
-CJ_HD Classes classify_words(const uint32_t* w, uint32_t one) {
-    const uint32_t H = 0x80808080u;
+// Bit-sliced: the bytes are turned into 8 bit planes (bit_planes32) and each
+// class is a boolean function of the planes, 32 bytes per logic operation.
+//   " 0x22 = 0010 0010      \ 0x5C = 0101 1100
+//   , 0x2C = 0010 1100      : 0x3A = 0011 1010      \n 0x0A = 0000 1010
+//   [ 0x5B = 0101 1011      ] 0x5D = 0101 1101      { 0x7B, } 0x7D (bit 5 set)
+// The four brackets are exactly 01x11yz1 with y != z (open: y = 0, z = 1), the
+// comma and the colon exactly 001a1bc0 with b != a and c == a.
+template <bool LINES>
+CJ_HD Classes classify32(const uint32_t w[8]) {
+    uint32_t P[8];
+    bit_planes32(w, P);
+    const uint32_t n7 = ~P[7];
     Classes c;
-    c.q = c.bs = c.st = c.op = c.br = c.cur = c.hi = 0;
-    const uint32_t four = one << 2;
-#pragma unroll
-    for (int k = N - 1; k >= 0; k--) {
-        const uint32_t x = w[k];
-        const uint32_t xl = x & 0x7F7F7F7Fu, yl = x & 0x5F5F5F5Fu, nx = ~x & H;
-        const uint32_t g22 = mad_u32(xl, one, 0x5E5E5E5Eu), g23 = mad_u32(xl, one, 0x5D5D5D5Du);
-        const uint32_t g2C = mad_u32(xl, one, 0x54545454u), g2D = mad_u32(xl, one, 0x53535353u);
-        const uint32_t g3A = mad_u32(xl, one, 0x46464646u), g3B = mad_u32(xl, one, 0x45454545u);
-        const uint32_t g5C = mad_u32(xl, one, 0x24242424u), g5D = mad_u32(xl, one, 0x23232323u);
-        const uint32_t h5B = mad_u32(yl, one, 0x25252525u), h5C = mad_u32(yl, one, 0x24242424u);
-        const uint32_t h5D = mad_u32(yl, one, 0x23232323u), h5E = mad_u32(yl, one, 0x22222222u);
-        const uint32_t q = (g22 ^ g23) & nx;                 // "
-        const uint32_t b = (g5C ^ g5D) & nx;                 // backslash
-        const uint32_t o = (h5B ^ h5C) & nx;                 // [ {
-        const uint32_t br = o | ((h5D ^ h5E) & nx);          // [ { ] }
-        uint32_t s = br | ((g2C ^ g2D) & nx) | ((g3A ^ g3B) & nx);   // , :
-        if (LINES) s |= (mad_u32(xl, one, 0x76767676u) ^ mad_u32(xl, one, 0x75757575u)) & nx;   // '\n'
-        const uint32_t cu = mad_u32(x, four, 0u) & br;       // bit 5 (curly) -> bit 7
-        c.q = gather_step(q, c.q);
-        c.bs = gather_step(b, c.bs);
-        c.st = gather_step(s, c.st);
-        c.op = gather_step(o, c.op);
-        c.br = gather_step(br, c.br);
-        c.cur = gather_step(cu, c.cur);
-        c.hi |= x;
-    }
-    c.hi &= H;
+    c.br = n7 & P[6] & P[4] & P[3] & P[0] & (P[1] ^ P[2]);
+    c.op = c.br & P[1];
+    c.cur = c.br & P[5];
+    const uint32_t u = n7 & ~P[6] & P[5];                                        // 0x20 .. 0x3F
+    c.q = u & P[1] & ~(P[4] | P[3] | P[2] | P[0]);
+    c.bs = n7 & P[6] & ~P[5] & P[4] & P[3] & P[2] & ~(P[1] | P[0]);
+    const uint32_t cc = u & P[3] & ~P[0] & (P[4] ^ P[2]) & ~(P[4] ^ P[1]);     // , :
+    c.st = c.br | cc;
+    if (LINES) c.st |= n7 & P[3] & P[1] & ~(P[6] | P[5] | P[4] | P[2] | P[0]);   // '\n'
+    c.hi = P[7];
     return c;
 }
-
-template <bool LINES>
-CJ_HD Classes classify16(const uint32_t w[4], uint32_t one) { return classify_words<LINES, 4>(w, one); }
-
-// Character classes of 32 bytes held as 8 little-endian words.
-template <bool LINES>
-CJ_HD Classes classify32(const uint32_t w[8], uint32_t one) { return classify_words<LINES, 8>(w, one); }
 
 // carry out of a 32-byte word entered without escape: whether its trailing
 // backslash run has odd length (not meaningful for an all-backslash word)

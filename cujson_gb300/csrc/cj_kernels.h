@@ -25,7 +25,6 @@ struct ScanParams {
     uint32_t epoch;
     uint32_t* seg_err;          // per-segment verdict bits (independent documents),
                                 // nullptr: verdicts go to ctrl->error_flags
-    uint32_t one;               // 1 (a run-time value, see classify_words)
     // Bytes of the input layout (`in`, from its start) already in device
     // memory, raised by the host's copies while the scan runs; a tile is
     // handed out once its bytes are there.  nullptr: all input is present.

@@ -192,7 +192,6 @@ cj_status parse_noalloc(const uint8_t* d_data, size_t size, int32_t* d_out, size
     noalloc_setup<<<1, 32, 0, stream>>>(s, size);
 
     ScanParams sp{};
-    sp.one = 1;
     sp.in = s->in;
     sp.segs = &s->seg;
     sp.tile_seg = nullptr;

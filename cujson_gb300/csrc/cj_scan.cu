@@ -3,14 +3,17 @@
 //
 // A persistent grid of CTAs (one per SM: 16 classifying warps and one
 // coordinator warp) takes 128 KiB tiles in document order from an atomic
-// ticket.  Each classifying warp owns a contiguous 8 KiB region of a tile and
-// works through it in 1 KiB steps (32 lanes x 32 bytes) staged in its own
-// 3-deep shared-memory ring by bulk TMA copies (cp.async.bulk completing on
-// per-warp mbarriers).
+// ticket; the coordinator draws each ticket two tiles ahead and keeps the
+// tile's segment geometry in shared memory.  Each classifying warp owns a
+// contiguous 8 KiB region of a tile and works through it in 1 KiB steps
+// (32 lanes x 32 bytes) staged in its own 3-deep shared-memory ring by bulk
+// TMA copies (cp.async.bulk completing on per-warp mbarriers); the copies of
+// a region's first steps start as soon as the warp's previous phase A ends.
 //
 //   A. (tile t) every classifying warp, on its own: builds the quote, backslash,
-//      structural and bracket bitmaps of each lane's 32 bytes, validates UTF-8
-//      (byte-parallel, only on steps holding non-ASCII bytes), resolves
+//      structural and bracket bitmaps of each lane's 32 bytes (bit-sliced:
+//      8 bit planes, one logic operation per class and 32 bytes), validates
+//      UTF-8 (byte-parallel, only on steps holding non-ASCII bytes), resolves
 //      escapes and the in-string mask assuming its region is entered outside
 //      any string and escape (carries move lane to lane with ballots and
 //      shuffles, step to step in registers), keeps the masks in shared memory
@@ -20,17 +23,16 @@
 //   B. (tile t, coordinator warp, while the classifying warps run phase A of
 //      tile t+1) composes the 16 warp tables into the tile's table, publishes
 //      it (decoupled look-back descriptor), finds the tile's exclusive prefix by
-//      look-back (32 predecessors per step, loaded in parallel and composed
+//      look-back (64 predecessors per round, loaded in parallel and composed
 //      with an ordered shuffle reduction), publishes the inclusive value and
 //      derives each warp's entry value.
 //   C. (tile t, after phase A of tile t+1) every classifying warp replays its
 //      masks with its entry value and writes 1-based structural positions, a
 //      zeroed pair row and one bracket record (structural index, level, open
 //      flag, brace or bracket) per bracket.
-// Hand-offs between the two roles use named barriers (bar.arrive / bar.sync),
-// one pair per mask slot, so a barrier is never re-armed before its previous
-// phase completed; the look-back never stalls the classifying warps unless it
-// takes longer than a whole phase A.
+// Hand-offs between the two roles are mbarriers (tile_ready, a_done,
+// prefix_ready; see Smem) with bounded waits; the look-back never stalls the
+// classifying warps unless it takes longer than a whole phase A.
 //
 // This replaces the reference's stage 1 (checkAscii + checkUTF8,
 // cujson/parse_standard_json.cu:186-327) and stage 2 (bitMapCreatorSimd :446,
@@ -50,8 +52,15 @@ namespace cj {
 namespace {
 
 constexpr int kStages = 3;                // TMA ring depth per warp
-constexpr int kMaskFields = 5;            // st, br, op, cur, M per lane per step
-constexpr uint32_t kSpinLimit = 1u << 20; // look-back polls before giving up
+// Per lane and step, four mask words: open brackets, close brackets, `x`
+// (curly among brackets, and every other structural: , : and '\n') and the
+// structurals that are inside a string when the region is entered outside
+// one.  Structurals = open | close | x; brackets = open | close.
+constexpr int kMaskFields = 4;
+constexpr int kSlots = 3;                 // mask slots: phase C runs two tiles behind phase A
+constexpr uint32_t kSpinLimit = 1u << 16; // look-back polls before giving up
+constexpr uint32_t kLookSleepMin = 64;    // ns between look-back polls, doubling per poll ...
+constexpr uint32_t kLookSleepMax = 1024;  // ... up to this: a waiting look-back costs few issue slots
 constexpr int kLookPerLane = 2;           // predecessors per lane and look-back round
 constexpr uint32_t kWaitLimit = 1u << 20; // mbarrier polls (each suspends <= kPollNs) before giving up
 constexpr uint32_t kPollNs = 1000;
@@ -74,19 +83,36 @@ struct __align__(16) Slot {
     Ent wtab[kWarps][4];       // per-warp transfer tables
     Ent wentry[kWarps];        // per-warp entry values (after the look-back)
     uint32_t we[kWarps];       // per-warp flip, then per-warp in-string inversion
-    uint32_t tile;             // tile index, kNoTile when empty
-    uint32_t resolved;         // prefix known (entries valid)
 };
+
+// A tile as the coordinator hands it out: its ticket and the geometry of its
+// segment, so the classifying warps never wait on global loads for them.
+struct __align__(16) TileInfo {
+    const uint8_t* seg_base;   // the segment's first byte in the device input
+    uint64_t tile_off;         // tile start within the segment
+    uint64_t seg_len;
+    uint64_t seg_log;          // added to byte positions
+    uint64_t out_base;         // output index base of the segment
+    uint64_t brk_base;         // bracket-record base of the segment
+    uint32_t tile;             // kNoTile: no tiles left
+    uint32_t segi;
+    int32_t tile_len;
+    uint32_t flags;            // kTileFirst | kTileLast | kTileImmediate
+};
+constexpr uint32_t kTileFirst = 1u, kTileLast = 2u, kTileImmediate = 4u;
+constexpr int kTickets = 4;    // ticket ring: ticket i lives in info[i % kTickets]
 
 struct __align__(128) Smem {
     WarpSmem w[kWarps];
-    Slot slot[2];
-    // hand-offs per slot, all mbarriers (bounded waits; no warp waits on
-    // another classifying warp):
-    //   tile_ready   coordinator -> classifying warps: slot.tile is set
-    //   a_done       classifying warps (one arrival each) -> coordinator
-    //   prefix_ready coordinator -> classifying warps: entry values are set
-    unsigned long long tile_ready[2], a_done[2], prefix_ready[2];
+    Slot slot[kSlots];
+    TileInfo info[kTickets];
+    // hand-offs, all mbarriers (bounded waits; no warp waits on another
+    // classifying warp).  The i-th tile a CTA takes is ticket i: its info in
+    // info[i % kTickets], its masks in slot[i % kSlots].
+    //   tile_ready[i % kTickets]  coordinator -> classifying warps: info is set
+    //   a_done[i % kSlots]        classifying warps (one arrival each) -> coordinator
+    //   prefix_ready[i % kSlots]  coordinator -> classifying warps: entry values are set
+    unsigned long long tile_ready[kTickets], a_done[kSlots], prefix_ready[kSlots];
 };
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
@@ -191,53 +217,69 @@ __device__ __forceinline__ void mask_chunk(uint4& v, int valid) {
     }
 }
 
-struct TileGeom {
-    const Segment* sp;
-    uint32_t segi;
-    uint64_t tile_off;   // within the segment
-    uint64_t seg_len;
-    int tile_len;
-    bool seg_first, seg_last, immediate;
-    const uint8_t* seg_base;
-};
-
-__device__ __forceinline__ TileGeom tile_geom(const ScanParams& P, uint32_t tile) {
-    TileGeom g;
-    g.segi = P.tile_seg ? __ldg(P.tile_seg + tile) : 0u;
-    g.sp = P.segs + g.segi;
-    const uint32_t first = __ldg(&g.sp->first_tile);
-    const uint32_t ntiles = __ldg(&g.sp->n_tiles);
-    const uint32_t flags = __ldg(&g.sp->flags);
+// the info of ticket `tile` (kNoTile past the last tile)
+__device__ __forceinline__ void tile_info(const ScanParams& P, uint32_t tile, TileInfo& g) {
+    g.tile = tile;
+    if (tile == kNoTile) return;
+    const uint32_t segi = P.tile_seg ? __ldg(P.tile_seg + tile) : 0u;
+    const Segment* sp = P.segs + segi;
+    const uint32_t first = __ldg(&sp->first_tile);
+    const uint32_t ntiles = __ldg(&sp->n_tiles);
+    const uint32_t flags = __ldg(&sp->flags);
     const uint32_t tin = tile - first;
-    g.seg_len = __ldg(&g.sp->len);
-    g.tile_off = (uint64_t)tin * kTileBytes;
-    const uint64_t rem = g.seg_len - g.tile_off;
+    const uint64_t seg_len = __ldg(&sp->len);
+    const uint64_t tile_off = (uint64_t)tin * kTileBytes;
+    const uint64_t rem = seg_len - tile_off;
+    g.segi = segi;
+    g.seg_len = seg_len;
+    g.tile_off = tile_off;
     g.tile_len = rem < (uint64_t)kTileBytes ? (int)rem : kTileBytes;
-    g.seg_first = (tin == 0);
-    g.seg_last = (tin + 1 == ntiles);
-    g.immediate = g.seg_first && !(flags & kSegContinue);
-    g.seg_base = P.in + __ldg(&g.sp->dev_off);
-    return g;
+    g.seg_base = P.in + __ldg(&sp->dev_off);
+    g.seg_log = __ldg(&sp->logical_off);
+    g.out_base = __ldg(&sp->out_base);
+    g.brk_base = __ldg(&sp->brk_base);
+    g.flags = (tin == 0 ? kTileFirst : 0u) | (tin + 1 == ntiles ? kTileLast : 0u) |
+              ((tin == 0 && !(flags & kSegContinue)) ? kTileImmediate : 0u);
+}
+
+// bytes of warp `warp`'s region of a tile, and its 1 KiB steps
+__device__ __forceinline__ int region_len(const TileInfo& g, int warp) {
+    return max(0, min(kWarpBytes, g.tile_len - warp * kWarpBytes));
+}
+
+// Lane 0 of a classifying warp: start the bulk copies of the first steps of
+// its region into the ring (every stage must be free).
+__device__ __forceinline__ void start_region(const TileInfo& g, WarpSmem& W, int warp) {
+    const int nsteps = (region_len(g, warp) + kStepBytes - 1) / kStepBytes;
+    const uint8_t* reg_src = g.seg_base + g.tile_off + (uint64_t)warp * kWarpBytes;
+    fence_proxy_async();
+    for (int j = 0; j < kStages && j < nsteps; j++)
+        tma_load(W.ring[j], reg_src + (size_t)j * kStepBytes, &W.mbar[j]);
+}
+
+// the 4 input bytes before warp `warp`'s region of a tile (0 at a segment start)
+__device__ __forceinline__ uint32_t region_prev_word(const TileInfo& g, int warp) {
+    const uint64_t off = g.tile_off + (uint64_t)warp * kWarpBytes;
+    return (off > 0 && region_len(g, warp) > 0)
+               ? __ldg(reinterpret_cast<const uint32_t*>(g.seg_base + off) - 1) : 0u;
 }
 
 // Phase A of one warp's region: classify, validate, resolve strings, keep masks.
+// The first steps' copies were started by start_region (at the end of the
+// warp's previous phase A, or here when `started_copies` is false);
+// `prev_last` holds region_prev_word.
 template <bool LINES>
-__device__ __forceinline__ void phase_a(const ScanParams& P, const TileGeom& g, WarpSmem& W, Slot& sl,
-                                        uint32_t& parity, int warp, int lane, uint32_t lt)
+__device__ __forceinline__ void phase_a(const ScanParams& P, const TileInfo& g, WarpSmem& W, Slot& sl,
+                                        uint32_t& parity, int warp, int lane, uint32_t lt,
+                                        bool started_copies, uint32_t prev_last)
 {
     const int reg_off = warp * kWarpBytes;
-    const int reg_len = max(0, min(kWarpBytes, g.tile_len - reg_off));
+    const int reg_len = region_len(g, warp);
     const int nsteps = (reg_len + kStepBytes - 1) / kStepBytes;
     const uint8_t* reg_src = g.seg_base + g.tile_off + reg_off;
-    if (lane == 0) {
-        fence_proxy_async();
-        for (int j = 0; j < kStages && j < nsteps; j++)
-            tma_load(W.ring[j], reg_src + (size_t)j * kStepBytes, &W.mbar[j]);
-    }
+    if (lane == 0 && !started_copies) start_region(g, W, warp);
     uint32_t carry = 0, par = 0;           // escape carry / quote parity (warp uniform)
     uint32_t started = 0, wflip = 0;       // first non-all-backslash lane seen / its flip
-    uint32_t prev_last = (g.tile_off + (uint64_t)reg_off > 0 && nsteps > 0)
-                             ? __ldg(reinterpret_cast<const uint32_t*>(reg_src) - 1) : 0u;
     uint32_t n_c0 = 0, n_ct = 0, n_k0 = 0, n_kt = 0, n_o0 = 0, n_ot = 0;   // per lane
     for (int j = 0; j < nsteps; j++) {
         const int st_i = j % kStages;
@@ -262,7 +304,7 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileGeom& g, 
         if (16 > valid) mask_chunk(lo, valid);
         if (32 > valid) mask_chunk(hi, valid - 16);
         const uint32_t w[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
-        const Classes c = classify32<LINES>(w, P.one);
+        const Classes c = classify32<LINES>(w);
 
         // UTF-8, byte-parallel, on steps that hold a non-ASCII byte
         if (__any_sync(FULL, c.hi != 0u) || (prev_last & 0x80808000u)) {
@@ -321,11 +363,10 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileGeom& g, 
         n_k0 += __popc(br & ~M);   n_kt += __popc(br);
         n_o0 += __popc(c.op & ~M); n_ot += __popc(c.op);
         uint32_t (&m)[kMaskFields][32] = sl.masks[warp][j];
-        m[0][lane] = c.st;
-        m[1][lane] = br;
-        m[2][lane] = c.op;
-        m[3][lane] = c.cur;
-        m[4][lane] = M;
+        m[0][lane] = c.op;
+        m[1][lane] = br & ~c.op;
+        m[2][lane] = c.cur | (c.st & ~br);
+        m[3][lane] = c.st & M;
     }
     // the warp's transfer table, relative to the state it is entered in
     const int32_t C0 = (int32_t)__reduce_add_sync(FULL, n_c0), Ct = (int32_t)__reduce_add_sync(FULL, n_ct);
@@ -366,15 +407,15 @@ __device__ __forceinline__ Ent shfl_up_ent(Ent e, int o) {
 // Coordinator, whole warp: given the slot's exclusive prefix `excl` and its
 // table T, publish the inclusive value (lane 0) and set every classifying
 // warp's entry value, lane w for warp w from its exclusive prefix table pre.
-__device__ __forceinline__ void finish_prefix(const ScanParams& P, const TileGeom& g, Slot& sl, Ent excl,
+__device__ __forceinline__ void finish_prefix(const ScanParams& P, const TileInfo& g, Slot& sl, Ent excl,
                                               const Ent T[4], const Ent pre[4], uint32_t ep, int lane)
 {
     const Ent incl = ent_apply(excl, T);
     if (lane == 0) {
         // the release store orders the descriptor before the flag
-        __stcg(P.desc_incl + sl.tile, make_uint4(incl.st, incl.s, incl.k, (uint32_t)incl.d));
-        st_release(P.desc_flag + sl.tile, (ep << 2) | kFlagIncl);
-        if (g.seg_last) {
+        __stcg(P.desc_incl + g.tile, make_uint4(incl.st, incl.s, incl.k, (uint32_t)incl.d));
+        st_release(P.desc_flag + g.tile, (ep << 2) | kFlagIncl);
+        if (g.flags & kTileLast) {
             SegmentOut so;
             so.s_end = incl.s;
             so.k_end = incl.k;
@@ -386,14 +427,13 @@ __device__ __forceinline__ void finish_prefix(const ScanParams& P, const TileGeo
                 else atomicOr(&P.ctrl->error_flags, CJ_FLAG_BRACKETS);
             }
         }
-        if (sl.tile + 1 == P.n_tiles) {
+        if (g.tile + 1 == P.n_tiles) {
             P.ctrl->s_total = incl.s;
             P.ctrl->k_total = incl.k;
         }
-        sl.resolved = 1;
     }
     Ent v = excl;
-    if (g.seg_first) { v.st = 0; v.d = 0; }
+    if (g.flags & kTileFirst) { v.st = 0; v.d = 0; }
     if (lane < kWarps) {
         const Ent e = ent_apply(v, pre);
         const uint32_t es = e.st & 3u;
@@ -415,7 +455,7 @@ __device__ __forceinline__ Ent look_back(const ScanParams& P, uint32_t tile, uin
     Ent acc[4];
     tab_identity(acc);
     int64_t pred_hi = (int64_t)tile - 1;
-    uint32_t spins = 0;
+    uint32_t spins = 0, sleep_ns = kLookSleepMin;
     while (true) {
         uint32_t st_bits = 0;           // 2 bits per index: status
 #pragma unroll
@@ -445,7 +485,10 @@ __device__ __forceinline__ Ent look_back(const ScanParams& P, uint32_t tile, uin
                 if (lane == 0) give_up(P.ctrl, kGaveLookBack);
                 return ent_identity(0);
             }
-            __nanosleep(32);
+            // the look-back has a whole phase A of slack before its entry
+            // values are needed, so it backs off rather than polling hard
+            __nanosleep(sleep_ns);
+            sleep_ns = min(2u * sleep_ns, kLookSleepMax);
             continue;
         }
         // this lane's tables, farthest first, and the inclusive value
@@ -492,15 +535,15 @@ __device__ __forceinline__ Ent look_back(const ScanParams& P, uint32_t tile, uin
 }
 
 // Phase C of one warp's region.
-__device__ __forceinline__ void phase_c(const ScanParams& P, const TileGeom& g, const Slot& sl,
+__device__ __forceinline__ void phase_c(const ScanParams& P, const TileInfo& g, const Slot& sl,
                                         int warp, int lane)
 {
     const int reg_off = warp * kWarpBytes;
-    const int reg_len = max(0, min(kWarpBytes, g.tile_len - reg_off));
+    const int reg_len = region_len(g, warp);
     const int nsteps = (reg_len + kStepBytes - 1) / kStepBytes;
-    const uint64_t seg_log = __ldg(&g.sp->logical_off);
-    const uint64_t seg_outb = __ldg(&g.sp->out_base);
-    const uint64_t seg_brkb = __ldg(&g.sp->brk_base);
+    const uint64_t seg_log = g.seg_log;
+    const uint64_t seg_outb = g.out_base;
+    const uint64_t seg_brkb = g.brk_base;
     const Ent entry = sl.wentry[warp];
     const uint32_t flip = sl.we[warp] ? FULL : 0u;
     uint32_t s_base = entry.s, k_base = entry.k;
@@ -511,12 +554,12 @@ __device__ __forceinline__ void phase_c(const ScanParams& P, const TileGeom& g, 
     const uint64_t pos_base = seg_log + g.tile_off + (uint64_t)reg_off + (uint64_t)lane * kBytesPerThread + 1u;
     for (int j = 0; j < nsteps; j++) {
         const uint32_t (&m)[kMaskFields][32] = sl.masks[warp][j];
-        const uint32_t Mf = m[4][lane] ^ flip;
-        uint32_t stm = m[0][lane] & ~Mf;
+        const uint32_t opw = m[0][lane], brw = opw | m[1][lane], xw = m[2][lane];
+        uint32_t stm = (brw | xw) & ~(m[3][lane] ^ flip);
         if (!__any_sync(FULL, stm)) continue;      // nothing outside strings in this step
-        const uint32_t brm = m[1][lane] & ~Mf;
-        const uint32_t opm = m[2][lane] & ~Mf;
-        const uint32_t curm = m[3][lane];
+        const uint32_t brm = brw & stm;
+        const uint32_t opm = opw & stm;
+        const uint32_t curm = xw & brw;
         // the three counts (each <= 32 per lane) packed in 10-bit fields: one
         // scan; exclusive prefixes stay <= 31 * 32 < 1024 per field
         const uint32_t own = (uint32_t)__popc(stm) | ((uint32_t)__popc(brm) << 10) |
@@ -561,28 +604,26 @@ __device__ __forceinline__ void phase_c(const ScanParams& P, const TileGeom& g, 
 
 size_t scan_smem_bytes() { return sizeof(Smem); }
 
-// Coordinator lane 0: the next tile from the ticket counter, once its input
-// bytes are in device memory (bounded wait; the timeout flag on expiry).
-__device__ __forceinline__ uint32_t next_tile(const ScanParams& P)
+// Coordinator lane 0: the next tile from the ticket counter and its info,
+// once its input bytes are in device memory (bounded wait; the timeout flag
+// on expiry).
+__device__ __forceinline__ void draw_tile(const ScanParams& P, TileInfo& g)
 {
     const uint32_t t = atomicAdd(&P.ctrl->tile_ticket, 1u);
-    if (t >= P.n_tiles) return kNoTile;
-    if (P.ready) {
-        const TileGeom g = tile_geom(P, t);
-        const uint64_t padded = (g.seg_len + kPadBytes - 1) / kPadBytes * kPadBytes;
-        const uint64_t end = g.tile_off + (uint64_t)kTileBytes;
-        const uint64_t need = (uint64_t)(g.seg_base - P.in) + (end < padded ? end : padded);
-        const uint32_t limit = P.input_wait_limit ? P.input_wait_limit : kInputWaitLimit;
-        uint32_t spins = 0;
-        while (ld_acquire64(P.ready) < need) {
-            if (++spins > limit || ((spins & 255u) == 0u && aborted(P.ctrl))) {
-                give_up(P.ctrl, kGaveInput);
-                break;
-            }
-            __nanosleep(256);
+    tile_info(P, t < P.n_tiles ? t : kNoTile, g);
+    if (g.tile == kNoTile || !P.ready) return;
+    const uint64_t padded = (g.seg_len + kPadBytes - 1) / kPadBytes * kPadBytes;
+    const uint64_t end = g.tile_off + (uint64_t)kTileBytes;
+    const uint64_t need = (uint64_t)(g.seg_base - P.in) + (end < padded ? end : padded);
+    const uint32_t limit = P.input_wait_limit ? P.input_wait_limit : kInputWaitLimit;
+    uint32_t spins = 0;
+    while (ld_acquire64(P.ready) < need) {
+        if (++spins > limit || ((spins & 255u) == 0u && aborted(P.ctrl))) {
+            give_up(P.ctrl, kGaveInput);
+            break;
         }
+        __nanosleep(256);
     }
-    return t;
 }
 
 template <bool LINES>
@@ -598,40 +639,59 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
         fence_mbar_init();
     }
     if (warp == kWarps && lane == 0) {
-        for (int s = 0; s < 2; s++) {
-            mbar_init(&S.tile_ready[s], 1);
+        for (int k = 0; k < kTickets; k++) mbar_init(&S.tile_ready[k], 1);
+        for (int s = 0; s < kSlots; s++) {
             mbar_init(&S.a_done[s], kWarps);
             mbar_init(&S.prefix_ready[s], 1);
-            S.slot[s].tile = kNoTile;
         }
         fence_mbar_init();
     }
     __syncthreads();
 
-    if (warp == kWarps) {
-        // ---- coordinator: hand out tiles, publish, look back, derive entries ---------
-        if (lane == 0) {
-            S.slot[0].tile = next_tile(P);
+    if (warp >= kWarps) {
+        // ---- coordinators: hand out tiles, publish, look back, derive entries --------
+        // Coordinator c resolves tickets c, c + kCoords, ...: a tile's
+        // look-back and composition may take kCoords phase A's without
+        // holding up the tiles after it.  Ticket i + 1 is drawn by ticket i's
+        // coordinator as soon as every warp has finished phase A of ticket i,
+        // so tiles are taken in the order their phase A begins and a
+        // look-back rarely waits on a predecessor that has not started.
+        const uint32_t c = (uint32_t)(warp - kWarps);
+        if (c == 0 && lane == 0) {
+            draw_tile(P, S.info[0]);
             mbar_arrive(&S.tile_ready[0]);
         }
         __syncwarp();
-        uint32_t use = 0;          // bit s: phase parity of slot s's a_done
-        int s = 0;
-        while (true) {
-            Slot& sl = S.slot[s];
-            const uint32_t tile = sl.tile;
-            if (tile == kNoTile) break;
-            if (!mbar_wait(&S.a_done[s], (use >> s) & 1u, P.ctrl) && lane == 0) give_up(P.ctrl, kGaveADone);
-            use ^= 1u << s;
-            // the warps go on to phase C of the other slot's tile and then
-            // start that slot's next one: hand it out now, just in time, so
-            // that tiles are taken in the order their phase A begins and a
-            // look-back rarely waits on a predecessor that has not started
-            if (lane == 0) {
-                S.slot[s ^ 1].tile = next_tile(P);
-                mbar_arrive(&S.tile_ready[s ^ 1]);
+        for (uint32_t i = c;; i += kCoords) {
+            // ticket i exists only if ticket i - 1 was a tile (it is drawn
+            // after that tile's phase A).  info[(i - 1) % kTickets] is next
+            // written by this coordinator (ticket i + 3, drawn after tile
+            // i + 2), info[i % kTickets] only after phase A of ticket i + 3,
+            // which follows phase C of ticket i.
+            if (i >= 1) {
+                if (!__shfl_sync(FULL, mbar_wait(&S.tile_ready[(i - 1) % kTickets], ((i - 1) / kTickets) & 1u,
+                                                 P.ctrl), 0)) {
+                    if (lane == 0) give_up(P.ctrl, kGaveTileReady);
+                    break;
+                }
+                if (S.info[(i - 1) % kTickets].tile == kNoTile) break;
             }
-            const TileGeom g = tile_geom(P, tile);
+            if (!__shfl_sync(FULL, mbar_wait(&S.tile_ready[i % kTickets], (i / kTickets) & 1u, P.ctrl), 0)) {
+                if (lane == 0) give_up(P.ctrl, kGaveTileReady);
+                break;
+            }
+            const TileInfo& g = S.info[i % kTickets];
+            const uint32_t tile = g.tile;
+            if (tile == kNoTile) break;
+            const uint32_t s = i % kSlots;
+            Slot& sl = S.slot[s];
+            if (!mbar_wait(&S.a_done[s], (i / kSlots) & 1u, P.ctrl) && lane == 0) give_up(P.ctrl, kGaveADone);
+            if (lane == 0) {
+                // info[(i + 1) % kTickets] last held ticket i + 1 - kTickets,
+                // whose phase C ended before any warp's phase A of ticket i began
+                draw_tile(P, S.info[(i + 1) % kTickets]);
+                mbar_arrive(&S.tile_ready[(i + 1) % kTickets]);
+            }
             // inclusive scan of the 16 warp tables over lanes 0..15, then the
             // tile's table (lane 15) and each warp's exclusive prefix table
             Ent t[4];
@@ -655,14 +715,14 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
                 pre[k] = shfl_up_ent(t[k], 1);
             }
             if (lane == 0) tab_identity(pre);
-            if (g.seg_first) {
+            if (g.flags & kTileFirst) {
                 // a segment starts outside strings and escapes, at depth 0
                 const Ent t0 = T[0];
 #pragma unroll
                 for (int k = 0; k < 4; k++) { T[k] = t0; T[k].st |= 4u; }
             }
             Ent excl = ent_identity(0);
-            if (!g.immediate) {
+            if (!(g.flags & kTileImmediate)) {
                 if (lane == 0) {
 #pragma unroll
                     for (int k = 0; k < 4; k++)
@@ -676,49 +736,44 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
             __syncwarp();
             if (lane == 0) mbar_arrive(&S.prefix_ready[s]);
             __syncwarp();
-            s ^= 1;
         }
         return;
     }
 
     // ---- classifying warps -----------------------------------------------------------
+    // Ticket i: phase A into slot i % kSlots, then phase C of ticket i - 2, so
+    // a tile's look-back has two phase A's of slack before its entry values
+    // are needed.
     WarpSmem& W = S.w[warp];
     const uint32_t lt = lanemask_lt();
-    // phase parities to wait for: bits 0..kStages-1 the ring stages, then two
-    // bits for the slots' tile_ready and two for their prefix_ready
-    constexpr int kTB = kStages, kPB = kStages + 2;
-    uint32_t parity = 0;
-    int s = 0;
-    uint32_t prev_tile = kNoTile;
-    while (true) {
+    uint32_t parity = 0;          // bit j: phase parity of ring stage j
+    for (uint32_t i = 0;; i++) {
         // a wait that expired (lane 0 decides for the warp) ends the warp's
-        // work: the slot's contents are then not trusted
+        // work: the ticket is then not trusted
         const bool got_tile =
-            __shfl_sync(FULL, mbar_wait(&S.tile_ready[s], (parity >> (kTB + s)) & 1u, P.ctrl), 0);
+            __shfl_sync(FULL, mbar_wait(&S.tile_ready[i % kTickets], (i / kTickets) & 1u, P.ctrl), 0);
         if (!got_tile && lane == 0) give_up(P.ctrl, kGaveTileReady);
-        parity ^= 1u << (kTB + s);
-        const uint32_t tile = got_tile ? S.slot[s].tile : kNoTile;
+        const uint32_t tile = got_tile ? S.info[i % kTickets].tile : kNoTile;
         if (tile != kNoTile) {
-            const TileGeom g = tile_geom(P, tile);
-            phase_a<LINES>(P, g, W, S.slot[s], parity, warp, lane, lt);
+            const TileInfo& g = S.info[i % kTickets];
+            phase_a<LINES>(P, g, W, S.slot[i % kSlots], parity, warp, lane, lt, false, region_prev_word(g, warp));
             __syncwarp();
-            if (lane == 0) mbar_arrive(&S.a_done[s]);
+            if (lane == 0) mbar_arrive(&S.a_done[i % kSlots]);
         }
-        if (prev_tile != kNoTile) {
-            const int q = s ^ 1;
+        // phase C of ticket i - 2, and after the last ticket also of i - 1
+        const uint32_t c_lo = i >= 2 ? i - 2 : 0u;
+        const uint32_t c_hi = (tile == kNoTile) ? i : (i >= 2 ? i - 1 : 0u);
+        for (uint32_t k = c_lo; k < c_hi; k++) {
+            const uint32_t q = k % kSlots;
             const bool got_prefix =
-                __shfl_sync(FULL, mbar_wait(&S.prefix_ready[q], (parity >> (kPB + q)) & 1u, P.ctrl), 0);
-            parity ^= 1u << (kPB + q);
+                __shfl_sync(FULL, mbar_wait(&S.prefix_ready[q], (k / kSlots) & 1u, P.ctrl), 0);
             if (got_prefix) {
-                const TileGeom g = tile_geom(P, prev_tile);
-                phase_c(P, g, S.slot[q], warp, lane);
+                phase_c(P, S.info[k % kTickets], S.slot[q], warp, lane);
             } else if (lane == 0) {
                 give_up(P.ctrl, kGavePrefixReady);   // no entry value: no writes
             }
         }
         if (tile == kNoTile) break;
-        prev_tile = tile;
-        s ^= 1;
     }
 }
 

@@ -33,6 +33,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "cj_device.cuh"
 #include "cujson_gb300.h"
 
 namespace {
@@ -48,7 +49,7 @@ uint64_t doc_device_bytes(size_t size)
     const uint64_t b = size;
     const uint64_t chunked = (b + 511) / 512 * 512 + 512;
     const uint64_t raw = (b + 1024) + 8 * (b + 1) + 8 * chunked + 4 * chunked + 4 * (2 * b + 4) +
-                         84 * (b / 131072 + 1) + 64;
+                         84 * (b / cj::kTileBytes + 1) + 64;
     return raw + raw / 8;
 }
 

@@ -108,7 +108,7 @@ extern "C" int cjm_parse(const uint8_t* data, size_t n, int lines, const size_t*
                     }
                     w[k] = v;
                 }
-                c[t] = lines ? classify32<true>(w, 1u) : classify32<false>(w, 1u);
+                c[t] = lines ? classify32<true>(w) : classify32<false>(w);
                 {
                     // previous 4 bytes of the segment (zero before its start)
                     uint32_t pw = 0;
@@ -312,4 +312,51 @@ extern "C" int cjm_parse(const uint8_t* data, size_t n, int lines, const size_t*
     *out_flags = flags;
     for (size_t i = 0; i < pos.size() && i < cap; i++) { out_pos[i] = pos[i]; out_pair[i] = pair[i]; }
     return 0;
+}
+
+// Character classes of the kernels' bit-sliced classifier (classify32) against
+// their byte-by-byte definition: every byte value at every one of the 32
+// positions (the other bytes random), then `n_random` random 32-byte blocks.
+// Returns the number of mismatching blocks.
+extern "C" int cjm_classify_check(uint64_t seed, int n_random)
+{
+    std::mt19937_64 rng(seed);
+    int bad = 0;
+    auto one = [&](const uint8_t* b, bool lines) {
+        uint32_t w[8];
+        for (int k = 0; k < 8; k++)
+            w[k] = (uint32_t)b[4 * k] | ((uint32_t)b[4 * k + 1] << 8) | ((uint32_t)b[4 * k + 2] << 16) |
+                   ((uint32_t)b[4 * k + 3] << 24);
+        const Classes c = lines ? classify32<true>(w) : classify32<false>(w);
+        uint32_t q = 0, bs = 0, st = 0, op = 0, br = 0, cur = 0, hi = 0;
+        for (int j = 0; j < 32; j++) {
+            const uint8_t x = b[j];
+            const uint32_t bit = 1u << j;
+            if (x == '"') q |= bit;
+            if (x == '\\') bs |= bit;
+            if (x == '{' || x == '}' || x == '[' || x == ']' || x == ':' || x == ',' || (lines && x == '\n'))
+                st |= bit;
+            if (x == '{' || x == '[') op |= bit;
+            if (x == '{' || x == '}' || x == '[' || x == ']') br |= bit;
+            if (x == '{' || x == '}') cur |= bit;
+            if (x >= 0x80) hi |= bit;
+        }
+        if (c.q != q || c.bs != bs || c.st != st || c.op != op || c.br != br || c.cur != cur || c.hi != hi) bad++;
+    };
+    uint8_t b[32];
+    for (int lines = 0; lines < 2; lines++) {
+        for (int j = 0; j < 32; j++)
+            for (int v = 0; v < 256; v++) {
+                for (int k = 0; k < 32; k++) b[k] = (uint8_t)rng();
+                b[j] = (uint8_t)v;
+                one(b, lines != 0);
+            }
+        const char alphabet[] = "\"\\{}[]:,\n \t0aZ";
+        for (int i = 0; i < n_random; i++) {
+            for (int k = 0; k < 32; k++)
+                b[k] = (i & 1) ? (uint8_t)rng() : (uint8_t)alphabet[rng() % (sizeof(alphabet) - 1)];
+            one(b, lines != 0);
+        }
+    }
+    return bad;
 }

@@ -26,7 +26,7 @@ def mixed_docs(cj, seed=7):
     docs = [np.frombuffer(b, np.uint8).copy() for b in (
         b"1", b"[]", b'{"a":"b\\"c,d"}', b"[[[", b"[1,[2]]", b"]]", b"{}", b"[{]}", b"[]",
         b'"\\\\"', b"   ", b'{"k":[{},[]],"x":{}}', b"\xc0\x80", b'["\xed\xa0\x80"]', b"[\"\xe2\x82\xac\"]")]
-    for k, n in enumerate([1023, 1024, 1025, 4095, 65536, 131071, 131072, 131073, 300001, 1 << 20]):
+    for k, n in enumerate([1023, 1024, 1025, 4095, 65536, 114687, 114688, 114689, 131072, 300001, 1 << 20]):
         docs.append(cj.synth_document(seed * 100 + k, n, max_depth=10))
     bad = cj.synth_document(seed * 100 + 50, 200000)
     assert cj.synth_corrupt(bad, cj.CORRUPT_SURROGATE, 3)

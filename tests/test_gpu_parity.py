@@ -22,8 +22,9 @@ def test_small(ctx, oracle, doc):
     assert_same(res, oracle.parse(doc))
 
 
-@pytest.mark.parametrize("n", [1, 2, 31, 32, 33, 255, 8191, 8192, 8193, 16384, 65537, 131071,
-                               131072, 131073, 300001, 1 << 21])
+@pytest.mark.parametrize("n", [1, 2, 31, 32, 33, 255, 7167, 7168, 7169, 8191, 8192, 8193, 16384, 65537,
+                               114687, 114688, 114689, 131071, 131072, 131073, 229377, 300001,
+                               344064, 1 << 21])
 def test_sizes(cj, ctx, oracle, n):
     d = cj.synth_document(n, n) if n >= 2 else np.frombuffer(b"1", np.uint8)
     st, res = ctx.try_parse(d)
@@ -105,7 +106,8 @@ def test_utf8_cases(ctx, oracle):
     for body, ok in [("é€😀".encode(), True), (b"\xc0\x80", False), (b"\xe0\x80\x80", False),
                      (b"\xed\xa0\x80", False), (b"\xf5\x80\x80\x80", False), (b"\xe2\x82", False),
                      (b"\x80", False), (b"\xc3\x41", False)]:
-        for pad in (0, 1, 2, 29, 30, 31, 8189, 8190, 8191, 131069, 131070, 131071):
+        for pad in (0, 1, 2, 29, 30, 31, 7165, 7166, 7167, 8189, 8190, 8191, 114685, 114686, 114687,
+                    131069, 131070, 131071):
             doc = b"[" + b" " * pad + b'"' + body + b'"]'
             st, _ = ctx.try_parse(doc)
             assert (st == 0) == ok, (body, pad, st)

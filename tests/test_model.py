@@ -50,6 +50,13 @@ def check(model, oracle, data, lines=False, chunks=None, seed=1):
         np.testing.assert_array_equal(q, r.pair_row)
 
 
+def test_classify_bit_planes(model):
+    """The bit-sliced character classes equal their byte-by-byte definition."""
+    model.cjm_classify_check.restype = ctypes.c_int
+    model.cjm_classify_check.argtypes = [ctypes.c_uint64, ctypes.c_int]
+    assert model.cjm_classify_check(7, 20000) == 0
+
+
 @pytest.mark.parametrize("seed", range(6))
 def test_documents(cj, oracle, model, seed):
     n = [3000, 70000, 300000, 1 << 20, 123457, 9000][seed]
