@@ -135,12 +135,6 @@ constexpr uint32_t kEmpty = 0xFFFFFFFFu;
 
 // ---- word-level bit algorithms ----------------------------------------------
 
-// high bit of every byte of w that equals the corresponding byte of pat
-CJ_HD uint32_t eq_bytes(uint32_t w, uint32_t pat) {
-    uint32_t x = w ^ pat;
-    return ~(((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x) & 0x80808080u;
-}
-
 // byte selection of the 8 bytes {x, y} (x = bytes 0-3): result byte i is the
 // byte numbered by nibble i of s (0-7)
 CJ_HD uint32_t byte_perm(uint32_t x, uint32_t y, uint32_t s) {
@@ -210,9 +204,7 @@ struct Classes {
 // The four brackets are exactly 01x11yz1 with y != z (open: y = 0, z = 1), the
 // comma and the colon exactly 001a1bc0 with b != a and c == a.
 template <bool LINES>
-CJ_HD Classes classify32(const uint32_t w[8]) {
-    uint32_t P[8];
-    bit_planes32(w, P);
+CJ_HD Classes classify_planes(const uint32_t P[8]) {
     const uint32_t n7 = ~P[7];
     Classes c;
     c.br = n7 & P[6] & P[4] & P[3] & P[0] & (P[1] ^ P[2]);
@@ -226,6 +218,13 @@ CJ_HD Classes classify32(const uint32_t w[8]) {
     if (LINES) c.st |= n7 & P[3] & P[1] & ~(P[6] | P[5] | P[4] | P[2] | P[0]);   // '\n'
     c.hi = P[7];
     return c;
+}
+
+template <bool LINES>
+CJ_HD Classes classify32(const uint32_t w[8]) {
+    uint32_t P[8];
+    bit_planes32(w, P);
+    return classify_planes<LINES>(P);
 }
 
 // carry out of a 32-byte word entered without escape: whether its trailing
@@ -258,60 +257,92 @@ CJ_HD uint32_t escaped32(uint32_t bs, uint32_t carry, uint32_t* cout) {
     return (span & (ODD ^ odd_span)) | carry;
 }
 
-// (hi:lo << s) >> 32 for 0 < s < 32: the bytes of `hi` moved up by s/8 byte
-// positions, filled from the top of `lo` (the word before it)
-CJ_HD uint32_t funnel_l(uint32_t lo, uint32_t hi, int s) {
-#ifdef __CUDA_ARCH__
-    return __funnelshift_l(lo, hi, s);
-#else
-    return (hi << s) | (lo >> (32 - s));
-#endif
+// ---- UTF-8 on bit planes ------------------------------------------------------
+// RFC 3629 validity of one lane's 32 bytes from their bit planes (bit j of
+// P[k] = bit k of byte j; bytes past the end of the segment are zero).  Leads
+// 110xxxxx, 1110xxxx and 11110xxx expect continuation bytes (10xxxxxx) at
+// their next 1, 2 or 3 positions; the expected positions must be exactly the
+// continuation bytes.  11111xxx, C0 and C1 (overlong 2-byte forms) and F5-F7
+// (beyond U+10FFFF) are rejected, and the byte after E0 / ED / F0 / F4 must be
+// >= A0 / <= 9F / >= 90 / <= 8F (overlong 3- and 4-byte forms, surrogates,
+// beyond U+10FFFF).  `cin` is the carry word of the 32 bytes before (the
+// previous lane's utf8_carry_planes).  A sequence still open at the
+// end of the lane is the next lane's to check unless the segment ends there
+// (`seg_end`).  Returns nonzero on an error.
+//
+// Carry word: bit 0 lead needing >= 1 byte at position 31, bits 1-2 leads
+// needing >= 2 at 30-31, bits 3-5 leads needing 3 at 29-31, bits 6-9 an E0,
+// ED, F0 or F4 at position 31.
+CJ_HD uint32_t utf8_carry_out(uint32_t L1, uint32_t L2, uint32_t L3, uint32_t e0, uint32_t ed,
+                              uint32_t f0, uint32_t f4) {
+    return (L1 >> 31) | ((L2 >> 30) << 1) | ((L3 >> 29) << 3) | ((e0 >> 31) << 6) | ((ed >> 31) << 7) |
+           ((f0 >> 31) << 8) | ((f4 >> 31) << 9);
 }
 
-// RFC 3629 validity of one lane's 32 bytes (8 little-endian words, bytes past
-// the end of the segment already zeroed), given the 4 bytes before them in
-// `pw`.  Works on byte-form masks (bit 7 of each byte): leads >= C0, >= E0,
-// >= F0, and continuation bytes (10xxxxxx).  A lead expects continuation bytes
-// at its next 1, 2 or 3 positions (funnel shifts carry that across words and
-// from `pw`); the expected positions must be exactly the continuation bytes.
-// C0, C1 and F5..FF are rejected, and the byte after E0 / ED / F0 / F4 is
-// range-checked (overlong and surrogate forms, code points above U+10FFFF).
-// A sequence still open at the end of the 32 bytes is the next lane's to check,
-// unless the segment ends there (`seg_end`).  Returns nonzero on an error.
-CJ_HD uint32_t utf8_errors(const uint32_t w[8], uint32_t pw, bool seg_end) {
-    const uint32_t H = 0x80808080u;
-    uint32_t c2p = pw & (pw << 1) & H, c3p = c2p & (pw << 2), c4p = c3p & (pw << 3);
-    uint32_t err = 0, any3 = c3p;
-#pragma unroll
-    for (int k = 0; k < 8; k++) {
-        const uint32_t x = w[k];
-        const uint32_t c2 = x & (x << 1) & H;
-        const uint32_t c3 = c2 & (x << 2);
-        const uint32_t c4 = c3 & (x << 3);
-        const uint32_t cont = x & ~(x << 1) & H;
-        const uint32_t E = funnel_l(c2p, c2, 8) | funnel_l(c3p, c3, 16) | funnel_l(c4p, c4, 24);
-        err |= E ^ cont;
-        err |= c2 & ~c3 & ~((x & 0x1E1E1E1Eu) + 0x7F7F7F7Fu);      // C0, C1
-        err |= c4 & (((x & 0x0F0F0F0Fu) + 0x0B0B0B0Bu) << 3);      // F5..FF
-        any3 |= c3;
-        c2p = c2; c3p = c3; c4p = c4;
+// leads and special bytes of one lane's 32 bytes, from its bit planes
+struct Utf8Lane {
+    uint32_t cont, L1, L2, L3, bad, c0c1, f5f7, e0, ed, f0, f4;
+};
+
+CJ_HD Utf8Lane utf8_lane(const uint32_t P[8]) {
+    Utf8Lane u;
+    const uint32_t t76 = P[7] & P[6];
+    u.cont = P[7] & ~P[6];
+    const uint32_t l2 = t76 & ~P[5];
+    const uint32_t t765 = t76 & P[5];
+    const uint32_t l3 = t765 & ~P[4];
+    const uint32_t t7654 = t765 & P[4];
+    u.L3 = t7654 & ~P[3];                                             // 11110xxx
+    u.bad = t7654 & P[3];                                             // F8..FF
+    u.L2 = l3 | u.L3;
+    u.L1 = l2 | u.L2;
+    const uint32_t lo3 = P[2] | P[1] | P[0];
+    u.c0c1 = l2 & ~(P[4] | P[3] | P[2] | P[1]);                      // C0, C1
+    u.f5f7 = u.L3 & P[2] & (P[1] | P[0]);                             // F5, F6, F7
+    u.e0 = l3 & ~(P[3] | lo3);                                        // E0
+    u.ed = l3 & P[3] & P[2] & ~P[1] & P[0];                           // ED
+    u.f0 = u.L3 & ~lo3;                                               // F0
+    u.f4 = u.L3 & P[2] & ~(P[1] | P[0]);                              // F4
+    return u;
+}
+
+// the carry word this lane hands to the next (it depends on its bytes only)
+CJ_HD uint32_t utf8_carry_planes(const uint32_t P[8]) {
+    const Utf8Lane u = utf8_lane(P);
+    return utf8_carry_out(u.L1, u.L2, u.L3, u.e0, u.ed, u.f0, u.f4);
+}
+
+CJ_HD uint32_t utf8_errors_planes(const uint32_t P[8], uint32_t cin, bool seg_end) {
+    const Utf8Lane u = utf8_lane(P);
+    const uint32_t E = (u.L1 << 1) | (u.L2 << 2) | (u.L3 << 3) | (cin & 1u) | ((cin >> 1) & 3u) |
+                       ((cin >> 3) & 7u);
+    const uint32_t b54 = P[5] | P[4];
+    uint32_t err = (E ^ u.cont) | u.bad | u.c0c1 | u.f5f7;
+    err |= ((u.e0 << 1) | ((cin >> 6) & 1u)) & ~P[5];                // E0 then < A0
+    err |= ((u.ed << 1) | ((cin >> 7) & 1u)) & P[5];                 // ED then >= A0
+    err |= ((u.f0 << 1) | ((cin >> 8) & 1u)) & ~b54;                 // F0 then < 90
+    err |= ((u.f4 << 1) | ((cin >> 9) & 1u)) & b54;                  // F4 then >= 90
+    if (seg_end) err |= (u.L1 >> 31) | (u.L2 >> 30) | (u.L3 >> 29);
+    return err;
+}
+
+// carry word of the 4 bytes of `w` as the last bytes before a lane (byte 3 at
+// position 31); the same bits utf8_errors_planes hands on
+CJ_HD uint32_t utf8_carry_word(uint32_t w) {
+    uint32_t L1 = 0, L2 = 0, L3 = 0, e0 = 0, ed = 0, f0 = 0, f4 = 0;
+    for (int k = 1; k < 4; k++) {
+        const uint32_t b = (w >> (8 * k)) & 0xFFu;
+        const uint32_t bit = 1u << (28 + k);                            // positions 29, 30, 31
+        const bool is2 = (b & 0xE0u) == 0xC0u, is3 = (b & 0xF0u) == 0xE0u, is4 = (b & 0xF8u) == 0xF0u;
+        if (is2 || is3 || is4) L1 |= bit;
+        if (is3 || is4) L2 |= bit;
+        if (is4) L3 |= bit;
+        if (b == 0xE0u) e0 |= bit;
+        if (b == 0xEDu) ed |= bit;
+        if (b == 0xF0u) f0 |= bit;
+        if (b == 0xF4u) f4 |= bit;
     }
-    if (seg_end) err |= (c2p >> 24) | (c3p >> 16) | (c4p >> 8);
-    if (any3) {
-        uint32_t p = pw;
-#pragma unroll
-        for (int k = 0; k < 8; k++) {
-            const uint32_t x = w[k];
-            const uint32_t pb = funnel_l(p, x, 8);                   // byte before each position
-            const uint32_t b5 = x << 2, b4 = x << 3;                 // bits 5 / 4 -> bit 7
-            err |= eq_bytes(pb, 0xE0E0E0E0u) & ~b5;                  // E0 then < A0
-            err |= eq_bytes(pb, 0xEDEDEDEDu) & b5;                   // ED then >= A0
-            err |= eq_bytes(pb, 0xF0F0F0F0u) & ~(b5 | b4);           // F0 then < 90
-            err |= eq_bytes(pb, 0xF4F4F4F4u) & (b5 | b4);            // F4 then >= 90
-            p = x;
-        }
-    }
-    return err & H;
+    return utf8_carry_out(L1, L2, L3, e0, ed, f0, f4);
 }
 
 // inclusive prefix XOR over the bits of x

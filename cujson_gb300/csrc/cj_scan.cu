@@ -13,7 +13,8 @@
 //   A. (tile t) every classifying warp, on its own: builds the quote, backslash,
 //      structural and bracket bitmaps of each lane's 32 bytes (bit-sliced:
 //      8 bit planes, one logic operation per class and 32 bytes), validates
-//      UTF-8 (byte-parallel, only on steps holding non-ASCII bytes), resolves
+//      UTF-8 on the same planes (only on steps holding non-ASCII bytes or
+//      continuing a sequence; a packed carry word moves lane to lane), resolves
 //      escapes and the in-string mask assuming its region is entered outside
 //      any string and escape (carries move lane to lane with ballots and
 //      shuffles, step to step in registers), keeps the masks in shared memory
@@ -265,19 +266,17 @@ __device__ __forceinline__ uint32_t region_prev_word(const TileInfo& g, int warp
 }
 
 // Phase A of one warp's region: classify, validate, resolve strings, keep masks.
-// The first steps' copies were started by start_region (at the end of the
-// warp's previous phase A, or here when `started_copies` is false);
-// `prev_last` holds region_prev_word.
+// `prev_word` holds region_prev_word (the 4 input bytes before the region).
 template <bool LINES>
 __device__ __forceinline__ void phase_a(const ScanParams& P, const TileInfo& g, WarpSmem& W, Slot& sl,
-                                        uint32_t& parity, int warp, int lane, uint32_t lt,
-                                        bool started_copies, uint32_t prev_last)
+                                        uint32_t& parity, int warp, int lane, uint32_t lt, uint32_t prev_word)
 {
     const int reg_off = warp * kWarpBytes;
     const int reg_len = region_len(g, warp);
     const int nsteps = (reg_len + kStepBytes - 1) / kStepBytes;
     const uint8_t* reg_src = g.seg_base + g.tile_off + reg_off;
-    if (lane == 0 && !started_copies) start_region(g, W, warp);
+    if (lane == 0) start_region(g, W, warp);
+    uint32_t ucarry = 0;                   // UTF-8 carry into the step (warp uniform)
     uint32_t carry = 0, par = 0;           // escape carry / quote parity (warp uniform)
     uint32_t started = 0, wflip = 0;       // first non-all-backslash lane seen / its flip
     uint32_t n_c0 = 0, n_ct = 0, n_k0 = 0, n_kt = 0, n_o0 = 0, n_ot = 0;   // per lane
@@ -303,25 +302,28 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileInfo& g, 
         if (16 > valid) mask_chunk(lo, valid);
         if (32 > valid) mask_chunk(hi, valid - 16);
         const uint32_t w[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
-        const Classes c = classify32<LINES>(w);
+        uint32_t planes[8];
+        bit_planes32(w, planes);
+        const Classes c = classify_planes<LINES>(planes);
 
-        // UTF-8, byte-parallel, on steps that hold a non-ASCII byte
-        if (__any_sync(FULL, c.hi != 0u) || (prev_last & 0x80808000u)) {
-            uint32_t pw = __shfl_up_sync(FULL, w[7], 1);
-            if (lane == 0) pw = prev_last;
-            prev_last = __shfl_sync(FULL, w[7], 31);
-            const bool mine = valid > 0 && (c.hi || (pw & 0x80808000u));
-            if (__any_sync(FULL, mine) && valid > 0) {
+        // UTF-8 on the bit planes, on steps that hold a non-ASCII byte or
+        // continue a sequence from the bytes before them.  A lane's carry-out
+        // depends on its own bytes only, so one shuffle hands it on.
+        if (j == 0 && (prev_word & 0x80808000u)) ucarry = utf8_carry_word(prev_word);
+        if (__any_sync(FULL, c.hi != 0u) || ucarry != 0u) {
+            const uint32_t cout = utf8_carry_planes(planes);
+            uint32_t cin = __shfl_up_sync(FULL, cout, 1);
+            if (lane == 0) cin = ucarry;
+            ucarry = __shfl_sync(FULL, cout, 31);
+            if (valid > 0) {
                 const bool seg_end = g.tile_off + (uint64_t)(reg_off + j * kStepBytes + my0 + kBytesPerThread) >= g.seg_len;
-                if (utf8_errors(w, pw, seg_end)) {
+                if (utf8_errors_planes(planes, cin, seg_end)) {
                     if (P.seg_err) atomicOr(P.seg_err + g.segi, CJ_FLAG_UTF8);
                     else atomicOr(&P.ctrl->error_flags, CJ_FLAG_UTF8);
                 }
             }
         } else {
-            // an all-ASCII step after a word without lead bytes: nothing to
-            // check, and the step's last word has no high bit either
-            prev_last = 0u;
+            ucarry = 0u;           // an all-ASCII step opens no sequence
         }
 
         // escapes: carry from the nearest earlier lane that is not all backslashes
@@ -758,7 +760,7 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
         const uint32_t tile = got_tile ? S.info[i % kTickets].tile : kNoTile;
         if (tile != kNoTile) {
             const TileInfo& g = S.info[i % kTickets];
-            phase_a<LINES>(P, g, W, S.slot[i % kSlots], parity, warp, lane, lt, false, region_prev_word(g, warp));
+            phase_a<LINES>(P, g, W, S.slot[i % kSlots], parity, warp, lane, lt, region_prev_word(g, warp));
             __syncwarp();
             if (lane == 0) mbar_arrive(&S.a_done[i % kSlots]);
         }

@@ -98,6 +98,7 @@ extern "C" int cjm_parse(const uint8_t* data, size_t n, int lines, const size_t*
             static Classes c[W];
             static uint32_t cout0[W];
             static bool all_bs[W];
+            uint32_t ucarry = 0;
             for (int t = 0; t < W; t++) {
                 uint32_t w[8];
                 for (int k = 0; k < 8; k++) {
@@ -108,17 +109,26 @@ extern "C" int cjm_parse(const uint8_t* data, size_t n, int lines, const size_t*
                     }
                     w[k] = v;
                 }
-                c[t] = lines ? classify32<true>(w) : classify32<false>(w);
+                uint32_t P[8];
+                bit_planes32(w, P);
+                c[t] = lines ? classify_planes<true>(P) : classify_planes<false>(P);
                 {
-                    // previous 4 bytes of the segment (zero before its start)
-                    uint32_t pw = 0;
+                    // UTF-8 as the kernel checks it: on the bit planes, the
+                    // carry handed lane to lane and step to step, and taken
+                    // afresh from the 4 bytes before each warp region
                     const int64_t o0 = (int64_t)tile_off + t * 32;
-                    for (int b = 0; b < 4; b++) {
-                        const int64_t o = o0 - 4 + b;
-                        if (o >= 0 && (uint64_t)o < sg.len) pw |= (uint32_t)sb[o] << (8 * b);
+                    if ((t * 32) % kWarpBytes == 0) {
+                        uint32_t pw = 0;   // previous 4 bytes of the segment (zero before its start)
+                        for (int b = 0; b < 4; b++) {
+                            const int64_t o = o0 - 4 + b;
+                            if (o >= 0 && (uint64_t)o < sg.len) pw |= (uint32_t)sb[o] << (8 * b);
+                        }
+                        ucarry = utf8_carry_word(pw);
                     }
                     const bool seg_end = (uint64_t)(o0 + 32) >= sg.len;
-                    if ((uint64_t)o0 < sg.len && utf8_errors(w, pw, seg_end)) flags |= 1;
+                    const uint32_t next = utf8_carry_planes(P);
+                    if (utf8_errors_planes(P, ucarry, seg_end)) flags |= 1;
+                    ucarry = next;
                 }
                 escaped32(c[t].bs, 0, &cout0[t]);
                 all_bs[t] = c[t].bs == 0xFFFFFFFFu;

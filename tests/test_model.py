@@ -148,3 +148,24 @@ def test_utf8_dense_short(oracle, model):
         doc2 = b'[""]' + b" " * pad + body        # the bytes end the input
         _, _, fl = run_model(model, doc2)
         assert bool(fl & 1) == (not oracle.utf8_valid(doc2)), (body, pad)
+
+
+def test_utf8_across_region_and_tile_boundaries(oracle, model):
+    """Multi-byte sequences, valid and invalid, placed across 32-byte lane,
+    7 KiB warp-region and 112 KiB tile boundaries: the carries that hand an
+    open sequence to the next lane, step or region."""
+    seqs = ["é".encode(), "€".encode(), "😀".encode(), b"\xc0\x80", b"\xe0\x80\x80", b"\xed\xa0\x80",
+            b"\xf0\x80\x80\x80", b"\xf4\x90\x80\x80", b"\xf5\x80\x80\x80", b"\xe2\x82", b"\x80", b"\xc3\x41",
+            b"\xe0\xa0\x80", b"\xed\x9f\xbf", b"\xf0\x90\x80\x80", b"\xf4\x8f\xbf\xbf"]
+    for boundary in (32, 1024, 7168, 114688):
+        for body in seqs:
+            for shift in range(-4, 2):
+                pad = boundary + shift - 2          # the sequence starts at byte boundary + shift
+                if pad < 0:
+                    continue
+                doc = b"[" + b" " * pad + b'"' + body + b'"]'
+                _, _, fl = run_model(model, doc)
+                assert bool(fl & 1) == (not oracle.utf8_valid(doc)), (boundary, body, shift)
+                doc2 = b"[]" + b" " * (pad + 2) + body       # the sequence ends the input
+                _, _, fl = run_model(model, doc2)
+                assert bool(fl & 1) == (not oracle.utf8_valid(doc2)), (boundary, body, shift, "end")
