@@ -353,6 +353,14 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileInfo& g, 
                     started = 1;
                 }
                 carry = (couts >> (31 - __clz(nonall))) & 1u;
+            } else {
+                // every byte of the step is a backslash (inside a long run):
+                // an even run, so the escape carry passes through, and with
+                // no quote or structural byte the string state and counts
+                // stay and phase C has nothing to write
+                uint32_t (&mz)[kMaskFields][32] = sl.masks[warp][j];
+                mz[0][lane] = 0u; mz[1][lane] = 0u; mz[2][lane] = 0u; mz[3][lane] = 0u;
+                continue;
             }
         }
         uint32_t dummy;
@@ -386,7 +394,9 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileInfo& g, 
         t.k = (uint32_t)(e ? Kt - K0 : K0);
         t.d = e ? Dt - D0 : D0;
         sl.wtab[warp][lane] = t;
-        if (lane == 0) sl.we[warp] = wflip;
+        if (lane == 0) {
+            sl.we[warp] = wflip;
+        }
     }
 }
 
