@@ -279,6 +279,7 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileInfo& g, 
     uint32_t ucarry = 0;                   // UTF-8 carry into the step (warp uniform)
     uint32_t carry = 0, par = 0;           // escape carry / quote parity (warp uniform)
     uint32_t started = 0, wflip = 0;       // first non-all-backslash lane seen / its flip
+    uint32_t in_run = 0;                   // the previous step ended in 32 backslashes
     uint32_t n_c0 = 0, n_ct = 0, n_k0 = 0, n_kt = 0, n_o0 = 0, n_ot = 0;   // per lane
     for (int j = 0; j < nsteps; j++) {
         const int st_i = j % kStages;
@@ -302,6 +303,22 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileInfo& g, 
         if (16 > valid) mask_chunk(lo, valid);
         if (32 > valid) mask_chunk(hi, valid - 16);
         const uint32_t w[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+        uint32_t (&m)[kMaskFields][32] = sl.masks[warp][j];
+        if (in_run) {
+            // inside a long backslash run: a step of 1 KiB of backslashes is an
+            // even run (the escape carry passes through), opens no UTF-8
+            // sequence, and has no quote or structural byte, so the string
+            // state and the counts stay and phase C has nothing to write --
+            // checked without classifying
+            uint32_t d = 0;
+#pragma unroll
+            for (int k = 0; k < 8; k++) d |= w[k] ^ 0x5C5C5C5Cu;
+            if (__all_sync(FULL, d == 0u)) {
+                m[0][lane] = 0u; m[1][lane] = 0u; m[2][lane] = 0u; m[3][lane] = 0u;
+                ucarry = 0u;
+                continue;
+            }
+        }
         uint32_t planes[8];
         bit_planes32(w, planes);
         const Classes c = classify_planes<LINES>(planes);
@@ -331,6 +348,7 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileInfo& g, 
         if (!__any_sync(FULL, (int32_t)c.bs < 0)) {
             // no lane ends in a backslash: only lane 0 can receive a carry
             lane_carry = (lane == 0) ? carry : 0u;
+            in_run = 0;
             if (!started) {
                 wflip = __shfl_sync(FULL, (c.q >> (__ffs(~c.bs) - 1)) & 1u, 0);
                 started = 1;
@@ -353,13 +371,14 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileInfo& g, 
                     started = 1;
                 }
                 carry = (couts >> (31 - __clz(nonall))) & 1u;
+                in_run = (nonall >> 31) ^ 1u;    // lane 31: 32 backslashes
             } else {
                 // every byte of the step is a backslash (inside a long run):
                 // an even run, so the escape carry passes through, and with
                 // no quote or structural byte the string state and counts
                 // stay and phase C has nothing to write
-                uint32_t (&mz)[kMaskFields][32] = sl.masks[warp][j];
-                mz[0][lane] = 0u; mz[1][lane] = 0u; mz[2][lane] = 0u; mz[3][lane] = 0u;
+                m[0][lane] = 0u; m[1][lane] = 0u; m[2][lane] = 0u; m[3][lane] = 0u;
+                in_run = 1;
                 continue;
             }
         }
@@ -374,7 +393,6 @@ __device__ __forceinline__ void phase_a(const ScanParams& P, const TileInfo& g, 
         n_c0 += __popc(c.st & ~M); n_ct += __popc(c.st);
         n_k0 += __popc(br & ~M);   n_kt += __popc(br);
         n_o0 += __popc(c.op & ~M); n_ot += __popc(c.op);
-        uint32_t (&m)[kMaskFields][32] = sl.masks[warp][j];
         m[0][lane] = c.op;
         m[1][lane] = br & ~c.op;
         m[2][lane] = c.cur | (c.st & ~br);
