@@ -21,7 +21,7 @@ namespace cj {
 // by itself; a tile is the kWarps regions of one CTA, and the cross-tile carry
 // (decoupled look-back) runs once per tile.
 constexpr int kWarps = 16;                                // classifying warps per CTA
-constexpr int kCoords = 2;                                // coordinator warps (alternate tiles)
+constexpr int kCoords = 2;                                // coordinator warps (tickets in turn)
 constexpr int kThreads = (kWarps + kCoords) * 32;
 constexpr int kBytesPerThread = 32;
 constexpr int kStepBytes = 32 * kBytesPerThread;          // 1 KiB, one TMA copy

@@ -101,7 +101,10 @@ struct __align__(16) TileInfo {
     uint32_t flags;            // kTileFirst | kTileLast | kTileImmediate
 };
 constexpr uint32_t kTileFirst = 1u, kTileLast = 2u, kTileImmediate = 4u;
-constexpr int kTickets = 4;    // ticket ring: ticket i lives in info[i % kTickets]
+constexpr int kTickets = 8;    // ticket ring: ticket i lives in info[i % kTickets]
+// a coordinator reads tickets i - kCoords + 1 .. i before any warp can have
+// finished phase A of ticket i + 3 (see the coordinator loop)
+static_assert(kTickets >= kCoords + 3, "ticket ring too short for the coordinators");
 
 struct __align__(128) Smem {
     WarpSmem w[kWarps];
@@ -695,23 +698,23 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
         }
         __syncwarp();
         for (uint32_t i = c;; i += kCoords) {
-            // ticket i exists only if ticket i - 1 was a tile (it is drawn
-            // after that tile's phase A).  info[(i - 1) % kTickets] is next
-            // written by this coordinator (ticket i + 3, drawn after tile
-            // i + 2), info[i % kTickets] only after phase A of ticket i + 3,
-            // which follows phase C of ticket i.
-            if (i >= 1) {
-                if (!__shfl_sync(FULL, mbar_wait(&S.tile_ready[(i - 1) % kTickets], ((i - 1) / kTickets) & 1u,
-                                                 P.ctrl), 0)) {
+            // ticket t + 1 is drawn after phase A of ticket t, and only if
+            // ticket t is a tile: walk the tickets since this coordinator's
+            // previous one (always drawn) up to i, and stop at the first one
+            // past the last tile.  A ticket t read here is overwritten at the
+            // earliest by ticket t + kTickets, drawn after phase A of ticket
+            // t + kTickets - 1 >= i + 3, which every warp runs after phase C
+            // of ticket i, i.e. after this coordinator has resolved ticket i.
+            bool more = true;
+            for (uint32_t t = (i >= kCoords - 1 ? i - (kCoords - 1) : 0u); more && t <= i; t++) {
+                if (!__shfl_sync(FULL, mbar_wait(&S.tile_ready[t % kTickets], (t / kTickets) & 1u, P.ctrl), 0)) {
                     if (lane == 0) give_up(P.ctrl, kGaveTileReady);
-                    break;
+                    more = false;
+                } else if (S.info[t % kTickets].tile == kNoTile) {
+                    more = false;
                 }
-                if (S.info[(i - 1) % kTickets].tile == kNoTile) break;
             }
-            if (!__shfl_sync(FULL, mbar_wait(&S.tile_ready[i % kTickets], (i / kTickets) & 1u, P.ctrl), 0)) {
-                if (lane == 0) give_up(P.ctrl, kGaveTileReady);
-                break;
-            }
+            if (!more) break;
             const TileInfo& g = S.info[i % kTickets];
             const uint32_t tile = g.tile;
             if (tile == kNoTile) break;
@@ -720,7 +723,8 @@ __global__ void __launch_bounds__(kThreads, 1) scan_kernel(ScanParams P)
             if (!mbar_wait(&S.a_done[s], (i / kSlots) & 1u, P.ctrl) && lane == 0) give_up(P.ctrl, kGaveADone);
             if (lane == 0) {
                 // info[(i + 1) % kTickets] last held ticket i + 1 - kTickets,
-                // whose phase C ended before any warp's phase A of ticket i began
+                // whose phase C ended before any warp's phase A of ticket i
+                // began, and which every coordinator has read
                 draw_tile(P, S.info[(i + 1) % kTickets]);
                 mbar_arrive(&S.tile_ready[(i + 1) % kTickets]);
             }
