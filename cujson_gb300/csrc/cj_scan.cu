@@ -1,39 +1,41 @@
 // cj_scan.cu -- the single-pass structural scan (persistent, TMA-staged,
 // warp-independent, software-pipelined across tiles).
 //
-// A persistent grid of CTAs (one per SM: 16 classifying warps and one
-// coordinator warp) takes 128 KiB tiles in document order from an atomic
-// ticket; the coordinator draws each ticket two tiles ahead and keeps the
-// tile's segment geometry in shared memory.  Each classifying warp owns a
-// contiguous 8 KiB region of a tile and works through it in 1 KiB steps
-// (32 lanes x 32 bytes) staged in its own 3-deep shared-memory ring by bulk
-// TMA copies (cp.async.bulk completing on per-warp mbarriers); the copies of
-// a region's first steps start as soon as the warp's previous phase A ends.
+// A persistent grid of CTAs (one per SM: 16 classifying warps and
+// kCoords = 2 coordinator warps) takes 112 KiB tiles in document order from an
+// atomic ticket; the coordinator of ticket i draws ticket i + 1 once every
+// warp has finished phase A of ticket i, and keeps the tile's segment geometry
+// in shared memory.  Each classifying warp owns a contiguous 7 KiB region of a
+// tile and works through it in 1 KiB steps (32 lanes x 32 bytes) staged in its
+// own 3-deep shared-memory ring by bulk TMA copies (cp.async.bulk completing
+// on per-warp mbarriers).
 //
-//   A. (tile t) every classifying warp, on its own: builds the quote, backslash,
-//      structural and bracket bitmaps of each lane's 32 bytes (bit-sliced:
-//      8 bit planes, one logic operation per class and 32 bytes), validates
-//      UTF-8 on the same planes (only on steps holding non-ASCII bytes or
-//      continuing a sequence; a packed carry word moves lane to lane), resolves
-//      escapes and the in-string mask assuming its region is entered outside
-//      any string and escape (carries move lane to lane with ballots and
-//      shuffles, step to step in registers), keeps the masks in shared memory
-//      and sums the counts into a transfer table: for each of the 4 entry
-//      states (escape, in-string), the exit state, structural count, bracket
-//      count and depth delta.
-//   B. (tile t, coordinator warp, while the classifying warps run phase A of
-//      tile t+1) composes the 16 warp tables into the tile's table, publishes
-//      it (decoupled look-back descriptor), finds the tile's exclusive prefix by
-//      look-back (64 predecessors per round, loaded in parallel and composed
-//      with an ordered shuffle reduction), publishes the inclusive value and
-//      derives each warp's entry value.
-//   C. (tile t, after phase A of tile t+1) every classifying warp replays its
-//      masks with its entry value and writes 1-based structural positions, a
-//      zeroed pair row and one bracket record (structural index, level, open
-//      flag, brace or bracket) per bracket.
-// Hand-offs between the two roles are mbarriers (tile_ready, a_done,
-// prefix_ready; see Smem) with bounded waits; the look-back never stalls the
-// classifying warps unless it takes longer than a whole phase A.
+//   A. (ticket i) every classifying warp, on its own: builds the quote,
+//      backslash, structural and bracket bitmaps of each lane's 32 bytes
+//      (bit-sliced: 8 bit planes, one logic operation per class and 32 bytes),
+//      validates UTF-8 on the same planes (only on steps holding non-ASCII
+//      bytes or continuing a sequence; a packed carry word moves lane to lane),
+//      resolves escapes and the in-string mask assuming its region is entered
+//      outside any string and escape (carries move lane to lane with ballots,
+//      step to step in registers), keeps four mask words per lane and step in
+//      shared memory and sums the counts into a transfer table: for each of the
+//      4 entry states (escape, in-string), the exit state, structural count,
+//      bracket count and depth delta.  Steps of 1 KiB of backslashes (inside
+//      long backslash runs) change nothing but the escape carry and are
+//      skipped early.
+//   B. (ticket i, coordinator i % kCoords, while the classifying warps run the
+//      next tickets) composes the 16 warp tables into the tile's table,
+//      publishes it (decoupled look-back descriptor), finds the tile's
+//      exclusive prefix by look-back (64 predecessors per round, loaded in
+//      parallel and composed with an ordered shuffle reduction), publishes the
+//      inclusive value and derives each warp's entry value.
+//   C. (ticket i, after phase A of ticket i + 2) every classifying warp replays
+//      its masks with its entry value and writes 1-based structural
+//      positions, a zeroed pair row and one bracket record (structural index,
+//      level, open flag, brace or bracket) per bracket.
+// Hand-offs between the roles are mbarriers (tile_ready, a_done,
+// prefix_ready; see Smem) with bounded waits; with three mask slots a
+// look-back has two phase A's of slack before the classifying warps wait.
 //
 // This replaces the reference's stage 1 (checkAscii + checkUTF8,
 // cujson/parse_standard_json.cu:186-327) and stage 2 (bitMapCreatorSimd :446,
