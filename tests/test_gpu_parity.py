@@ -141,6 +141,31 @@ def test_empty_input_rejected(ctx):
     assert st == 1
 
 
+def _run_doc(pad, runs):
+    """A document whose string holds backslash runs of the given lengths, each
+    followed by a byte it may escape and separated by in-string text with
+    structural bytes; odd runs escape the quote after them."""
+    body = b""
+    for k, L in enumerate(runs):
+        body += b"\\" * L + (b'"x' if L % 2 else b"") + b"t{,}:[" * (k % 3)
+    return b"[" + b" " * pad + b'"' + body + b'",{"k":[1,{"v":"\\\""}]}]'
+
+
+@pytest.mark.parametrize("pad", [0, 1, 30, 31, 32, 511, 1022, 1023, 7167, 114687])
+def test_backslash_run_alignments(ctx, oracle, pad):
+    """Backslash runs starting and ending on and around 32-byte lane, 1 KiB
+    step, 7 KiB region and 112 KiB tile boundaries, even and odd: the steps
+    made only of backslashes are skipped by the scan (the escape carry passes
+    through), and the ones around them must still resolve every escape."""
+    for runs in ([1024], [1023], [1025], [2048], [2047], [3072, 1], [4096, 2, 4095],
+                 [7168], [7169], [7167, 1024, 1023], [114688], [114689, 3], [1 << 18, 1 << 18 | 1]):
+        doc = _run_doc(pad, runs)
+        st, res = ctx.try_parse(doc)
+        ref = oracle.parse(doc)
+        assert st == 0 and ref.flags == 0, (pad, runs)
+        assert_same(res, ref)
+
+
 def test_input_wait_timeout_reported(cj, ctx, oracle):
     """A bounded wait that runs out: the scan waits for input bytes that a
     counter nobody raises never reports; the kernel gives up after a few polls,
