@@ -131,9 +131,20 @@ __global__ void __launch_bounds__(256) pair_chunks(PairParams P)
         }
         const uint64_t base = c * kChunk;
         uint32_t err = 0;
-        for (int i = lane; i < kHeads; i += 32) heads[i] = kEmpty;
         const uint2 r0 = __ldcg(P.brk + base);
         const int32_t L0 = (int32_t)r0.y >> 1;
+        // the head slots this chunk's records use (levels L0 - kChunk ..
+        // L0 + kChunk map to slots 0 .. kHeads - 1): only those are cleared
+        // here and read back at the end
+        int32_t smin = kHeads - 1, smax = 0;
+        for (int i = lane; i < cnt; i += 32) {
+            const int32_t sl = ((int32_t)__ldcg(&P.brk[base + i].y) >> 1) - L0 + kChunk;
+            smin = min(smin, max(sl, 0));
+            smax = max(smax, min(sl, kHeads - 1));
+        }
+        smin = __reduce_min_sync(FULL, smin);
+        smax = __reduce_max_sync(FULL, smax);
+        for (int i = smin + lane; i <= smax; i += 32) heads[i] = kEmpty;
         const int32_t d_entry = (r0.y & 1u) ? L0 : L0 + 1;
         int32_t dmin = d_entry, maxd = INT_MIN;
         int32_t last_lvl = 0;
@@ -190,7 +201,7 @@ __global__ void __launch_bounds__(256) pair_chunks(PairParams P)
             maxd = max(maxd, __shfl_xor_sync(FULL, maxd, o));
         }
         const int32_t d_exit = last_open ? last_lvl + 1 : last_lvl;
-        for (int i = lane; i < kHeads; i += 32) {
+        for (int i = smin + lane; i <= smax; i += 32) {
             const uint32_t h = heads[i];
             if (h != kEmpty) {
                 const int32_t lvl = i - kChunk + L0;
