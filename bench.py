@@ -480,9 +480,34 @@ def run_other_configs(args, local, peak):
             "scan_ms": round(scan_ms / runs, 4), "scan_roofline_frac": round(B / (scan_ms / runs / 1e3) / 1e9 / peak, 4),
             "l2": "input larger than L2" if N > (129 << 20) else "input 64 MiB < 129 MB L2 (no flush: warm-L2 figure)",
             "e2e": e2e,
+            "plan": plan_timing(cj, ctx, data, local) if info["kind"] == "lines" else None,
         })
         ctx.close()
     return out
+
+
+def plan_timing(cj, ctx, data, local):
+    """The 4-chunk JSON-Lines plan of the input (loadJSONLines_chunkCount's
+    rule): the host planner on the host copy against the device planner on a
+    device copy (median of 5 each), and whether the plans agree."""
+    try:
+        import torch
+        d = torch.from_numpy(data).to(f"cuda:{local}")
+    except Exception as e:          # the device planner needs a device copy
+        return {"unavailable": str(e)[:120]}
+
+    def median_ms(fn):
+        ts = []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            r = fn()
+            ts.append((time.perf_counter() - t0) * 1e3)
+        return r, statistics.median(ts)
+
+    host, host_ms = median_ms(lambda: cj.plan_lines_count(data, 4))
+    dev, dev_ms = median_ms(lambda: ctx.plan_lines_count_device(d.data_ptr(), int(data.size), 4))
+    del d
+    return {"chunks": 4, "host_ms": round(host_ms, 3), "device_ms": round(dev_ms, 3), "same": host == dev}
 
 
 QUERY_SEED = 0xC0DE5004

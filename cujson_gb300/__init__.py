@@ -162,6 +162,8 @@ _SIGNATURES = {
     "cj_plan_lines_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
                                            ctypes.c_void_p, ctypes.c_size_t,
                                            ctypes.POINTER(ctypes.c_size_t)]),
+    "cj_plan_lines_count_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                                  ctypes.c_size_t, ctypes.c_void_p]),
     "cj_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "cj_last_status": (ctypes.c_int, []),
     "cj_last_error": (ctypes.c_char_p, []),
@@ -474,6 +476,14 @@ class Context:
         v = ctypes.c_double()
         _check(lib().cj_context_span_ms(self._h, ctypes.byref(v)), "span_ms")
         return v.value
+
+    def plan_lines_count_device(self, d_ptr: int, size: int, chunk_count: int) -> List[int]:
+        """cj_plan_lines_count_device: the chunk plan of a JSON-Lines buffer at
+        device address `d_ptr` (`size` bytes), computed on the device."""
+        out = np.zeros(chunk_count, dtype=np.uint64)
+        _check(lib().cj_plan_lines_count_device(self._h, ctypes.c_void_p(d_ptr) if size else None, size,
+                                                chunk_count, out.ctypes.data), "plan_lines_count_device")
+        return [int(x) for x in out]
 
     def parse_into(self, data, out: np.ndarray, lines: bool = False) -> ParseInfo:
         buf = _u8(data)

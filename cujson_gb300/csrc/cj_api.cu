@@ -118,6 +118,11 @@ struct cj_context {
     DevBuf<unsigned long long> q_count;
     DevBuf<long long> q_out;
 
+    // JSON-Lines chunk planning of device buffers (cj_plan_lines_count_device)
+    DevBuf<uint32_t> plan_counts;
+    DevBuf<uint2> plan_req;
+    DevBuf<unsigned long long> plan_pos;
+
     // launch shapes (0 = default), set by cj_context_set_tuning / cj_autotune_staged
     uint32_t tune_scan_ctas = 0;
     uint32_t tune_pair_blocks = 0;
@@ -884,6 +889,7 @@ void cj_context_destroy(cj_context* ctx)
     release(ctx->seg_err); release(ctx->seg_depth); release(ctx->rchunk_off);
     release(ctx->layout_off); release(ctx->layout); release(ctx->pack); release(ctx->pack_off);
     release(ctx->q_count); release(ctx->q_out);
+    release(ctx->plan_counts); release(ctx->plan_req); release(ctx->plan_pos);
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
     if (ctx->d_ready) cudaFree(ctx->d_ready);
@@ -1311,5 +1317,23 @@ const char* cj_status_string(int status)
 int cj_last_status(void) { return g_last_status; }
 void cj_set_last_status(int status) { g_last_status = status; }
 const char* cj_last_error(void) { return cj_status_string(g_last_status); }
+
+cj_status cj_plan_lines_count_device(cj_context* ctx, const uint8_t* d_data, size_t size, size_t chunk_count,
+                                     size_t* chunk_sizes)
+{
+    if (!ctx || chunk_count == 0 || !chunk_sizes || (!d_data && size)) return CJ_ERR_INVALID_ARGUMENT;
+    CJ_CUDA(cudaSetDevice(ctx->device));
+    if (size == 0) {
+        for (size_t i = 0; i < chunk_count; i++) chunk_sizes[i] = 0;
+        return CJ_OK;
+    }
+    const size_t nb = (size + 65535) / 65536;
+    cj_status st;
+    if ((st = ensure(ctx, ctx->plan_counts, nb))) return st;
+    if ((st = ensure(ctx, ctx->plan_req, chunk_count + 1))) return st;
+    if ((st = ensure(ctx, ctx->plan_pos, chunk_count + 1))) return st;
+    return plan_lines_count_device(d_data, size, chunk_count, chunk_sizes, ctx->plan_counts.p, ctx->plan_req.p,
+                                   ctx->plan_pos.p, ctx->stream) == cudaSuccess ? CJ_OK : CJ_ERR_CUDA;
+}
 
 }  // extern "C"

@@ -70,6 +70,12 @@ void launch_pair(const PairParams& p, int grid, cudaStream_t stream, int threads
 void launch_spine(const PairParams& p, int grid, cudaStream_t stream, int threads = 256);
 
 // key/value queries over a staged JSON-Lines result (cj_query.cu)
+// JSON-Lines chunk plan of a device buffer (cj_plan.cu); scratch: nb =
+// ceil(size / 64 KiB) counts, chunk_count + 1 requests and positions
+cudaError_t plan_lines_count_device(const uint8_t* d_data, size_t size, size_t chunk_count,
+                                    size_t* chunk_sizes, uint32_t* d_counts, uint2* d_req,
+                                    unsigned long long* d_pos, cudaStream_t stream);
+
 cudaError_t launch_query(const uint8_t* in, const Segment* segs, uint32_t n_segs, const int32_t* pos,
                          const int32_t* pair, const uint2* brk, uint32_t S, uint32_t K, const char* key,
                          int key_len, const char* value, int value_len, int64_t n_bytes, unsigned long long* count,

@@ -325,6 +325,16 @@ cj_status cj_plan_lines_count(const uint8_t* data, size_t size, size_t chunk_cou
                               size_t* chunk_sizes);
 cj_status cj_plan_lines_bytes(const uint8_t* data, size_t size, size_t chunk_bytes,
                               size_t* chunk_sizes, size_t cap, size_t* n_chunks);
+/* cj_plan_lines_count_device: the plan of cj_plan_lines_count for a buffer
+ * already in device memory (d_data, `size` bytes), computed on the device on
+ * the context's stream -- newlines counted per 64 KiB block, then the one
+ * newline that ends each chunk's last line located in its block; only the
+ * block counts and one position per chunk cross to the host (chunk_sizes is
+ * host memory of chunk_count entries).  Replaces the host '\n' scan of
+ * loadJSONLines_chunkCount (cujson/load_file.cu:71-78) for device-resident
+ * input; the chunk boundaries are the reference's. */
+cj_status cj_plan_lines_count_device(cj_context* ctx, const uint8_t* d_data, size_t size,
+                                     size_t chunk_count, size_t* chunk_sizes);
 
 const char* cj_status_string(int status);
 /* Status of the calling thread's last drop-in parse (parse_standard_json /
