@@ -12,12 +12,14 @@ compaction, nesting/pair recognition) of the 1 GiB standard-JSON workload
                the input, parse, D2H of the verdict and the result arrays
   roofline     the dominant (scan) kernel: algorithmic bytes N + 8*S per launch
                over its CUDA-event time, against the measured HBM copy bandwidth
-  cpu_baseline the CPU restatement of the reference's algorithm (oracle/), one
-               core, on a bounded sample of the same workload
+  cpu_baseline simdjson (the copy the reference ships with its paper's related
+               work, built for this machine) on the same 1 GiB document, on
+               every host core (independent parsers), beside one core; the
+               oracle port's figure is in cpu_baseline_port
 
 ``--impl reference`` times the reference's algorithm on the host cores (the
-oracle port; the reference itself is CUDA-only and does not build on the GPU
-box), with every host thread running an independent instance.
+oracle port; the reference's own path is CUDA-only and its sources are not on
+the GPU machine): every host thread parses the same 1 GiB document per step.
 """
 from __future__ import annotations
 
@@ -33,6 +35,7 @@ import time
 from pathlib import Path
 
 import numpy as np
+from tests import synth
 
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
@@ -63,9 +66,8 @@ def parse_args():
 
 
 def workload(size: int):
-    import cujson_gb300 as cj
-    seed = cj.CONFIG_SEED_BASE + 2
-    return cj.synth_document(seed, size, max_depth=20, huge_string_frac=0.01,
+    seed = synth.CONFIG_SEED_BASE + 2
+    return synth.synth_document(seed, size, max_depth=20, huge_string_frac=0.01,
                              huge_string_min=64 << 10, huge_string_max=128 << 10)
 
 
@@ -182,8 +184,7 @@ def cpu_baseline_sample(sample_bytes: int):
     """Oracle (CPU restatement of the reference algorithm), one thread, on a
     bounded sample of the same generator; returns (GB/s, description)."""
     from oracle import cj_oracle
-    import cujson_gb300 as cj
-    d = cj.synth_document(cj.CONFIG_SEED_BASE + 2, sample_bytes, max_depth=20,
+    d = synth.synth_document(synth.CONFIG_SEED_BASE + 2, sample_bytes, max_depth=20,
                           huge_string_frac=0.01, huge_string_min=64 << 10,
                           huge_string_max=128 << 10)
     cj_oracle.parse(d[: 1 << 20])        # load + warm
@@ -198,21 +199,44 @@ def cpu_baseline_sample(sample_bytes: int):
     return gbs, f"{sample_bytes} B document from the same generator, parsed {reps}x ({t_total:.1f} s)"
 
 
+def workload_config(N: int, world: int) -> dict:
+    """The `config` object both arms print (identical for the same workload)."""
+    return {"workload": WORKLOAD, "bytes": N, "parallelism": f"replicas x{world}",
+            "l2": "input 1 GiB > 129 MB L2, no flush between steps"}
+
+
 def run_reference(args, world, rank):
-    """Reference arm: the reference's algorithm (oracle port) on all host cores."""
+    """Reference arm: the reference's algorithm restated in C (the oracle
+    port) on all host cores.  Each step, every host thread parses the whole
+    1 GiB benchmark document (independent instances over the same bytes);
+    value = threads x bytes / step time.  Loads only the oracle and the input
+    generator, nothing of the GPU library."""
     if rank != 0:
         return
     from oracle import cj_oracle
-    import cujson_gb300 as cj
     from concurrent.futures import ThreadPoolExecutor
     cores = os.cpu_count() or 1
-    sample = 64 << 20
-    d = cj.synth_document(cj.CONFIG_SEED_BASE + 2, sample, max_depth=20, huge_string_frac=0.01,
-                          huge_string_min=64 << 10, huge_string_max=128 << 10)
+    d = workload(args.size)
+    N = d.size
+    first = cj_oracle.parse(d)           # the counts, to size each thread's outputs
+    if first.flags:
+        raise SystemExit("oracle rejected the workload")
+    S = first.n_structural
+    L = cj_oracle.lib()
+    outs = [(np.zeros(S + 1, np.int32), np.zeros(S + 1, np.int32)) for _ in range(cores)]
+
+    def one(i):
+        st = cj_oracle._Stats()
+        pos, pair = outs[i]
+        L.cjo_parse(d.ctypes.data, N, 0, None, 0, pos.ctypes.data, pair.ctypes.data, S + 1,
+                    ctypes.byref(st))
+        return st.flags == 0 and st.n_structural == S
+
     ex = ThreadPoolExecutor(max_workers=cores)
 
     def step():
-        list(ex.map(lambda _: cj_oracle.parse(d).flags, range(cores)))
+        if not all(ex.map(one, range(cores))):
+            raise SystemExit("oracle result differs between runs")
 
     for _ in range(args.warmup):
         step()
@@ -220,21 +244,54 @@ def run_reference(args, world, rank):
     for _ in range(args.steps):
         step()
     dt = time.perf_counter() - t0
-    value = sample * cores * args.steps / dt / 1e9
-    desc = (f"{cores} independent instances per step, each parsing a {sample} B document of the "
-            f"same generator")
+    value = N * cores * args.steps / dt / 1e9
+    desc = (f"{cores} host threads per step, each parsing the whole {N} B benchmark document "
+            f"(independent instances over the same bytes)")
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample_bytes": sample},
+        "config": workload_config(N, world),
         "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": desc},
         "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def simdjson_baseline(data: np.ndarray):
+    """simdjson 3.2.1 (the amalgamation the reference ships under
+    paper_reproduced/related_works/simdjson/, built here for this machine by
+    oracle/build_ref.py) on the benchmark document, timed on this machine's
+    host cores: ondemand::parser::iterate (UTF-8 validation + structural
+    index, cuJSON's stages 1-2) on 1 core and on every core (independent
+    parsers over the same bytes), and dom::parser::parse (the full tape,
+    nesting included) on every core.  None when its sources are absent."""
+    import tempfile
+    from oracle import build_ref
+    try:
+        exe = build_ref.build_simdjson()
+    except Exception as e:                      # a failed build is reported, not fatal
+        return {"unavailable": f"simdjson build failed: {str(e)[-200:]}"}
+    if exe is None:
+        return None
+    cores = os.cpu_count() or 1
+    res = {}
+    with tempfile.TemporaryDirectory() as td:
+        path = Path(td) / "doc.json"
+        data.tofile(path)
+        for key, mode, threads, reps in (("index_1", "index", 1, 3), ("index_all", "index", cores, 2),
+                                         ("dom_all", "dom", cores, 1)):
+            r = subprocess.run([str(exe), str(path), mode, str(threads), str(reps)], capture_output=True,
+                               text=True, timeout=900)
+            if r.returncode != 0:
+                res[key] = None
+                continue
+            f = r.stdout.split()
+            res[key] = float(f[4])
+    return {"cores": cores, "GBps": res}
 
 
 BATCH_DOCS = 4096
@@ -252,10 +309,10 @@ def run_batch(args, local):
     """Batched documents: one graph replay parses the whole batch, against a
     loop of plain per-document parses of the same documents."""
     import cujson_gb300 as cj
-    seed = cj.CONFIG_SEED_BASE + 4
+    seed = synth.CONFIG_SEED_BASE + 4
     pin = cj.PinnedBuffer(BATCH_BYTES + (256 << 20))
     t_gen = time.perf_counter()
-    packed, sizes, kinds = cj.batch_input(seed, BATCH_DOCS, BATCH_BYTES, out=pin.array)
+    packed, sizes, kinds = synth.batch_input(seed, BATCH_DOCS, BATCH_BYTES, out=pin.array)
     t_gen = time.perf_counter() - t_gen
     n = int(sizes.size)
     N = int(sizes.sum())
@@ -368,9 +425,9 @@ def run_serve(args, local):
     server at fractions of its measured capacity, under a fixed device-memory
     budget; beside it the plain per-document loop on the same requests."""
     import cujson_gb300 as cj
-    seed = cj.CONFIG_SEED_BASE + 5
+    seed = synth.CONFIG_SEED_BASE + 5
     t_gen = time.perf_counter()
-    docs, lines, kinds = cj.serve_requests(seed, SERVE_REQUESTS)
+    docs, lines, kinds = synth.serve_requests(seed, SERVE_REQUESTS)
     t_gen = time.perf_counter() - t_gen
     # requests live in pinned memory, as a server's receive buffers would
     offs = np.concatenate([[0], np.cumsum([d.size for d in docs])])
@@ -435,7 +492,7 @@ def run_other_configs(args, local, peak):
     import cujson_gb300 as cj
     out = []
     for config in (1, 3):
-        data, info = cj.config_input(config)
+        data, info = synth.config_input(config)
         ctx = cj.Context(local)
         if info["kind"] == "lines":
             sizes = cj.plan_lines_count(data, 4)
@@ -475,7 +532,7 @@ def run_other_configs(args, local, peak):
             pin_in.close()
             pin_out.close()
         out.append({
-            "config": config, "workload": f"{info['kind']} {N} B (seed {cj.CONFIG_SEED_BASE + config:#x})",
+            "config": config, "workload": f"{info['kind']} {N} B (seed {synth.CONFIG_SEED_BASE + config:#x})",
             "structurals": S, "GBps": round(N / (span / 1e3) / 1e9, 1), "ms_per_parse": round(span, 4),
             "scan_ms": round(scan_ms / runs, 4), "scan_roofline_frac": round(B / (scan_ms / runs / 1e3) / 1e9 / peak, 4),
             "l2": "input larger than L2" if N > (129 << 20) else "input 64 MiB < 129 MB L2 (no flush: warm-L2 figure)",
@@ -522,7 +579,7 @@ def run_query(args, local):
     size = args.query_bytes or cj.MAX_INPUT_BYTES
     pin = cj.PinnedBuffer(size)
     t_gen = time.perf_counter()
-    doc, nrec, npush = cj.synth_events(QUERY_SEED, size)
+    doc, nrec, npush = synth.synth_events(QUERY_SEED, size)
     pin.array[:] = doc
     t_gen = time.perf_counter() - t_gen
     sizes = cj.plan_lines_count(doc, 4)
@@ -565,7 +622,7 @@ def run_query(args, local):
     if not args.no_cpu_baseline:
         from oracle import cj_oracle
         sample = min(size, args.cpu_sample)
-        sdoc, srec, _ = cj.synth_events(QUERY_SEED, sample)
+        sdoc, srec, _ = synth.synth_events(QUERY_SEED, sample)
         ref = cj_oracle.parse(sdoc, lines=True)
         t0 = time.perf_counter()
         reps = 0
@@ -655,18 +712,28 @@ def run_ours(args, world, rank, local, pg):
     serve = None if args.no_serve else run_serve(args, local)
     query = None if args.no_query else run_query(args, local)
     others = None if args.no_configs else run_other_configs(args, local, peak)
-    cpu = None
+    cpu, cpu_port = None, None
     if not args.no_cpu_baseline:
         v, desc = cpu_baseline_sample(args.cpu_sample)
-        cpu = {"value": round(v, 4), "unit": UNIT, "cores": 1, "kind": "port", "sample": desc}
+        cpu_port = {"value": round(v, 4), "unit": UNIT, "cores": 1, "kind": "port", "sample": desc}
+        sj = simdjson_baseline(data)
+        if sj and sj.get("GBps", {}).get("index_all"):
+            g = sj["GBps"]
+            cpu = {"value": round(g["index_all"], 3), "unit": UNIT, "cores": sj["cores"], "kind": "simdjson",
+                   "sample": (f"the {N} B benchmark document, simdjson 3.2.1 ondemand::parser::iterate "
+                              f"(UTF-8 validation + structural index) on {sj['cores']} host threads, "
+                              f"independent parsers over the same bytes"),
+                   "one_core": g.get("index_1"), "dom_parse_all_cores": g.get("dom_all")}
+        else:
+            cpu = dict(cpu_port)
+            cpu["simdjson"] = sj
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(span_max / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "bytes": N, "structurals": S, "brackets": K,
-                   "max_depth": int(inf2.max_depth), "parallelism": f"replicas x{world}",
-                   "l2": "input 1 GiB > 129 MB L2, no flush between steps"},
+        "config": workload_config(N, world),
+        "workload_stats": {"structurals": S, "brackets": K, "max_depth": int(inf2.max_depth)},
         "roofline": {"bound": "hbm", "kernel": "scan_kernel", "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "peak_kind": peak_kind, "traffic": traffic,
@@ -674,7 +741,7 @@ def run_ours(args, world, rank, local, pg):
         "phases_ms_per_step": {"scan": round(scan_ms / runs, 4), "pair": round(pair_ms / runs, 4),
                                "spine": round(spine_ms / runs, 4)},
         "parse_roofline_frac": round(B / (span_max / args.steps / 1e3) / 1e9 / peak, 4),
-        "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": ck,
+        "e2e": e2e, "cpu_baseline": cpu, "cpu_baseline_port": cpu_port, "gpu_launches": int(launches), "clocks": ck,
         "batch": batch, "serving": serve, "query": query, "other_configs": others,
     }
     print(json.dumps(line), flush=True)

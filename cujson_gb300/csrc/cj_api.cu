@@ -107,6 +107,7 @@ struct cj_context {
     // which hands out a tile only once d_ready covers its bytes
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_reset = nullptr, ev_copied = nullptr;
+    cudaEvent_t ev_plan = nullptr;      // orders the device planner after the caller's stream
     unsigned long long* d_ready = nullptr;
     bool overlap_run = false;
     uint32_t input_wait_limit = 0;      // 0: the kernel's default
@@ -855,6 +856,7 @@ cj_status cj_context_create(int device, cj_context** out)
         cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_reset, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_copied, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_plan, cudaEventDisableTiming) != cudaSuccess ||
         cudaMalloc((void**)&ctx->d_ready, sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc((void**)&ctx->d_ctrl, sizeof(Ctrl)) != cudaSuccess) {
         cj_context_destroy(ctx);
@@ -895,6 +897,7 @@ void cj_context_destroy(cj_context* ctx)
     if (ctx->d_ready) cudaFree(ctx->d_ready);
     if (ctx->ev_reset) cudaEventDestroy(ctx->ev_reset);
     if (ctx->ev_copied) cudaEventDestroy(ctx->ev_copied);
+    if (ctx->ev_plan) cudaEventDestroy(ctx->ev_plan);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->d_ctrl) cudaFree(ctx->d_ctrl);
     if (ctx->h_ctrl) cudaFreeHost(ctx->h_ctrl);
@@ -1319,7 +1322,7 @@ void cj_set_last_status(int status) { g_last_status = status; }
 const char* cj_last_error(void) { return cj_status_string(g_last_status); }
 
 cj_status cj_plan_lines_count_device(cj_context* ctx, const uint8_t* d_data, size_t size, size_t chunk_count,
-                                     size_t* chunk_sizes)
+                                     size_t* chunk_sizes, void* stream)
 {
     if (!ctx || chunk_count == 0 || !chunk_sizes || (!d_data && size)) return CJ_ERR_INVALID_ARGUMENT;
     CJ_CUDA(cudaSetDevice(ctx->device));
@@ -1327,6 +1330,10 @@ cj_status cj_plan_lines_count_device(cj_context* ctx, const uint8_t* d_data, siz
         for (size_t i = 0; i < chunk_count; i++) chunk_sizes[i] = 0;
         return CJ_OK;
     }
+    // the planner runs on the context stream, after the work queued so far on
+    // `stream` (the one that fills d_data; NULL: the legacy default stream)
+    CJ_CUDA(cudaEventRecord(ctx->ev_plan, (cudaStream_t)stream));
+    CJ_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_plan, 0));
     const size_t nb = (size + 65535) / 65536;
     cj_status st;
     if ((st = ensure(ctx, ctx->plan_counts, nb))) return st;

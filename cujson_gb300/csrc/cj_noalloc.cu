@@ -94,11 +94,13 @@ __global__ void noalloc_setup(Scratch* s, uint64_t n)
 
 // Reference layout into the caller's buffer: [0]=0, [1..S] positions,
 // [S+1]=S+1, [S+2..2S+1] pair row, [2S+2], [2S+3] = 0.  Writes nothing when
-// 2S+4 entries do not fit.
+// 2S+4 entries do not fit, or when the document is invalid (any error flag,
+// or a close below depth 0; the pairing kernels before it have set them all).
 __global__ void noalloc_layout(const Scratch* s, int32_t* out, uint64_t cap)
 {
     const uint64_t S = s->ctrl.s_total;
     if (S > kScap - 1 || 2 * S + 4 > cap) return;
+    if (s->ctrl.error_flags != 0u || s->ctrl.neg_min_level > 0) return;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < S + 2; i += stride) {
         int32_t p, q;
@@ -144,8 +146,11 @@ cj_status device_setup(int dev, cudaStream_t stream, DeviceState& d)
         per_sm < 1)
         return CJ_ERR_CUDA;
     Scratch* s = static_cast<Scratch*>(ptr);
+    // cleared and finished before the call goes on, so no later call, on any
+    // stream, can run beside these clears
     if (cudaMemsetAsync(s->desc_flag, 0, sizeof(s->desc_flag), stream) != cudaSuccess ||
-        cudaMemsetAsync(s->tree, 0, sizeof(s->tree), stream) != cudaSuccess)
+        cudaMemsetAsync(s->tree, 0, sizeof(s->tree), stream) != cudaSuccess ||
+        cudaStreamSynchronize(stream) != cudaSuccess)
         return CJ_ERR_CUDA;
     d.scratch = s;
     d.scan_grid = (uint32_t)(per_sm * d.sm_count);
@@ -178,7 +183,8 @@ cj_status parse_noalloc(const uint8_t* d_data, size_t size, int32_t* d_out, size
         if (d->epoch == 0) {
             Scratch* s = d->scratch;
             if (cudaMemsetAsync(s->desc_flag, 0, sizeof(s->desc_flag), stream) != cudaSuccess ||
-                cudaMemsetAsync(s->tree, 0, sizeof(s->tree), stream) != cudaSuccess)
+                cudaMemsetAsync(s->tree, 0, sizeof(s->tree), stream) != cudaSuccess ||
+                cudaStreamSynchronize(stream) != cudaSuccess)
                 return CJ_ERR_CUDA;
             d->epoch = 1;
         }

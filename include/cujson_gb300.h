@@ -137,13 +137,17 @@ cj_status cj_parse_into(cj_context* ctx, const uint8_t* host_data, size_t size, 
  * __device__ array of the library, sized for documents of at most
  * CJ_NOALLOC_MAX_BYTES (about 21 MiB of device memory).  Larger documents are
  * refused with CJ_ERR_TOO_LARGE; an `out_cap` under 2*(S+2) with
- * CJ_ERR_CAPACITY (nothing is written to `d_out` then).  Returns once the
- * parse has finished, with `info` filled and the verdict as the status.
+ * CJ_ERR_CAPACITY.  Returns once the parse has finished, with `info` filled
+ * and the verdict as the status.  `d_out` is written only when the status is
+ * CJ_OK: after an invalid document (CJ_ERR_INVALID_UTF8,
+ * CJ_ERR_INVALID_BRACKETS, CJ_ERR_TIMEOUT) or a refusal it holds what it held
+ * before the call.
  *
- * The first call on each device resolves the scratch address and sets up the
- * kernels; make that first call before any stream capture.  All calls on one
- * device share the scratch: calls must not overlap (two in flight at once,
- * from two host threads or on two unordered streams, race on it). */
+ * The first call on each device resolves the scratch address, sets up the
+ * kernels and clears the scratch (waiting for the clear to finish); make that
+ * first call before any stream capture.  All calls on one device share the
+ * scratch: calls must not overlap -- two in flight at once, from two host
+ * threads or on two streams without ordering between them, race on it. */
 #define CJ_NOALLOC_MAX_BYTES 1048576ull
 cj_status cj_parse_standard_noalloc(const uint8_t* d_data, size_t size, int32_t* d_out,
                                     size_t out_cap, cj_parse_info* info, void* stream);
@@ -330,11 +334,16 @@ cj_status cj_plan_lines_bytes(const uint8_t* data, size_t size, size_t chunk_byt
  * the context's stream -- newlines counted per 64 KiB block, then the one
  * newline that ends each chunk's last line located in its block; only the
  * block counts and one position per chunk cross to the host (chunk_sizes is
- * host memory of chunk_count entries).  Replaces the host '\n' scan of
- * loadJSONLines_chunkCount (cujson/load_file.cu:71-78) for device-resident
- * input; the chunk boundaries are the reference's. */
+ * host memory of chunk_count entries).  `stream` (a cudaStream_t; NULL = the
+ * legacy default stream) is the stream whose work fills d_data: the planner
+ * reads d_data only after everything queued on it before this call, so a
+ * buffer still being written by an asynchronous copy or kernel there is
+ * planned correctly.  Returns after the plan is on the host.  Replaces the
+ * host '\n' scan of loadJSONLines_chunkCount (cujson/load_file.cu:71-78) for
+ * device-resident input; the chunk boundaries are the reference's
+ * (tests/test_plan_golden.py). */
 cj_status cj_plan_lines_count_device(cj_context* ctx, const uint8_t* d_data, size_t size,
-                                     size_t chunk_count, size_t* chunk_sizes);
+                                     size_t chunk_count, size_t* chunk_sizes, void* stream);
 
 const char* cj_status_string(int status);
 /* Status of the calling thread's last drop-in parse (parse_standard_json /
@@ -346,31 +355,6 @@ void cj_set_last_status(int status);
  * reference printed a reason and called exit(0) (parse_standard_json.cu,
  * parse_json_lines.cu on invalid input), a caller reads it here. */
 const char* cj_last_error(void);
-
-/* ---- synthetic inputs -------------------------------------------------------
- * Seeded generators standing in for the reference's evaluation datasets (not
- * available offline).  Deterministic for a given seed on every machine. */
-typedef struct cj_synth_params {
-    int32_t  max_depth;          /* nesting limit of values */
-    int32_t  keys_min, keys_max; /* members per top-level object */
-    int32_t  nested_max_items;   /* members / elements per nested container */
-    int32_t  str_min, str_max;   /* string lengths */
-    double   huge_string_frac;   /* fraction of strings that are huge */
-    int64_t  huge_string_min, huge_string_max;
-    uint64_t block_bytes;        /* independent generation block */
-    double   record_median, record_sigma;   /* JSON-Lines lognormal sizes */
-    int64_t  record_min, record_max;
-    uint32_t threads;            /* 0 = all host threads */
-} cj_synth_params;
-
-void   cj_synth_default_params(cj_synth_params* p);
-size_t cj_synth_document(uint64_t seed, size_t size, const cj_synth_params* p, uint8_t* out);
-size_t cj_synth_lines(uint64_t seed, size_t size, const cj_synth_params* p, uint8_t* out,
-                      uint64_t* n_records);
-size_t cj_synth_events(uint64_t seed, size_t size, uint8_t* out, uint64_t* n_records, uint64_t* n_push);
-size_t cj_synth_deep(size_t depth, uint8_t* out);
-size_t cj_synth_backslash_string(uint64_t seed, size_t body, uint8_t* out);
-int    cj_synth_corrupt(uint8_t* doc, size_t n, int kind, uint64_t seed);
 
 #ifdef __cplusplus
 }

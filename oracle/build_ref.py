@@ -21,6 +21,12 @@ What it builds (each only when the reference tree is present):
   launch function.  Its outputs are the golden parse vectors under
   tests/golden/.
 
+* ref_loader -- the reference's JSON-Lines loaders (cujson/load_file.cu:
+  loadJSONLines_chunkCount, _chunkSizeBytes, _chunkSizeMegaBytes) compiled
+  unchanged with g++ against the same cuda_runtime.h stand-in, driven by
+  oracle/refemu/load_driver.cpp.  Its chunk plans are the golden plans under
+  tests/golden/ and the chunk sizes of every JSON-Lines golden case.
+
 usage: python oracle/build_ref.py [reference root]
 """
 from __future__ import annotations
@@ -37,7 +43,9 @@ HERE = Path(__file__).resolve().parent
 REPO = HERE.parent
 OUT = HERE / "_ref"
 DRIVER = REPO / "tests" / "dropin" / "iter_driver.cpp"
-DEFAULT_REF = Path(os.environ.get("CUJSON_REFERENCE", "/root/reference"))
+# the reference tree: $CUJSON_REFERENCE, else a checkout named "reference"
+# beside this repository
+DEFAULT_REF = Path(os.environ.get("CUJSON_REFERENCE", str(REPO.parent / "reference")))
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 
 
@@ -133,6 +141,22 @@ def build_refemu(ref: Path, force: bool = False) -> dict:
     return out
 
 
+def build_loader(ref: Path, force: bool = False) -> Path:
+    """oracle/_ref/ref_loader: the reference's load_file.cu, as it lies, with
+    oracle/refemu/load_driver.cpp."""
+    src = ref / "cujson" / "load_file.cu"
+    drv = EMU / "load_driver.cpp"
+    exe = OUT / "ref_loader"
+    newest = max(p.stat().st_mtime for p in (src, drv, EMU / "shim" / "cuda_runtime.h", EMU / "cj_cuda_emu.h"))
+    if force or not exe.exists() or exe.stat().st_mtime < newest:
+        cmd = ["g++", "-std=c++17", "-O2", "-w", f"-I{EMU / 'shim'}", f"-I{ref / 'cujson'}", str(drv),
+               "-o", str(exe)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference loader build failed:\n{r.stderr[-4000:]}")
+    return exe
+
+
 def build(ref: Path = DEFAULT_REF, force: bool = False) -> dict:
     """Build what the reference tree allows; returns {name: path}."""
     if not (ref / "cujson" / "query").is_dir():
@@ -153,26 +177,60 @@ def build(ref: Path = DEFAULT_REF, force: bool = False) -> dict:
                 raise RuntimeError(f"reference iterator build failed:\n{r.stderr}")
         built[name] = exe
     built.update(build_refemu(ref, force))
+    built["ref_loader"] = build_loader(ref, force)
+    copy_simdjson_sources(ref)
     return built
+
+
+SIMDJSON_SRC = OUT / "simdjson_src"   # the amalgamation, copied beside the built checkers
+
+
+def copy_simdjson_sources(ref: Path = DEFAULT_REF) -> bool:
+    """Copy the simdjson amalgamation the reference ships
+    (paper_reproduced/related_works/simdjson/simdjson.{h,cpp}, Apache-2.0, the
+    licence text is in the header) into oracle/_ref/simdjson_src, which is not
+    committed but travels with the working tree to machines without the
+    reference tree, so that simdjson can be built and timed on their cores.
+    False when the reference tree is absent."""
+    sj = ref / "paper_reproduced" / "related_works" / "simdjson"
+    if not (sj / "simdjson.cpp").is_file():
+        return False
+    SIMDJSON_SRC.mkdir(parents=True, exist_ok=True)
+    for name in ("simdjson.h", "simdjson.cpp"):
+        dst = SIMDJSON_SRC / name
+        if not dst.exists() or dst.stat().st_mtime < (sj / name).stat().st_mtime:
+            shutil.copy2(sj / name, dst)
+    return True
 
 
 def build_simdjson(ref: Path = DEFAULT_REF, force: bool = False):
     """oracle/_ref/simdjson_bench: oracle/simdjson_driver.cpp with the simdjson
     amalgamation the reference ships (paper_reproduced/related_works/simdjson/),
-    compiled where it lies; None when the reference tree is absent.  Built on
-    request only (timing a related CPU parser, not a checker)."""
+    compiled from the reference tree or, without it, from the copy in
+    oracle/_ref/simdjson_src; None when neither exists.  Built on request only
+    (timing a related CPU parser, not a checker); the build is for the machine
+    it runs on (NEON on Arm, the x86 kernels elsewhere)."""
     sj = ref / "paper_reproduced" / "related_works" / "simdjson"
+    if not (sj / "simdjson.cpp").is_file():
+        sj = SIMDJSON_SRC
     if not (sj / "simdjson.cpp").is_file():
         return None
     OUT.mkdir(parents=True, exist_ok=True)
     exe = OUT / "simdjson_bench"
     drv = HERE / "simdjson_driver.cpp"
-    if force or not exe.exists() or exe.stat().st_mtime < drv.stat().st_mtime:
+    # an executable copied from another machine is not reused: the stamp names the one it was built on
+    stamp = OUT / "simdjson_bench.machine"
+    import platform
+    here = f"{platform.machine()} {platform.node()}"
+    fresh = exe.exists() and stamp.exists() and stamp.read_text() == here and \
+        exe.stat().st_mtime >= max(drv.stat().st_mtime, (sj / "simdjson.cpp").stat().st_mtime)
+    if force or not fresh:
         cmd = ["g++", "-std=c++17", "-O3", "-DNDEBUG", "-w", f"-I{sj}", str(drv), str(sj / "simdjson.cpp"),
                "-o", str(exe), "-pthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"simdjson build failed:\n{r.stderr[-3000:]}")
+        stamp.write_text(here)
     return exe
 
 

@@ -21,8 +21,8 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent))
 
-import cujson_gb300 as cj  # noqa: E402  (host-only generators)
 from oracle import build_ref  # noqa: E402
+from tests import synth  # noqa: E402  (seeded inputs)
 
 
 def cpu_name() -> str:
@@ -53,9 +53,9 @@ def main():
     with tempfile.TemporaryDirectory() as td:
         td = Path(td)
         docs = [
-            ("standard JSON 64 MiB (config 1 generator)", cj.config_input(1)[0], ["dom", "index"]),
-            ("standard JSON 1 GiB (config 2 generator)", cj.config_input(2)[0], ["dom", "index"]),
-            ("JSON Lines 256 MiB (config 3 generator)", cj.synth_lines(cj.CONFIG_SEED_BASE + 3, 256 << 20)[0],
+            ("standard JSON 64 MiB (config 1 generator)", synth.config_input(1)[0], ["dom", "index"]),
+            ("standard JSON 1 GiB (config 2 generator)", synth.config_input(2)[0], ["dom", "index"]),
+            ("JSON Lines 256 MiB (config 3 generator)", synth.synth_lines(synth.CONFIG_SEED_BASE + 3, 256 << 20)[0],
              ["lines"]),
         ]
         for name, data, modes in docs:

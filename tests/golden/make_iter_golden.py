@@ -29,9 +29,10 @@ HERE = Path(__file__).resolve().parent
 REPO = HERE.parent.parent
 sys.path.insert(0, str(REPO))
 
-import cujson_gb300 as cj  # noqa: E402  (host-only generators)
 from oracle import build_ref, cj_oracle  # noqa: E402
+from tests.golden.make_plan_golden import ref_chunk_sizes  # noqa: E402
 from tests.dropin import build as dropin_build  # noqa: E402
+from tests import synth  # noqa: E402  (seeded inputs)
 
 OUT = HERE / "iter_golden.json"
 
@@ -177,17 +178,17 @@ def cases():
         out.append((f"hand_lines_{i}", d, True, [len(d)]))
     for i, seed in enumerate([11, 12, 13, 14]):
         size = [1024, 2048, 4096, 6144][i]
-        d = bytes(cj.synth_document(0xC0DE1000 + seed, size, max_depth=6))
+        d = bytes(synth.synth_document(0xC0DE1000 + seed, size, max_depth=6))
         out.append((f"synth_std_{size}", d, False, None))
     for i, seed in enumerate([21, 22, 23]):
         size = [1500, 3000, 5000][i]
-        d = bytes(cj.synth_lines(0xC0DE2000 + seed, size)[0])
+        d = bytes(synth.synth_lines(0xC0DE2000 + seed, size)[0])
         nchunks = [1, 2, 3][i]
-        sizes = cj.plan_lines_count(np.frombuffer(d, np.uint8), nchunks)
+        sizes = ref_chunk_sizes(np.frombuffer(d, np.uint8), nchunks)
         out.append((f"synth_lines_{size}_c{nchunks}", d, True, sizes))
     # a hand document split into several chunks
     d = HAND_LINES[0]
-    out.append(("hand_lines_0_c2", d, True, cj.plan_lines_count(np.frombuffer(d, np.uint8), 2)))
+    out.append(("hand_lines_0_c2", d, True, ref_chunk_sizes(np.frombuffer(d, np.uint8), 2)))
     return rng, out
 
 

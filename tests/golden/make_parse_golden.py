@@ -29,8 +29,9 @@ HERE = Path(__file__).resolve().parent
 REPO = HERE.parent.parent
 sys.path.insert(0, str(REPO))
 
-import cujson_gb300 as cj  # noqa: E402  (host-only generators)
 from oracle import build_ref  # noqa: E402
+from tests.golden.make_plan_golden import ref_chunk_sizes  # noqa: E402
+from tests import synth  # noqa: E402  (seeded inputs)
 
 OUT = HERE / "parse_golden.json"
 
@@ -71,25 +72,26 @@ SYNTH = [
 # seeded documents with one planted error (the reference's verdict is recorded
 # as observed; its UTF-8 predicate misses some classes)
 CORRUPT = [
-    ("bad_overlong2", dict(seed=0x601D0010, size=5000, max_depth=6), cj.CORRUPT_OVERLONG2),
-    ("bad_overlong3", dict(seed=0x601D0011, size=5000, max_depth=6), cj.CORRUPT_OVERLONG3),
-    ("bad_surrogate", dict(seed=0x601D0012, size=5000, max_depth=6), cj.CORRUPT_SURROGATE),
-    ("bad_unbalanced", dict(seed=0x601D0013, size=5000, max_depth=6), cj.CORRUPT_UNBALANCED),
-    ("bad_mismatched", dict(seed=0x601D0014, size=5000, max_depth=6), cj.CORRUPT_MISMATCHED),
+    ("bad_overlong2", dict(seed=0x601D0010, size=5000, max_depth=6), synth.CORRUPT_OVERLONG2),
+    ("bad_overlong3", dict(seed=0x601D0011, size=5000, max_depth=6), synth.CORRUPT_OVERLONG3),
+    ("bad_surrogate", dict(seed=0x601D0012, size=5000, max_depth=6), synth.CORRUPT_SURROGATE),
+    ("bad_unbalanced", dict(seed=0x601D0013, size=5000, max_depth=6), synth.CORRUPT_UNBALANCED),
+    ("bad_mismatched", dict(seed=0x601D0014, size=5000, max_depth=6), synth.CORRUPT_MISMATCHED),
 ]
 
 
 def make_input(kind: str, args: dict):
     """(bytes, chunk sizes or None) for a case; also used by the tests."""
     if kind == "document":
-        return cj.synth_document(**args), None
+        return synth.synth_document(**args), None
     if kind == "backslash":
-        return cj.synth_backslash_string(args["seed"], args["body"]), None
+        return synth.synth_backslash_string(args["seed"], args["body"]), None
     if kind == "deep":
-        return cj.synth_deep(args["depth"]), None
+        return synth.synth_deep(args["depth"]), None
     if kind == "lines":
-        d, _ = cj.synth_lines(args["seed"], args["size"])
-        return d, cj.plan_lines_count(d, args["chunks"])
+        # the chunk sizes are the reference loader's, stored with the case
+        d, _ = synth.synth_lines(args["seed"], args["size"])
+        return d, None
     raise ValueError(kind)
 
 
@@ -131,11 +133,12 @@ def main():
         add("hand_lines", "hand", {"b64": base64.b64encode(b'{"a":1}\n[2,3]\n"x"\n{"b":{"c":[]}}\n').decode()},
             np.frombuffer(b'{"a":1}\n[2,3]\n"x"\n{"b":{"c":[]}}\n', np.uint8), [14, 19])
         for name, kind, args in SYNTH:
-            data, chunks = make_input(kind, args)
-            add(name, kind, {"args": args}, data, [int(c) for c in chunks] if chunks is not None else None)
+            data, _ = make_input(kind, args)
+            chunks = ref_chunk_sizes(data, args["chunks"]) if kind == "lines" else None
+            add(name, kind, {"args": args}, data, chunks)
         for name, args, k in CORRUPT:
             data, _ = make_input("document", args)
-            assert cj.synth_corrupt(data, k, args["seed"])
+            assert synth.synth_corrupt(data, k, args["seed"])
             add(name, "corrupt", {"args": args, "corrupt": k}, data, None)
     OUT.write_text(json.dumps({"generator": "tests/golden/make_parse_golden.py",
                                "source": "reference cujson parse path, CPU emulation (oracle/build_ref.py)",

@@ -28,9 +28,10 @@ HERE = Path(__file__).resolve().parent
 REPO = HERE.parent.parent
 sys.path.insert(0, str(REPO))
 
-import cujson_gb300 as cj  # noqa: E402  (host-only generators)
 from oracle import build_ref, cj_oracle  # noqa: E402
+from tests.golden.make_plan_golden import ref_chunk_sizes  # noqa: E402
 from tests.golden.make_iter_golden import layout_words, run_driver  # noqa: E402
+from tests import synth  # noqa: E402  (seeded inputs)
 
 OUT = HERE / "query_golden.json"
 
@@ -82,10 +83,10 @@ def cases():
     out = []
     for name, d in HAND.items():
         out.append((name, d, [len(d)]))
-    d = bytes(cj.synth_events(0xC0DE5001, 256 << 10)[0])
+    d = bytes(synth.synth_events(0xC0DE5001, 256 << 10)[0])
     out.append(("events_256k", d, [len(d)]))
-    d = bytes(cj.synth_events(0xC0DE5002, 192 << 10)[0])
-    out.append(("events_192k_c3", d, cj.plan_lines_count(np.frombuffer(d, np.uint8), 3)))
+    d = bytes(synth.synth_events(0xC0DE5002, 192 << 10)[0])
+    out.append(("events_192k_c3", d, ref_chunk_sizes(np.frombuffer(d, np.uint8), 3)))
     return out
 
 

@@ -7,7 +7,7 @@
 // workloads need.  Everything is derived from one 64-bit seed through
 // std::mt19937_64, block by block, so output is identical on every machine and
 // for any thread count.
-#include "cujson_gb300.h"
+#include "cj_synth.h"
 
 #include <algorithm>
 #include <atomic>

@@ -5,6 +5,7 @@ import re
 from pathlib import Path
 
 import numpy as np
+from tests import synth
 
 ROOT = Path(__file__).resolve().parent.parent
 
@@ -33,8 +34,8 @@ def test_status_strings(cj):
 
 
 def test_generator_deterministic(cj, oracle):
-    a = cj.synth_document(cj.CONFIG_SEED_BASE + 1, 3 << 20, max_depth=6, threads=1)
-    b = cj.synth_document(cj.CONFIG_SEED_BASE + 1, 3 << 20, max_depth=6, threads=8)
+    a = synth.synth_document(synth.CONFIG_SEED_BASE + 1, 3 << 20, max_depth=6, threads=1)
+    b = synth.synth_document(synth.CONFIG_SEED_BASE + 1, 3 << 20, max_depth=6, threads=8)
     assert np.array_equal(a, b)
     r = oracle.parse(a)
     assert r.flags == 0 and r.max_depth <= 8
@@ -42,7 +43,7 @@ def test_generator_deterministic(cj, oracle):
 
 
 def test_generator_lines(cj, oracle):
-    d, n = cj.synth_lines(3, 1 << 20)
+    d, n = synth.synth_lines(3, 1 << 20)
     assert d[-1] == 10 and n > 1000
     assert oracle.parse(d, lines=True).flags == 0
     sizes = np.diff(np.flatnonzero(np.concatenate([[10], d])[:-1] == 10))
@@ -52,8 +53,8 @@ def test_generator_lines(cj, oracle):
 def test_corrupt_kinds(cj, oracle):
     for kind, bit in [(1, oracle.ERR_UTF8), (2, oracle.ERR_UTF8), (3, oracle.ERR_UTF8),
                       (4, oracle.ERR_BRACKETS), (5, oracle.ERR_BRACKETS)]:
-        d = cj.synth_document(kind, 20000)
-        assert cj.synth_corrupt(d, kind, 9)
+        d = synth.synth_document(kind, 20000)
+        assert synth.synth_corrupt(d, kind, 9)
         assert oracle.parse(d).flags & bit
 
 

@@ -18,11 +18,14 @@ from pathlib import Path
 import numpy as np
 import pytest
 
+from oracle import build_ref
+
 from tests.dropin import build as dropin_build
+from tests import synth
 
 REPO = Path(__file__).resolve().parent.parent
 GOLDEN = REPO / "tests" / "golden" / "iter_golden.json"
-REFERENCE = Path("/root/reference")
+REFERENCE = build_ref.DEFAULT_REF
 
 
 def compact(line: str) -> str:
@@ -167,12 +170,12 @@ def test_example_program_on_gpu(cj, oracle, tmp_path, mode, arg):
     exe = dropin_build.build_example(Path(cj.lib()._name).parent)
     f = tmp_path / "doc.json"
     if mode == "std":
-        doc = cj.synth_document(0xD0C0001, 3 << 20, max_depth=12)
+        doc = synth.synth_document(0xD0C0001, 3 << 20, max_depth=12)
         f.write_bytes(doc.tobytes())
         args = [str(exe), mode, str(f), str(tmp_path / "out.bin")]
         ref = oracle.parse(doc)
     else:
-        doc, _ = cj.synth_lines(0xD0C0002, 3 << 20)
+        doc, _ = synth.synth_lines(0xD0C0002, 3 << 20)
         f.write_bytes(doc.tobytes())
         args = [str(exe), mode, str(f), str(arg), str(tmp_path / "out.bin")]
         sizes = (cj.plan_lines_count(doc, arg) if mode == "lines"

@@ -4,6 +4,7 @@ per-document verdicts, graph replays and autotuned launch shapes giving the
 same results."""
 import numpy as np
 import pytest
+from tests import synth
 
 pytestmark = pytest.mark.gpu
 
@@ -27,15 +28,15 @@ def mixed_docs(cj, seed=7):
         b"1", b"[]", b'{"a":"b\\"c,d"}', b"[[[", b"[1,[2]]", b"]]", b"{}", b"[{]}", b"[]",
         b'"\\\\"', b"   ", b'{"k":[{},[]],"x":{}}', b"\xc0\x80", b'["\xed\xa0\x80"]', b"[\"\xe2\x82\xac\"]")]
     for k, n in enumerate([1023, 1024, 1025, 4095, 65536, 114687, 114688, 114689, 131072, 300001, 1 << 20]):
-        docs.append(cj.synth_document(seed * 100 + k, n, max_depth=10))
-    bad = cj.synth_document(seed * 100 + 50, 200000)
-    assert cj.synth_corrupt(bad, cj.CORRUPT_SURROGATE, 3)
+        docs.append(synth.synth_document(seed * 100 + k, n, max_depth=10))
+    bad = synth.synth_document(seed * 100 + 50, 200000)
+    assert synth.synth_corrupt(bad, synth.CORRUPT_SURROGATE, 3)
     docs.append(bad)
-    bad2 = cj.synth_document(seed * 100 + 51, 150000)
-    assert cj.synth_corrupt(bad2, cj.CORRUPT_MISMATCHED, 3)
+    bad2 = synth.synth_document(seed * 100 + 51, 150000)
+    assert synth.synth_corrupt(bad2, synth.CORRUPT_MISMATCHED, 3)
     docs.append(bad2)
-    docs.append(cj.synth_deep(100000))
-    docs.append(cj.synth_backslash_string(seed, 300000))
+    docs.append(synth.synth_deep(100000))
+    docs.append(synth.synth_backslash_string(seed, 300000))
     return docs
 
 
@@ -72,7 +73,7 @@ def test_batch_same_alone_and_in_the_mix(cj, ctx):
 
 
 def test_batch_generated(cj, oracle, ctx):
-    packed, sizes, kinds = cj.batch_input(0xC0DE1004, 300, 96 << 20)
+    packed, sizes, kinds = synth.batch_input(0xC0DE1004, 300, 96 << 20)
     ctx.stage_batch_packed(packed, sizes)
     ctx.run_graph()
     res = ctx.batch_results()
@@ -83,7 +84,7 @@ def test_batch_generated(cj, oracle, ctx):
 
 
 def test_autotune_keeps_results(cj, oracle, ctx):
-    packed, sizes, _ = cj.batch_input(0xC0DE2004, 64, 16 << 20)
+    packed, sizes, _ = synth.batch_input(0xC0DE2004, 64, 16 << 20)
     ctx.stage_batch_packed(packed, sizes)
     ctx.run_graph()
     want = ctx.batch_layout()[0].copy()
@@ -96,7 +97,7 @@ def test_autotune_keeps_results(cj, oracle, ctx):
 
 
 def test_single_document_after_batch(cj, oracle, ctx):
-    d = cj.synth_document(1234, 500000)
+    d = synth.synth_document(1234, 500000)
     st, res = ctx.try_parse(d)
     assert st == cj.OK
     np.testing.assert_array_equal(res.buffer, oracle.parse(d).reference_layout())
@@ -136,7 +137,7 @@ def test_padded_batch_overlapped(cj, oracle, ctx):
 def test_padded_batch_full_size(cj, ctx):
     """Config 4 (4096 documents, 2 GiB, 1 % invalid UTF-8, 1 % bad brackets)
     through the overlapped padded path: identical to the packed graph path."""
-    packed, sizes, kinds = cj.batch_input(cj.CONFIG_SEED_BASE + 4, 4096, 2 << 30)
+    packed, sizes, kinds = synth.batch_input(synth.CONFIG_SEED_BASE + 4, 4096, 2 << 30)
     ctx.stage_batch_packed(packed, sizes)
     ctx.run_graph()
     want, wst, wS, wd, woff = ctx.batch_layout()

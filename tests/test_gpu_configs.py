@@ -5,6 +5,7 @@ open to a later close of the same kind, JSON-Lines records split at their
 newline entries."""
 import numpy as np
 import pytest
+from tests import synth
 
 pytestmark = pytest.mark.gpu
 
@@ -31,7 +32,7 @@ def check_properties(doc: np.ndarray, res, lines: bool):
 
 
 def test_config1_64mib(cj, oracle, ctx):
-    doc, _ = cj.config_input(1)
+    doc, _ = synth.config_input(1)
     res = ctx.parse_standard_json(doc)
     ref = oracle.parse(doc)
     assert ref.valid
@@ -40,7 +41,7 @@ def test_config1_64mib(cj, oracle, ctx):
 
 
 def test_config2_1gib(cj, oracle, ctx):
-    doc, _ = cj.config_input(2)
+    doc, _ = synth.config_input(2)
     res = ctx.parse_standard_json(doc)
     ref = oracle.parse(doc)
     assert ref.valid
@@ -51,7 +52,7 @@ def test_config2_1gib(cj, oracle, ctx):
 
 
 def test_config3_2gb_lines(cj, oracle, ctx):
-    doc, info = cj.config_input(3)
+    doc, info = synth.config_input(3)
     assert doc.size == cj.MAX_INPUT_BYTES
     sizes = cj.plan_lines_count(doc, 4)
     offs = np.concatenate([[0], np.cumsum(sizes)])
@@ -69,7 +70,7 @@ def test_config3_2gb_lines(cj, oracle, ctx):
 
 
 def test_config4_batch_full(cj, oracle, ctx):
-    packed, sizes, kinds = cj.batch_input(cj.CONFIG_SEED_BASE + 4, 4096, 2 << 30)
+    packed, sizes, kinds = synth.batch_input(synth.CONFIG_SEED_BASE + 4, 4096, 2 << 30)
     ctx.stage_batch_packed(packed, sizes)
     ctx.run_graph()
     layout, status, S, depth, off = ctx.batch_layout()
@@ -89,7 +90,7 @@ def test_overlapped_copy_pinned(cj, oracle, ctx):
     """One-shot parses of pinned inputs of 64 MiB and more copy the input on a
     second stream while the scan runs; results equal the oracle's and the
     staged (copy-then-run) path's."""
-    doc = cj.synth_document(0x0E71A9, (80 << 20) + 12345, max_depth=12)
+    doc = synth.synth_document(0x0E71A9, (80 << 20) + 12345, max_depth=12)
     pin = cj.PinnedBuffer(doc.size)
     pin.array[:] = doc
     ref = oracle.parse(doc)
@@ -103,7 +104,7 @@ def test_overlapped_copy_pinned(cj, oracle, ctx):
     ctx.run()
     np.testing.assert_array_equal(ctx.staged_result().buffer, res.buffer)
     pin.close()
-    lines, _ = cj.synth_lines(0x0E71AA, 96 << 20)
+    lines, _ = synth.synth_lines(0x0E71AA, 96 << 20)
     pl = cj.PinnedBuffer(lines.size)
     pl.array[:] = lines
     sizes = cj.plan_lines_count(lines, 3)

@@ -1,6 +1,7 @@
 """GPU parse vs the oracle, through the C ABI (bit-exact; integer outputs)."""
 import numpy as np
 import pytest
+from tests import synth
 
 pytestmark = pytest.mark.gpu
 
@@ -26,7 +27,7 @@ def test_small(ctx, oracle, doc):
                                114687, 114688, 114689, 131071, 131072, 131073, 229377, 300001,
                                344064, 1 << 21])
 def test_sizes(cj, ctx, oracle, n):
-    d = cj.synth_document(n, n) if n >= 2 else np.frombuffer(b"1", np.uint8)
+    d = synth.synth_document(n, n) if n >= 2 else np.frombuffer(b"1", np.uint8)
     st, res = ctx.try_parse(d)
     ref = oracle.parse(d)
     assert st == 0 and ref.flags == 0
@@ -36,26 +37,46 @@ def test_sizes(cj, ctx, oracle, n):
 @pytest.mark.parametrize("seed", range(8))
 def test_documents(cj, ctx, oracle, seed):
     n = [5000, 70000, 1 << 20, 3 << 20, 123457, 9999, 2 << 20, 777777][seed]
-    d = cj.synth_document(2000 + seed, n, max_depth=10)
+    d = synth.synth_document(2000 + seed, n, max_depth=10)
     res = ctx.parse_standard_json(d)
     assert_same(res, oracle.parse(d))
 
 
 def test_huge_strings(cj, ctx, oracle):
-    d = cj.synth_document(78, 4 << 20, max_depth=20, huge_string_frac=0.05,
+    d = synth.synth_document(78, 4 << 20, max_depth=20, huge_string_frac=0.05,
                           huge_string_min=20000, huge_string_max=90000)
     assert_same(ctx.parse_standard_json(d), oracle.parse(d))
 
 
 @pytest.mark.parametrize("seed", range(3))
 def test_backslash_runs(cj, ctx, oracle, seed):
-    d = cj.synth_backslash_string(seed, 200000 + 4093 * seed)
+    d = synth.synth_backslash_string(seed, 200000 + 4093 * seed)
     assert_same(ctx.parse_standard_json(d), oracle.parse(d))
+
+
+@pytest.mark.parametrize("seed", [0xC0DE5005, 11])
+def test_backslash_string_32mib(cj, ctx, oracle, seed):
+    """The serving workload's adversarial request: one 32 MiB string of
+    backslash runs (even runs, escaped quotes), alone, and as one JSON-Lines
+    record between ordinary records, cut into 1 and 3 chunks."""
+    d = synth.synth_backslash_string(seed, 32 << 20)
+    ref = oracle.parse(d)
+    assert ref.flags == 0
+    assert_same(ctx.parse_standard_json(d), ref)
+    recs, _ = synth.synth_lines(seed, 300000)
+    assert recs[-1] == ord("\n")
+    lines = np.concatenate([recs, d, np.frombuffer(b"\n", np.uint8), recs])
+    for chunks in (1, 3):
+        sizes = cj.plan_lines_count(lines, chunks)
+        st, res = ctx.try_parse(lines, lines=True, chunk_sizes=sizes)
+        ref = oracle.parse(lines, lines=True, chunk_sizes=sizes)
+        assert st == 0 and ref.flags == 0
+        assert_same(res, ref)
 
 
 @pytest.mark.parametrize("depth", [1, 256, 257, 10000, 100000])
 def test_deep(cj, ctx, oracle, depth):
-    d = cj.synth_deep(depth)
+    d = synth.synth_deep(depth)
     res = ctx.parse_standard_json(d)
     assert_same(res, oracle.parse(d))
     assert res.max_depth == depth
@@ -78,7 +99,7 @@ def test_random_bytes(cj, ctx, oracle, seed):
 
 
 def test_lines(cj, ctx, oracle):
-    d, _ = cj.synth_lines(5, 3 << 20)
+    d, _ = synth.synth_lines(5, 3 << 20)
     nl = np.flatnonzero(d == 10)
     cuts = [0] + [int(nl[i * len(nl) // 4]) + 1 for i in range(1, 4)] + [d.size]
     sizes = [cuts[i + 1] - cuts[i] for i in range(4)]
@@ -90,8 +111,8 @@ def test_lines(cj, ctx, oracle):
 
 @pytest.mark.parametrize("kind,status", [(1, 2), (2, 2), (3, 2), (4, 3), (5, 3)])
 def test_invalid(cj, ctx, oracle, kind, status):
-    d = cj.synth_document(500 + kind, 200000)
-    assert cj.synth_corrupt(d, kind, 3)
+    d = synth.synth_document(500 + kind, 200000)
+    assert synth.synth_corrupt(d, kind, 3)
     st, res = ctx.try_parse(d)
     assert st == status and res is None
 
@@ -118,14 +139,14 @@ def test_utf8_cases(ctx, oracle):
 
 
 def test_repeat_deterministic(cj, ctx):
-    d = cj.synth_document(99, 2 << 20)
+    d = synth.synth_document(99, 2 << 20)
     first = ctx.parse_standard_json(d).buffer
     for _ in range(20):
         assert np.array_equal(ctx.parse_standard_json(d).buffer, first)
 
 
 def test_staged_and_into(cj, ctx, oracle):
-    d = cj.synth_document(123, 1 << 20)
+    d = synth.synth_document(123, 1 << 20)
     ref = oracle.parse(d)
     ctx.stage_standard(d)
     ctx.run()
@@ -171,7 +192,7 @@ def test_input_wait_timeout_reported(cj, ctx, oracle):
     counter nobody raises never reports; the kernel gives up after a few polls,
     finishes with its timeout flag, and the context parses normally afterwards."""
     import ctypes
-    d = cj.synth_document(4242, 300001)
+    d = synth.synth_document(4242, 300001)
     ctx.stage_standard(d)
     info = cj.ParseInfo()
     st = cj.lib().cj_run_staged_starved(ctx.handle, 64, ctypes.byref(info))

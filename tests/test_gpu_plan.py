@@ -1,8 +1,10 @@
 """cj_plan_lines_count_device (JSON-Lines chunk plan computed on the device)
-against cj_plan_lines_count (the host planner, whose chunk boundaries other
-tests pin to the reference's loadJSONLines_chunkCount rule)."""
+against cj_plan_lines_count (the host planner; both are pinned to the
+reference's loadJSONLines_chunkCount by tests/test_plan_golden.py), and its
+ordering after the stream that fills the buffer."""
 import numpy as np
 import pytest
+from tests import synth
 
 pytestmark = pytest.mark.gpu
 
@@ -19,7 +21,7 @@ def torch_cuda():
 
 def _cases(cj):
     rng = np.random.default_rng(0xC0DE7001)
-    lines, _ = cj.synth_lines(cj.CONFIG_SEED_BASE + 3, 8 << 20)
+    lines, _ = synth.synth_lines(synth.CONFIG_SEED_BASE + 3, 8 << 20)
     yield "generated", lines
     yield "open last line", np.concatenate([lines, np.frombuffer(b'{"a":1}', np.uint8)])
     yield "one line, no newline", np.frombuffer(b'{"a":[1,2,3]}', np.uint8)
@@ -47,3 +49,27 @@ def test_device_plan_matches_host_plan(cj, ctx, torch_cuda):
 
 def test_device_plan_empty(ctx):
     assert ctx.plan_lines_count_device(0, 0, 3) == [0, 0, 0]
+
+
+def test_device_plan_waits_for_the_filling_stream(cj, ctx, torch_cuda):
+    """The buffer is filled by an asynchronous copy from pinned memory on a
+    side stream that is still running when the planner is called with that
+    stream: the plan must see the copied bytes, not the zeros before them."""
+    torch = torch_cuda
+    lines, _ = synth.synth_lines(cj_seed(), 64 << 20)
+    want = cj.plan_lines_count(lines, 5)
+    host = torch.from_numpy(lines).pin_memory()
+    side = torch.cuda.Stream()
+    for _ in range(3):
+        d = torch.zeros(lines.size, dtype=torch.uint8, device="cuda")
+        torch.cuda.synchronize()
+        with torch.cuda.stream(side):
+            torch.cuda._sleep(2_000_000)          # keep the stream busy before the copy
+            d.copy_(host, non_blocking=True)
+        got = ctx.plan_lines_count_device(d.data_ptr(), int(lines.size), 5, stream=side.cuda_stream)
+        assert got == want
+        torch.cuda.synchronize()
+
+
+def cj_seed():
+    return synth.CONFIG_SEED_BASE + 3

@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 
 from tests.golden.make_query_golden import value_digest
+from tests import synth
 
 pytestmark = pytest.mark.gpu
 
@@ -43,7 +44,7 @@ def test_golden_queries(cj, oracle, ctx, name):
 
 def test_events_full_size(cj, oracle, ctx):
     """2 GB of event-log records (the JSON-Lines size limit)."""
-    doc, nrec, npush = cj.synth_events(0xC0DE5004, cj.MAX_INPUT_BYTES)
+    doc, nrec, npush = synth.synth_events(0xC0DE5004, cj.MAX_INPUT_BYTES)
     sizes = cj.plan_lines_count(doc, 4)
     res = staged(ctx, doc, sizes)
     ref = oracle.parse(doc, lines=True, chunk_sizes=sizes)
@@ -60,7 +61,7 @@ def test_events_full_size(cj, oracle, ctx):
 def test_random_keys_config3_shape(cj, oracle, ctx):
     """The 2 GB JSON-Lines workload's own records (random keys): the first
     record's first key, extracted everywhere it occurs at top level."""
-    doc, _ = cj.synth_lines(cj.CONFIG_SEED_BASE + 3, 256 << 20)
+    doc, _ = synth.synth_lines(synth.CONFIG_SEED_BASE + 3, 256 << 20)
     sizes = cj.plan_lines_count(doc, 2)
     staged(ctx, doc, sizes)
     ref = oracle.parse(doc, lines=True, chunk_sizes=sizes)
@@ -103,9 +104,9 @@ def test_random_documents_and_keys(cj, oracle, ctx, seed):
     by the oracle, bit for bit."""
     rng = np.random.default_rng(seed)
     if seed % 2:
-        doc, _ = cj.synth_lines(seed, 3 << 20, max_depth=4)
+        doc, _ = synth.synth_lines(seed, 3 << 20, max_depth=4)
     else:
-        doc, _, _ = cj.synth_events(seed, 3 << 20)
+        doc, _, _ = synth.synth_events(seed, 3 << 20)
     n_chunks = int(rng.integers(1, 5))
     sizes = cj.plan_lines_count(doc, n_chunks)
     staged(ctx, doc, sizes)

@@ -3,6 +3,7 @@ same document parsed alone and the oracle's; verdicts per request; memory
 budget admission; Poisson replay."""
 import numpy as np
 import pytest
+from tests import synth
 
 pytestmark = pytest.mark.gpu
 
@@ -14,10 +15,10 @@ def alone(ctx, doc, lines):
 
 
 def test_results_same_alone_and_in_the_mix(cj, oracle, ctx):
-    docs, lines, kinds = cj.serve_requests(0x5E4E0001, 240, median=16 << 10, max_size=4 << 20,
+    docs, lines, kinds = synth.serve_requests(0x5E4E0001, 240, median=16 << 10, max_size=4 << 20,
                                            adversarial_frac=0.02, backslash_bytes=1 << 20)
-    bad = cj.synth_document(77, 30000)
-    assert cj.synth_corrupt(bad, cj.CORRUPT_OVERLONG3, 1)
+    bad = synth.synth_document(77, 30000)
+    assert synth.synth_corrupt(bad, synth.CORRUPT_OVERLONG3, 1)
     docs.insert(17, bad)
     lines = np.insert(lines, 17, False)
     with cj.Server(slots=2, max_batch_docs=64, memory_budget=2 << 30) as srv:
@@ -39,7 +40,7 @@ def test_results_same_alone_and_in_the_mix(cj, oracle, ctx):
 
 
 def test_replay_poisson(cj):
-    docs, lines, _ = cj.serve_requests(0x5E4E0002, 300, median=8 << 10, max_size=1 << 20,
+    docs, lines, _ = synth.serve_requests(0x5E4E0002, 300, median=8 << 10, max_size=1 << 20,
                                        adversarial_frac=0.0)
     rng = np.random.default_rng(3)
     arrivals = np.cumsum(rng.exponential(1 / 5000.0, len(docs)))
@@ -53,7 +54,7 @@ def test_replay_poisson(cj):
 
 def test_memory_budget_admission(cj):
     budget = 64 << 20                     # 32 MiB of device bytes per slot
-    docs, lines, _ = cj.serve_requests(0x5E4E0003, 120, median=64 << 10, max_size=512 << 10,
+    docs, lines, _ = synth.serve_requests(0x5E4E0003, 120, median=64 << 10, max_size=512 << 10,
                                        adversarial_frac=0.0)
     with cj.Server(slots=2, max_batch_docs=1024, memory_budget=budget) as srv:
         tickets = [srv.submit(d, bool(l)) for d, l in zip(docs, lines)]
@@ -62,6 +63,6 @@ def test_memory_budget_admission(cj):
         st = srv.stats()
         assert st.peak_admitted_bytes <= budget // 2
         assert st.batches > 2
-        big = cj.synth_document(5, 4 << 20)
+        big = synth.synth_document(5, 4 << 20)
         with pytest.raises(cj.CujsonError):
             srv.submit(big)               # more than a slot's share of the budget

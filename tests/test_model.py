@@ -10,6 +10,7 @@ import pytest
 
 sys.path.insert(0, str(Path(__file__).resolve().parent / "model"))
 import build as model_build  # noqa: E402
+from tests import synth  # noqa: E402  (seeded inputs)
 
 
 @pytest.fixture(scope="module")
@@ -60,28 +61,28 @@ def test_classify_bit_planes(model):
 @pytest.mark.parametrize("seed", range(6))
 def test_documents(cj, oracle, model, seed):
     n = [3000, 70000, 300000, 1 << 20, 123457, 9000][seed]
-    d = cj.synth_document(1000 + seed, n, max_depth=8)
+    d = synth.synth_document(1000 + seed, n, max_depth=8)
     check(model, oracle, d, seed=seed)
 
 
 def test_huge_strings(cj, oracle, model):
-    d = cj.synth_document(77, 3 << 20, max_depth=20, huge_string_frac=0.05,
+    d = synth.synth_document(77, 3 << 20, max_depth=20, huge_string_frac=0.05,
                           huge_string_min=20000, huge_string_max=70000)
     check(model, oracle, d)
 
 
 def test_backslash_runs(cj, oracle, model):
     for seed in range(4):
-        check(model, oracle, cj.synth_backslash_string(seed, 100000 + seed * 777))
+        check(model, oracle, synth.synth_backslash_string(seed, 100000 + seed * 777))
 
 
 @pytest.mark.parametrize("depth", [1, 300, 5000, 20000])
 def test_deep(cj, oracle, model, depth):
-    check(model, oracle, cj.synth_deep(depth))
+    check(model, oracle, synth.synth_deep(depth))
 
 
 def test_lines(cj, oracle, model):
-    d, _ = cj.synth_lines(5, 600000)
+    d, _ = synth.synth_lines(5, 600000)
     check(model, oracle, d, lines=True)
     # reference-style line-aligned chunks
     nl = np.flatnonzero(d == 10)
@@ -100,8 +101,8 @@ def test_random_bytes(cj, oracle, model, seed):
 
 def test_corrupt(cj, oracle, model):
     for kind in range(1, 6):
-        d = cj.synth_document(42 + kind, 50000)
-        assert cj.synth_corrupt(d, kind, kind)
+        d = synth.synth_document(42 + kind, 50000)
+        assert synth.synth_corrupt(d, kind, kind)
         check(model, oracle, d)
 
 

@@ -12,7 +12,9 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-REF_DATASET = Path("/root/reference/dataset")
+from oracle import build_ref
+
+REF_DATASET = build_ref.DEFAULT_REF / "dataset"
 
 
 def _pos(r):

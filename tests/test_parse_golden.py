@@ -16,6 +16,7 @@ import numpy as np
 import pytest
 
 from tests.golden.make_parse_golden import digests, make_input
+from tests import synth
 
 GOLDEN = Path(__file__).resolve().parent / "golden" / "parse_golden.json"
 CASES = json.loads(GOLDEN.read_text())["cases"]
@@ -35,7 +36,7 @@ def case_input(c):
     if c["kind"] == "corrupt":
         import cujson_gb300 as cj
         data, _ = make_input("document", c["source"]["args"])
-        assert cj.synth_corrupt(data, c["source"]["corrupt"], c["source"]["args"]["seed"])
+        assert synth.synth_corrupt(data, c["source"]["corrupt"], c["source"]["args"]["seed"])
         return data, None
     data, chunks = make_input(c["kind"], c["source"]["args"])
     return data, c["chunk_sizes"]

@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 
 from tests.golden.make_query_golden import value_digest
+from tests import synth
 
 GOLDEN = json.loads((Path(__file__).resolve().parent / "golden" / "query_golden.json").read_text())
 
@@ -46,7 +47,7 @@ def test_oracle_matches_reference_iterator(oracle, q):
 
 
 def test_generator_push_count_matches_oracle(cj, oracle):
-    doc, nrec, npush = cj.synth_events(0xC0DE5003, 1 << 20)
+    doc, nrec, npush = synth.synth_events(0xC0DE5003, 1 << 20)
     res = oracle.parse(doc, lines=True)
     assert res.valid
     n, _ = oracle.query_lines(doc, res, b"type", b"PushEvent")

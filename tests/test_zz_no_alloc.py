@@ -10,6 +10,7 @@ from pathlib import Path
 
 import numpy as np
 import pytest
+from tests import synth
 
 REPO = Path(__file__).resolve().parent.parent
 MAX = 1048576   # CJ_NOALLOC_MAX_BYTES
@@ -52,10 +53,10 @@ def test_noalloc_matches_arena_path_calls_in_a_row(cj, torch_cuda):
     torch = torch_cuda
     ctx = cj.Context()
     try:
-        docs = [cj.synth_document(0xA110C001, 300001, max_depth=12),
-                cj.synth_document(0xA110C002, MAX, max_depth=20),
+        docs = [synth.synth_document(0xA110C001, 300001, max_depth=12),
+                synth.synth_document(0xA110C002, MAX, max_depth=20),
                 np.frombuffer(b'{"k":[{},[]],"x":{}}', np.uint8).copy(),
-                cj.synth_document(0xA110C001, 300001, max_depth=12)]
+                synth.synth_document(0xA110C001, 300001, max_depth=12)]
         for doc in docs:
             want = ctx.parse_standard_json(doc)
             S = want.n_structural
@@ -73,15 +74,20 @@ def test_noalloc_verdicts_and_limits(cj, torch_cuda):
     torch = torch_cuda
     ctx = cj.Context()
     try:
-        bad = cj.synth_document(0xA110C003, 50000)
-        assert cj.synth_corrupt(bad, 1, 5)
+        bad = synth.synth_document(0xA110C003, 50000)
+        assert synth.synth_corrupt(bad, 1, 5)
         st_arena, _ = ctx.try_parse(bad)
-        st, info, _ = _noalloc(cj, torch, bad, 2 * bad.size + 4)
+        st, info, out = _noalloc(cj, torch, bad, 2 * bad.size + 4)
         assert st == st_arena != cj.OK
         assert info.status == st
+        assert (out == -7).all()          # an invalid document writes nothing
+        unbalanced = synth.synth_document(0xA110C005, 50000)
+        assert synth.synth_corrupt(unbalanced, synth.CORRUPT_UNBALANCED, 6)
+        st, info, out = _noalloc(cj, torch, unbalanced, 2 * unbalanced.size + 4)
+        assert st == cj.ERR_INVALID_BRACKETS and (out == -7).all()
 
         # output too small: refused, nothing written
-        doc = cj.synth_document(0xA110C004, 20000)
+        doc = synth.synth_document(0xA110C004, 20000)
         st, info, out = _noalloc(cj, torch, doc, 8)
         assert st == cj.ERR_CAPACITY
         assert (out == -7).all()
