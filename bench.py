@@ -663,6 +663,7 @@ def run_ours(args, world, rank, local, pg):
     for _ in range(args.steps):
         ctx.run()
     scan_ms, pair_ms, spine_ms, runs = ctx.phase_ms()     # synchronises the stream
+    tables_ms, prefix_ms, emit_ms, _ = ctx.scan_phase_ms()
     span_ms = ctx.span_ms()
     barrier(pg)
     launches = ctx.launches - launches0
@@ -738,8 +739,9 @@ def run_ours(args, world, rank, local, pg):
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "peak_kind": peak_kind, "traffic": traffic,
                      "algorithmic_bytes": B},
-        "phases_ms_per_step": {"scan": round(scan_ms / runs, 4), "pair": round(pair_ms / runs, 4),
-                               "spine": round(spine_ms / runs, 4)},
+        "phases_ms_per_step": {"scan": round(scan_ms / runs, 4), "scan_tables": round(tables_ms / runs, 4),
+                               "scan_prefix": round(prefix_ms / runs, 4), "scan_emit": round(emit_ms / runs, 4),
+                               "pair": round(pair_ms / runs, 4), "spine": round(spine_ms / runs, 4)},
         "parse_roofline_frac": round(B / (span_max / args.steps / 1e3) / 1e9 / peak, 4),
         "e2e": e2e, "cpu_baseline": cpu, "cpu_baseline_port": cpu_port, "gpu_launches": int(launches), "clocks": ck,
         "batch": batch, "serving": serve, "query": query, "other_configs": others,

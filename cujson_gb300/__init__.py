@@ -68,11 +68,13 @@ class _Result(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     """Launch shapes (cj_tuning): 0 = default."""
-    _fields_ = [("scan_ctas", ctypes.c_int32), ("pair_blocks", ctypes.c_int32),
+    _fields_ = [("region_kib", ctypes.c_int32), ("scan_blocks_per_sm", ctypes.c_int32),
+                ("emit_blocks_per_sm", ctypes.c_int32), ("pair_blocks", ctypes.c_int32),
                 ("pair_threads", ctypes.c_int32), ("ms", ctypes.c_float)]
 
     def as_dict(self):
-        return {"scan_ctas": self.scan_ctas, "pair_blocks": self.pair_blocks,
+        return {"region_kib": self.region_kib, "scan_blocks_per_sm": self.scan_blocks_per_sm,
+                "emit_blocks_per_sm": self.emit_blocks_per_sm, "pair_blocks": self.pair_blocks,
                 "pair_threads": self.pair_threads, "ms": round(float(self.ms), 4)}
 
 
@@ -141,6 +143,9 @@ _SIGNATURES = {
                                            ctypes.POINTER(ctypes.c_double),
                                            ctypes.POINTER(ctypes.c_double),
                                            ctypes.POINTER(ctypes.c_int64)]),
+    "cj_context_scan_phase_ms": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                                ctypes.POINTER(ctypes.c_int64)]),
     "cj_context_span_ms": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
     "cj_host_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
     "cj_host_free": (None, [ctypes.c_void_p]),
@@ -421,8 +426,9 @@ class Context:
         return res
 
     # ---- launch shapes -------------------------------------------------------------
-    def set_tuning(self, scan_ctas: int = 0, pair_blocks: int = 0, pair_threads: int = 0) -> None:
-        t = Tuning(scan_ctas, pair_blocks, pair_threads, 0.0)
+    def set_tuning(self, region_kib: int = 0, scan_blocks_per_sm: int = 0, emit_blocks_per_sm: int = 0,
+                   pair_blocks: int = 0, pair_threads: int = 0) -> None:
+        t = Tuning(region_kib, scan_blocks_per_sm, emit_blocks_per_sm, pair_blocks, pair_threads, 0.0)
         _check(lib().cj_context_set_tuning(self._h, ctypes.byref(t)), "set_tuning")
 
     def get_tuning(self) -> Tuning:
@@ -449,6 +455,15 @@ class Context:
         n = ctypes.c_int64()
         _check(lib().cj_context_phase_ms(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
                                          ctypes.byref(n)), "phase_ms")
+        return a.value, b.value, c.value, n.value
+
+    def scan_phase_ms(self):
+        """(tables_ms, prefix_ms, emit_ms, runs): the scan's kernels, summed over
+        the recorded runs."""
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        n = ctypes.c_int64()
+        _check(lib().cj_context_scan_phase_ms(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                              ctypes.byref(n)), "scan_phase_ms")
         return a.value, b.value, c.value, n.value
 
     def span_ms(self) -> float:

@@ -39,22 +39,25 @@ struct DevBuf {
 
 size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
 
+// recorded run: start, after the scan's tables, prefix and emit kernels, after
+// pair, after spine
+constexpr size_t kEventsPerRun = 6;
+
 }  // namespace
 
 struct cj_context {
     int device = 0;
     int sm_count = 0;
-    uint32_t scan_grid = 0;             // resident scan CTAs (persistent grid)
     cudaStream_t stream = nullptr;
 
     DevBuf<uint8_t> in;
     DevBuf<int32_t> pos, pair;
     DevBuf<uint2> brk;
-    DevBuf<uint32_t> desc_flag;
-    DevBuf<uint4> desc_agg, desc_incl;
+    DevBuf<uint4> rtab, rentry, bagg;   // region tables, entry values, prefix block tables
+    DevBuf<uint32_t> work;              // regions the emit kernel visits
     DevBuf<Segment> segs;
     DevBuf<SegmentOut> seg_out;
-    DevBuf<uint32_t> tile_seg;
+    DevBuf<uint32_t> region_seg;
     DevBuf<uint32_t> spine;
     DevBuf<int4> cinfo;
     DevBuf<unsigned long long> tree;
@@ -64,7 +67,7 @@ struct cj_context {
 
     Ctrl* h_ctrl = nullptr;             // pinned mirrors
     std::vector<Segment> h_segs;
-    std::vector<uint32_t> h_tile_seg;
+    std::vector<uint32_t> h_region_seg;
     SegmentOut* h_seg_out = nullptr;
     size_t h_seg_out_cap = 0;
 
@@ -73,12 +76,13 @@ struct cj_context {
     bool lines = false;
     size_t n_bytes = 0;
     uint32_t n_segs = 0;
-    uint32_t n_tiles = 0;
+    uint32_t n_regions = 0;
+    int run_region_steps = kRegionStepsDefault;   // region size of the staged layout
     int64_t launches = 0;
     size_t dev_bytes = 0;
 
     bool timing = false;
-    std::vector<cudaEvent_t> events;   // 4 per recorded run
+    std::vector<cudaEvent_t> events;   // kEventsPerRun per recorded run
     size_t events_used = 0;
 
     // batches of independent documents
@@ -104,7 +108,7 @@ struct cj_context {
     uint64_t arena_gen = 0;             // bumped whenever a device buffer is (re)allocated
 
     // one-shot parses of large inputs: copies on copy_stream overlap the scan,
-    // which hands out a tile only once d_ready covers its bytes
+    // which scans a region only once d_ready covers its bytes
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_reset = nullptr, ev_copied = nullptr;
     cudaEvent_t ev_plan = nullptr;      // orders the device planner after the caller's stream
@@ -125,7 +129,9 @@ struct cj_context {
     DevBuf<unsigned long long> plan_pos;
 
     // launch shapes (0 = default), set by cj_context_set_tuning / cj_autotune_staged
-    uint32_t tune_scan_ctas = 0;
+    int tune_region_steps = 0;
+    int tune_tables_per_sm = 0;
+    int tune_emit_per_sm = 0;
     uint32_t tune_pair_blocks = 0;
     uint32_t tune_pair_threads = 0;
 };
@@ -157,12 +163,33 @@ cj_status ensure(cj_context* ctx, DevBuf<T>& b, size_t n)
 template <typename T>
 void release(DevBuf<T>& b) { if (b.p) cudaFree(b.p); b.p = nullptr; b.cap = 0; }
 
+int region_steps(const cj_context* ctx)
+{
+    return ctx->tune_region_steps ? ctx->tune_region_steps : kRegionStepsDefault;
+}
+
+// regions of an input of `bytes` in `segs` segments, for any region size
+size_t max_regions(size_t bytes, size_t segs)
+{
+    return bytes / ((size_t)kRegionStepsAllowed[0] * kStepBytes) + segs + 1;
+}
+
+cj_status reserve_regions(cj_context* ctx, size_t regions)
+{
+    cj_status st;
+    if ((st = ensure(ctx, ctx->rtab, regions * 4))) return st;
+    if ((st = ensure(ctx, ctx->rentry, regions))) return st;
+    if ((st = ensure(ctx, ctx->work, regions))) return st;
+    if ((st = ensure(ctx, ctx->region_seg, regions))) return st;
+    if ((st = ensure(ctx, ctx->bagg, prefix_blocks(regions) * 4))) return st;
+    return CJ_OK;
+}
+
 // Size every buffer for an input of `bytes` in `segs` segments.  S, the
 // structural count, is at most the byte count, and so is the bracket count.
 cj_status reserve(cj_context* ctx, size_t bytes, size_t segs)
 {
     size_t padded = round_up(bytes, kPadBytes) + segs * (size_t)kPadBytes;
-    size_t tiles = bytes / kTileBytes + segs + 1;
     size_t s_cap = bytes + 1;
     size_t chunks = (bytes + kChunk - 1) / kChunk + 1;
     cj_status st;
@@ -170,15 +197,9 @@ cj_status reserve(cj_context* ctx, size_t bytes, size_t segs)
     if ((st = ensure(ctx, ctx->pos, s_cap))) return st;
     if ((st = ensure(ctx, ctx->pair, s_cap))) return st;
     if ((st = ensure(ctx, ctx->brk, s_cap))) return st;
-    bool new_desc = ctx->desc_flag.cap < tiles;
-    if ((st = ensure(ctx, ctx->desc_flag, tiles))) return st;
-    if (new_desc)
-        CJ_CUDA(cudaMemsetAsync(ctx->desc_flag.p, 0, ctx->desc_flag.cap * sizeof(uint32_t), ctx->stream));
-    if ((st = ensure(ctx, ctx->desc_agg, tiles * 4))) return st;
-    if ((st = ensure(ctx, ctx->desc_incl, tiles))) return st;
+    if ((st = reserve_regions(ctx, max_regions(bytes, segs)))) return st;
     if ((st = ensure(ctx, ctx->segs, segs))) return st;
     if ((st = ensure(ctx, ctx->seg_out, segs))) return st;
-    if ((st = ensure(ctx, ctx->tile_seg, tiles))) return st;
     if ((st = ensure(ctx, ctx->spine, chunks * (size_t)kChunk))) return st;
     if ((st = ensure(ctx, ctx->cinfo, chunks))) return st;
     if (chunks > ctx->chunk_cap) {
@@ -205,7 +226,39 @@ cj_status reserve(cj_context* ctx, size_t bytes, size_t segs)
     return CJ_OK;
 }
 
-// Lay the chunks out on tile boundaries and copy them to the device.
+// Cut every segment of ctx->h_segs (dev_off, len set) into regions of the
+// tuned size and queue the copies of the segment table and the region ->
+// segment map (the host vectors must live until the stream passes them).
+cj_status place_regions(cj_context* ctx)
+{
+    const int R = region_steps(ctx);
+    const uint64_t rb = (uint64_t)R * kStepBytes;
+    const size_t n = ctx->h_segs.size();
+    uint64_t regions = 0;
+    for (size_t i = 0; i < n; i++) {
+        Segment& g = ctx->h_segs[i];
+        g.first_region = (uint32_t)regions;
+        g.n_regions = (uint32_t)((g.len + rb - 1) / rb);
+        regions += g.n_regions;
+    }
+    if (regions >= 0xFFFFFFFFull) return CJ_ERR_TOO_LARGE;
+    ctx->run_region_steps = R;
+    ctx->n_regions = (uint32_t)regions;
+    CJ_CUDA(cudaMemcpyAsync(ctx->segs.p, ctx->h_segs.data(), n * sizeof(Segment), cudaMemcpyHostToDevice,
+                            ctx->stream));
+    if (n > 1) {
+        ctx->h_region_seg.resize(regions);
+        for (size_t i = 0; i < n; i++)
+            for (uint32_t t = 0; t < ctx->h_segs[i].n_regions; t++)
+                ctx->h_region_seg[ctx->h_segs[i].first_region + t] = (uint32_t)i;
+        CJ_CUDA(cudaMemcpyAsync(ctx->region_seg.p, ctx->h_region_seg.data(), regions * sizeof(uint32_t),
+                                cudaMemcpyHostToDevice, ctx->stream));
+    }
+    return CJ_OK;
+}
+
+// Lay the chunks out on 1 KiB boundaries, cut them into regions and copy them
+// to the device.
 cj_status stage(cj_context* ctx, const uint8_t* const* chunks, const size_t* sizes, size_t n,
                 bool lines)
 {
@@ -224,7 +277,6 @@ cj_status stage(cj_context* ctx, const uint8_t* const* chunks, const size_t* siz
 
     ctx->h_segs.resize(n);
     uint64_t dev_off = 0, logical = 0;
-    uint32_t tile = 0;
     for (size_t i = 0; i < n; i++) {
         Segment& s = ctx->h_segs[i];
         s.dev_off = dev_off;
@@ -232,32 +284,19 @@ cj_status stage(cj_context* ctx, const uint8_t* const* chunks, const size_t* siz
         s.logical_off = logical;
         s.out_base = 0;
         s.brk_base = 0;
-        s.first_tile = tile;
-        s.n_tiles = (uint32_t)((sizes[i] + kTileBytes - 1) / kTileBytes);
         s.flags = (i > 0) ? kSegContinue : 0u;
         s.pad = 0;
         dev_off += round_up(sizes[i], kPadBytes);
         logical += sizes[i];
-        tile += s.n_tiles;
     }
     for (size_t i = 0; i < n; i++)
         CJ_CUDA(cudaMemcpyAsync(ctx->in.p + ctx->h_segs[i].dev_off, chunks[i], sizes[i],
                                 cudaMemcpyHostToDevice, ctx->stream));
-    CJ_CUDA(cudaMemcpyAsync(ctx->segs.p, ctx->h_segs.data(), n * sizeof(Segment),
-                            cudaMemcpyHostToDevice, ctx->stream));
-    if (n > 1) {
-        ctx->h_tile_seg.resize(tile);
-        for (size_t i = 0; i < n; i++)
-            for (uint32_t t = 0; t < ctx->h_segs[i].n_tiles; t++)
-                ctx->h_tile_seg[ctx->h_segs[i].first_tile + t] = (uint32_t)i;
-        CJ_CUDA(cudaMemcpyAsync(ctx->tile_seg.p, ctx->h_tile_seg.data(), tile * sizeof(uint32_t),
-                                cudaMemcpyHostToDevice, ctx->stream));
-    }
+    if ((st = place_regions(ctx))) return st;
     // host vectors must outlive the copies
     CJ_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->n_bytes = total;
     ctx->n_segs = (uint32_t)n;
-    ctx->n_tiles = tile;
     ctx->lines = lines;
     ctx->batch = false;
     ctx->graph_valid = false;
@@ -272,20 +311,18 @@ uint32_t pair_threads(const cj_context* ctx)
 
 // Every kernel of one staged run, on the context stream, without host
 // synchronisation.  `graph` selects the form that a CUDA graph replays: the
-// epoch stays fixed and the descriptor flags and min-tree are cleared by the
-// run itself instead of being told apart by epoch.
+// epoch stays fixed and the pairing min-tree is cleared by the run itself
+// instead of being told apart by epoch.
 cj_status enqueue(cj_context* ctx, bool graph)
 {
     if (!graph) {
         ctx->epoch = (ctx->epoch + 1) & 0x3FFFFFFFu;
         if (ctx->epoch == 0) {
-            // epoch wrapped: stale descriptors could alias, so clear them
-            CJ_CUDA(cudaMemsetAsync(ctx->desc_flag.p, 0, ctx->desc_flag.cap * sizeof(uint32_t), ctx->stream));
+            // epoch wrapped: stale min-tree tags could alias, so clear them
             CJ_CUDA(cudaMemsetAsync(ctx->tree.p, 0, ctx->tree.cap * sizeof(unsigned long long), ctx->stream));
             ctx->epoch = 1;
         }
     } else {
-        CJ_CUDA(cudaMemsetAsync(ctx->desc_flag.p, 0, (size_t)ctx->n_tiles * sizeof(uint32_t), ctx->stream));
         CJ_CUDA(cudaMemsetAsync(ctx->tree.p, 0, ctx->tree.cap * sizeof(unsigned long long), ctx->stream));
     }
     CJ_CUDA(cudaMemsetAsync(ctx->d_ctrl, 0, sizeof(Ctrl), ctx->stream));
@@ -298,45 +335,48 @@ cj_status enqueue(cj_context* ctx, bool graph)
 
     cudaEvent_t* ev = nullptr;
     if (ctx->timing && !graph) {
-        if (ctx->events_used + 4 > ctx->events.size()) {
-            for (int i = 0; i < 4; i++) {
+        if (ctx->events_used + kEventsPerRun > ctx->events.size()) {
+            for (size_t i = 0; i < kEventsPerRun; i++) {
                 cudaEvent_t e;
                 CJ_CUDA(cudaEventCreate(&e));
                 ctx->events.push_back(e);
             }
         }
         ev = ctx->events.data() + ctx->events_used;
-        ctx->events_used += 4;
+        ctx->events_used += kEventsPerRun;
         CJ_CUDA(cudaEventRecord(ev[0], ctx->stream));
     }
 
     ScanParams sp{};
     sp.in = ctx->in.p;
     sp.segs = ctx->segs.p;
-    sp.tile_seg = (ctx->n_segs > 1) ? ctx->tile_seg.p : nullptr;
+    sp.region_seg = (ctx->n_segs > 1) ? ctx->region_seg.p : nullptr;
     sp.n_segs = ctx->n_segs;
-    sp.n_tiles = ctx->n_tiles;
+    sp.n_regions = ctx->n_regions;
     sp.pos = ctx->pos.p;
     sp.pair = ctx->pair.p;
     sp.brk = ctx->brk.p;
-    sp.desc_flag = ctx->desc_flag.p;
-    sp.desc_agg = ctx->desc_agg.p;
-    sp.desc_incl = ctx->desc_incl.p;
+    sp.out_cap = ctx->pos.cap;
+    sp.brk_cap = ctx->brk.cap;
+    sp.rtab = ctx->rtab.p;
+    sp.rentry = ctx->rentry.p;
+    sp.bagg = ctx->bagg.p;
+    sp.work = ctx->work.p;
     sp.ctrl = ctx->d_ctrl;
     sp.seg_out = ctx->seg_out.p;
-    sp.epoch = ctx->epoch;
     sp.seg_err = ctx->batch ? ctx->seg_err.p : nullptr;
     sp.ready = ctx->overlap_run ? ctx->d_ready : nullptr;
     sp.input_wait_limit = ctx->input_wait_limit;
-    uint32_t scan_grid = ctx->scan_grid;
-    if (ctx->tune_scan_ctas) scan_grid = std::min(scan_grid, ctx->tune_scan_ctas);
-    launch_scan(sp, ctx->lines, (int)std::min<uint32_t>(ctx->n_tiles, scan_grid), ctx->stream);
+    sp.region_steps = ctx->run_region_steps;
+    sp.sm_count = ctx->sm_count;
+    ScanShape shape{ctx->tune_tables_per_sm, ctx->tune_emit_per_sm};
+    launch_scan(sp, ctx->lines, shape, ctx->stream, ev ? ev + 1 : nullptr);
+    ctx->launches += scan_launches(ctx->n_regions);
     if (ctx->batch) {
         launch_batch_prefix(ctx->segs.p, ctx->seg_out.p, ctx->n_segs, ctx->layout_off.p, ctx->rchunk_off.p,
                             ctx->stream);
         ctx->launches += 1;
     }
-    if (ev) CJ_CUDA(cudaEventRecord(ev[1], ctx->stream));
 
     PairParams pp{};
     pp.brk = ctx->brk.p;
@@ -364,10 +404,10 @@ cj_status enqueue(cj_context* ctx, bool graph)
                                      (size_t)ctx->sm_count * 8 * 256 / pthreads);
     if (ctx->tune_pair_blocks) grid = (int)std::min<size_t>((size_t)grid, ctx->tune_pair_blocks);
     launch_pair(pp, grid, ctx->stream, (int)pthreads);
-    if (ev) CJ_CUDA(cudaEventRecord(ev[2], ctx->stream));
+    if (ev) CJ_CUDA(cudaEventRecord(ev[4], ctx->stream));
     launch_spine(pp, grid, ctx->stream, (int)pthreads);
-    if (ev) CJ_CUDA(cudaEventRecord(ev[3], ctx->stream));
-    ctx->launches += (ctx->n_tiles ? 1 : 0) + 2;
+    if (ev) CJ_CUDA(cudaEventRecord(ev[5], ctx->stream));
+    ctx->launches += 2;
     if (ctx->batch) {
         launch_batch_layout(ctx->segs.p, ctx->seg_out.p, ctx->n_segs, ctx->pos.p, ctx->pair.p,
                             ctx->layout_off.p, ctx->layout.p, ctx->sm_count, ctx->stream);
@@ -408,7 +448,7 @@ cj_status run_graph(cj_context* ctx)
         ctx->graph_valid = true;
     }
     CJ_CUDA(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
-    ctx->launches += (ctx->n_tiles ? 1 : 0) + 2 + (ctx->batch ? 2 : 0);
+    ctx->launches += scan_launches(ctx->n_regions) + 2 + (ctx->batch ? 2 : 0);
     ctx->batch_read = false;
     return CJ_OK;
 }
@@ -446,7 +486,6 @@ cj_status stage_overlapped(cj_context* ctx, const uint8_t* const* chunks, const 
     if (st) return st;
     ctx->h_segs.resize(n);
     uint64_t dev_off = 0, logical = 0;
-    uint32_t tile = 0;
     for (size_t i = 0; i < n; i++) {
         Segment& g = ctx->h_segs[i];
         g.dev_off = dev_off;
@@ -454,29 +493,16 @@ cj_status stage_overlapped(cj_context* ctx, const uint8_t* const* chunks, const 
         g.logical_off = logical;
         g.out_base = 0;
         g.brk_base = 0;
-        g.first_tile = tile;
-        g.n_tiles = (uint32_t)((sizes[i] + kTileBytes - 1) / kTileBytes);
         g.flags = (i > 0) ? kSegContinue : 0u;
         g.pad = 0;
         dev_off += round_up(sizes[i], kPadBytes);
         logical += sizes[i];
-        tile += g.n_tiles;
     }
-    CJ_CUDA(cudaMemcpyAsync(ctx->segs.p, ctx->h_segs.data(), n * sizeof(Segment), cudaMemcpyHostToDevice,
-                            ctx->stream));
-    if (n > 1) {
-        ctx->h_tile_seg.resize(tile);
-        for (size_t i = 0; i < n; i++)
-            for (uint32_t t = 0; t < ctx->h_segs[i].n_tiles; t++)
-                ctx->h_tile_seg[ctx->h_segs[i].first_tile + t] = (uint32_t)i;
-        CJ_CUDA(cudaMemcpyAsync(ctx->tile_seg.p, ctx->h_tile_seg.data(), tile * sizeof(uint32_t),
-                                cudaMemcpyHostToDevice, ctx->stream));
-    }
+    if ((st = place_regions(ctx))) return st;
     CJ_CUDA(cudaMemsetAsync(ctx->d_ready, 0, sizeof(unsigned long long), ctx->stream));
     CJ_CUDA(cudaEventRecord(ctx->ev_reset, ctx->stream));
     ctx->n_bytes = total;
     ctx->n_segs = (uint32_t)n;
-    ctx->n_tiles = tile;
     ctx->lines = lines;
     ctx->batch = false;
     ctx->staged = true;
@@ -549,6 +575,7 @@ cj_status read_info(cj_context* ctx, cj_parse_info* info)
     if (flags & CJ_FLAG_TIMEOUT) flags |= (c.gave_up & 0xFFu) << 16;
     cj_status verdict = CJ_OK;
     if (flags & CJ_FLAG_TIMEOUT) verdict = CJ_ERR_TIMEOUT;
+    else if (flags & CJ_FLAG_OVERFLOW) verdict = CJ_ERR_CUDA;     // inconsistent scan counts (a defect)
     else if (flags & CJ_FLAG_UTF8) verdict = CJ_ERR_INVALID_UTF8;
     else if (flags & CJ_FLAG_BRACKETS) verdict = CJ_ERR_INVALID_BRACKETS;
     if (info) {
@@ -617,7 +644,7 @@ cj_status to_result(cj_context* ctx, const cj_parse_info& info, cj_result* out)
 //          so a pairing chunk never holds two documents)
 //   layout: every document's 2*(S_i+2) result back to back (offsets on the device)
 cj_status reserve_batch(cj_context* ctx, uint64_t in_bytes, uint64_t out_cap, uint64_t brk_cap,
-                        uint64_t tiles, size_t n, uint64_t layout_cap, uint64_t pack_bytes)
+                        uint64_t regions, size_t n, uint64_t layout_cap, uint64_t pack_bytes)
 {
     const uint64_t chunks = brk_cap / kChunk + 1;
     cj_status st;
@@ -625,12 +652,9 @@ cj_status reserve_batch(cj_context* ctx, uint64_t in_bytes, uint64_t out_cap, ui
     if ((st = ensure(ctx, ctx->pos, out_cap))) return st;
     if ((st = ensure(ctx, ctx->pair, out_cap))) return st;
     if ((st = ensure(ctx, ctx->brk, brk_cap + 1))) return st;
-    if ((st = ensure(ctx, ctx->desc_flag, tiles))) return st;
-    if ((st = ensure(ctx, ctx->desc_agg, tiles * 4))) return st;
-    if ((st = ensure(ctx, ctx->desc_incl, tiles))) return st;
+    if ((st = reserve_regions(ctx, regions))) return st;
     if ((st = ensure(ctx, ctx->segs, n))) return st;
     if ((st = ensure(ctx, ctx->seg_out, n))) return st;
-    if ((st = ensure(ctx, ctx->tile_seg, tiles))) return st;
     if ((st = ensure(ctx, ctx->spine, chunks * (size_t)kChunk))) return st;
     if ((st = ensure(ctx, ctx->cinfo, chunks))) return st;
     if ((st = ensure(ctx, ctx->seg_err, n))) return st;
@@ -653,8 +677,7 @@ cj_status reserve_batch(cj_context* ctx, uint64_t in_bytes, uint64_t out_cap, ui
         if ((st = ensure(ctx, ctx->tree, off))) return st;
         ctx->chunk_cap = chunks;
     }
-    // a fresh or regrown descriptor / tree array must not hold stale tags
-    CJ_CUDA(cudaMemsetAsync(ctx->desc_flag.p, 0, ctx->desc_flag.cap * sizeof(uint32_t), ctx->stream));
+    // a fresh or regrown tree array must not hold stale tags
     CJ_CUDA(cudaMemsetAsync(ctx->tree.p, 0, ctx->tree.cap * sizeof(unsigned long long), ctx->stream));
     if (!ctx->h_ctrl) CJ_CUDA(cudaMallocHost((void**)&ctx->h_ctrl, sizeof(Ctrl)));
     return CJ_OK;
@@ -673,27 +696,27 @@ cj_status stage_batch(cj_context* ctx, const uint8_t* const* docs, const uint8_t
     ctx->staged = false;
     ctx->graph_valid = false;
     if (!sizes || n == 0 || n > 0xFFFFFFFEu || (!docs && !packed && !tables_only)) return CJ_ERR_INVALID_ARGUMENT;
-    uint64_t in_bytes = 0, out_cap = 0, brk_cap = 0, tiles = 0, layout_cap = 0, total = 0;
+    // region capacity for the smallest region size, so a tuning change needs no regrowth
+    uint64_t in_bytes = 0, out_cap = 0, brk_cap = 0, regions = 0, layout_cap = 0, total = 0;
+    const uint64_t rb = (uint64_t)kRegionStepsAllowed[0] * kStepBytes;
     for (size_t i = 0; i < n; i++) {
         if (sizes[i] == 0 || (docs && !docs[i])) return CJ_ERR_INVALID_ARGUMENT;
         if (sizes[i] > CJ_MAX_INPUT_BYTES) return CJ_ERR_TOO_LARGE;
         in_bytes += round_up(sizes[i], kPadBytes);
         out_cap += sizes[i] + 1;
         brk_cap += round_up(sizes[i], kChunk);
-        tiles += (sizes[i] + kTileBytes - 1) / kTileBytes;
+        regions += (sizes[i] + rb - 1) / rb;
         layout_cap += 2 * (uint64_t)sizes[i] + 4;
         total += sizes[i];
     }
-    if (tiles >= 0xFFFFFFFFull) return CJ_ERR_TOO_LARGE;
+    if (regions >= 0xFFFFFFFFull) return CJ_ERR_TOO_LARGE;
     CJ_CUDA(cudaSetDevice(ctx->device));
-    cj_status st = reserve_batch(ctx, in_bytes, out_cap, brk_cap, tiles + 1, n, layout_cap,
+    cj_status st = reserve_batch(ctx, in_bytes, out_cap, brk_cap, regions + 1, n, layout_cap,
                                  (packed && !tables_only) ? total : 0);
     if (st) return st;
 
     ctx->h_segs.resize(n);
-    ctx->h_tile_seg.resize(tiles);
     uint64_t dev_off = 0, out_base = 0, brk_base = 0;
-    uint32_t tile = 0;
     for (size_t i = 0; i < n; i++) {
         Segment& g = ctx->h_segs[i];
         g.dev_off = dev_off;
@@ -701,15 +724,11 @@ cj_status stage_batch(cj_context* ctx, const uint8_t* const* docs, const uint8_t
         g.logical_off = 0;
         g.out_base = out_base;
         g.brk_base = brk_base;
-        g.first_tile = tile;
-        g.n_tiles = (uint32_t)((sizes[i] + kTileBytes - 1) / kTileBytes);
         g.flags = 0;
         g.pad = 0;
-        for (uint32_t t = 0; t < g.n_tiles; t++) ctx->h_tile_seg[tile + t] = (uint32_t)i;
         dev_off += round_up(sizes[i], kPadBytes);
         out_base += sizes[i] + 1;
         brk_base += round_up(sizes[i], kChunk);
-        tile += g.n_tiles;
     }
     if (tables_only) {
         // the caller copies the data (cj_parse_batch_padded)
@@ -734,10 +753,7 @@ cj_status stage_batch(cj_context* ctx, const uint8_t* const* docs, const uint8_t
             CJ_CUDA(cudaMemcpyAsync(ctx->in.p + ctx->h_segs[i].dev_off, docs[i], sizes[i],
                                     cudaMemcpyHostToDevice, ctx->stream));
     }
-    CJ_CUDA(cudaMemcpyAsync(ctx->segs.p, ctx->h_segs.data(), n * sizeof(Segment), cudaMemcpyHostToDevice,
-                            ctx->stream));
-    CJ_CUDA(cudaMemcpyAsync(ctx->tile_seg.p, ctx->h_tile_seg.data(), tiles * sizeof(uint32_t),
-                            cudaMemcpyHostToDevice, ctx->stream));
+    if ((st = place_regions(ctx))) return st;
     if (packed && !tables_only) {
         launch_batch_scatter(ctx->pack.p, ctx->pack_off.p, ctx->pack_off.p + n + 1, ctx->segs.p, (uint32_t)n,
                              ctx->h_pack_off[2 * n + 1], ctx->in.p, ctx->sm_count, ctx->stream);
@@ -748,7 +764,6 @@ cj_status stage_batch(cj_context* ctx, const uint8_t* const* docs, const uint8_t
     CJ_CUDA(cudaStreamSynchronize(ctx->stream));   // host vectors must outlive the copies
     ctx->n_bytes = total;
     ctx->n_segs = (uint32_t)n;
-    ctx->n_tiles = tile;
     ctx->lines = lines;
     ctx->batch = true;
     ctx->batch_read = false;
@@ -759,7 +774,7 @@ cj_status stage_batch(cj_context* ctx, const uint8_t* const* docs, const uint8_t
 
 // A batch whose host buffer already has the device layout (every document at
 // its 1 KiB-aligned offset, cj_batch_padded_offsets): the run starts at once
-// and the copy follows on the copy stream in chunks; the scan hands out a tile
+// and the copy follows on the copy stream in chunks; the scan takes a region
 // once the bytes counter covers it (as in stage_overlapped).  Without the
 // driver's stream write the copy simply precedes the run.
 cj_status parse_batch_padded(cj_context* ctx, const uint8_t* padded, const size_t* sizes, size_t n, bool lines)
@@ -819,6 +834,7 @@ cj_status read_batch(cj_context* ctx)
 cj_status doc_verdict(const cj_context* ctx, size_t i)
 {
     if (ctx->h_ctrl->error_flags & CJ_FLAG_TIMEOUT) return CJ_ERR_TIMEOUT;
+    if (ctx->h_ctrl->error_flags & CJ_FLAG_OVERFLOW) return CJ_ERR_CUDA;   // inconsistent scan counts
     const uint32_t e = ctx->h_seg_err[i];
     if (e & CJ_FLAG_UTF8) return CJ_ERR_INVALID_UTF8;
     if (e & CJ_FLAG_BRACKETS) return CJ_ERR_INVALID_BRACKETS;
@@ -842,16 +858,11 @@ cj_status cj_context_create(int device, cj_context** out)
     CJ_CUDA(cudaSetDevice(device));
     cj_context* ctx = new cj_context();
     ctx->device = device;
-    cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
-    int per_sm = 0;
-    if (scan_configure() != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, scan_kernel_ptr(), kThreads,
-                                                      scan_smem_bytes()) != cudaSuccess ||
-        per_sm < 1) {
+    if (cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        ctx->sm_count < 1) {
         delete ctx;
         return CJ_ERR_CUDA;
     }
-    ctx->scan_grid = (uint32_t)(per_sm * ctx->sm_count);
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_reset, cudaEventDisableTiming) != cudaSuccess ||
@@ -885,8 +896,8 @@ void cj_context_destroy(cj_context* ctx)
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     release(ctx->in); release(ctx->pos); release(ctx->pair); release(ctx->brk);
-    release(ctx->desc_flag); release(ctx->desc_agg); release(ctx->desc_incl);
-    release(ctx->segs); release(ctx->seg_out); release(ctx->tile_seg);
+    release(ctx->rtab); release(ctx->rentry); release(ctx->bagg); release(ctx->work);
+    release(ctx->segs); release(ctx->seg_out); release(ctx->region_seg);
     release(ctx->spine); release(ctx->cinfo); release(ctx->tree);
     release(ctx->seg_err); release(ctx->seg_depth); release(ctx->rchunk_off);
     release(ctx->layout_off); release(ctx->layout); release(ctx->pack); release(ctx->pack_off);
@@ -921,17 +932,37 @@ cj_status cj_context_phase_ms(cj_context* ctx, double* scan_ms, double* pair_ms,
     if (!ctx) return CJ_ERR_INVALID_ARGUMENT;
     CJ_CUDA(cudaStreamSynchronize(ctx->stream));
     double a = 0, b = 0, c = 0;
-    for (size_t i = 0; i + 4 <= ctx->events_used; i += 4) {
+    for (size_t i = 0; i + kEventsPerRun <= ctx->events_used; i += kEventsPerRun) {
+        float x = 0, y = 0, z = 0;
+        CJ_CUDA(cudaEventElapsedTime(&x, ctx->events[i], ctx->events[i + 3]));
+        CJ_CUDA(cudaEventElapsedTime(&y, ctx->events[i + 3], ctx->events[i + 4]));
+        CJ_CUDA(cudaEventElapsedTime(&z, ctx->events[i + 4], ctx->events[i + 5]));
+        a += x; b += y; c += z;
+    }
+    if (scan_ms) *scan_ms = a;
+    if (pair_ms) *pair_ms = b;
+    if (spine_ms) *spine_ms = c;
+    if (runs) *runs = (int64_t)(ctx->events_used / kEventsPerRun);
+    return CJ_OK;
+}
+
+cj_status cj_context_scan_phase_ms(cj_context* ctx, double* tables_ms, double* prefix_ms, double* emit_ms,
+                                   int64_t* runs)
+{
+    if (!ctx) return CJ_ERR_INVALID_ARGUMENT;
+    CJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    double a = 0, b = 0, c = 0;
+    for (size_t i = 0; i + kEventsPerRun <= ctx->events_used; i += kEventsPerRun) {
         float x = 0, y = 0, z = 0;
         CJ_CUDA(cudaEventElapsedTime(&x, ctx->events[i], ctx->events[i + 1]));
         CJ_CUDA(cudaEventElapsedTime(&y, ctx->events[i + 1], ctx->events[i + 2]));
         CJ_CUDA(cudaEventElapsedTime(&z, ctx->events[i + 2], ctx->events[i + 3]));
         a += x; b += y; c += z;
     }
-    if (scan_ms) *scan_ms = a;
-    if (pair_ms) *pair_ms = b;
-    if (spine_ms) *spine_ms = c;
-    if (runs) *runs = (int64_t)(ctx->events_used / 4);
+    if (tables_ms) *tables_ms = a;
+    if (prefix_ms) *prefix_ms = b;
+    if (emit_ms) *emit_ms = c;
+    if (runs) *runs = (int64_t)(ctx->events_used / kEventsPerRun);
     return CJ_OK;
 }
 
@@ -939,7 +970,7 @@ cj_status cj_context_span_ms(cj_context* ctx, double* ms)
 {
     if (!ctx || !ms) return CJ_ERR_INVALID_ARGUMENT;
     *ms = 0;
-    if (ctx->events_used < 4) return CJ_OK;
+    if (ctx->events_used < kEventsPerRun) return CJ_OK;
     CJ_CUDA(cudaStreamSynchronize(ctx->stream));
     float x = 0;
     CJ_CUDA(cudaEventElapsedTime(&x, ctx->events[0], ctx->events[ctx->events_used - 1]));
@@ -1149,21 +1180,35 @@ cj_status cj_run_staged_graph(cj_context* ctx)
 cj_status cj_context_set_tuning(cj_context* ctx, const cj_tuning* t)
 {
     if (!ctx) return CJ_ERR_INVALID_ARGUMENT;
-    uint32_t sc = t ? (uint32_t)std::max(0, t->scan_ctas) : 0u;
-    uint32_t pb = t ? (uint32_t)std::max(0, t->pair_blocks) : 0u;
-    uint32_t pt = t ? (uint32_t)std::max(0, t->pair_threads) : 0u;
+    const int rk = t ? std::max(0, t->region_kib) : 0;
+    const int tb = t ? std::max(0, t->scan_blocks_per_sm) : 0;
+    const int eb = t ? std::max(0, t->emit_blocks_per_sm) : 0;
+    const uint32_t pb = t ? (uint32_t)std::max(0, t->pair_blocks) : 0u;
+    const uint32_t pt = t ? (uint32_t)std::max(0, t->pair_threads) : 0u;
     if (pt && pt != 64 && pt != 128 && pt != 256) return CJ_ERR_INVALID_ARGUMENT;
-    ctx->tune_scan_ctas = sc;
+    if (rk && !region_steps_valid(rk)) return CJ_ERR_INVALID_ARGUMENT;
+    ctx->tune_region_steps = rk;
+    ctx->tune_tables_per_sm = tb;
+    ctx->tune_emit_per_sm = eb;
     ctx->tune_pair_blocks = pb;
     ctx->tune_pair_threads = pt;
     ctx->graph_valid = false;
+    if (ctx->staged && ctx->run_region_steps != region_steps(ctx)) {
+        // the staged input is cut into regions of the new size
+        CJ_CUDA(cudaSetDevice(ctx->device));
+        cj_status st = place_regions(ctx);
+        if (st) { ctx->staged = false; return st; }
+        CJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
     return CJ_OK;
 }
 
 cj_status cj_context_get_tuning(cj_context* ctx, cj_tuning* t)
 {
     if (!ctx || !t) return CJ_ERR_INVALID_ARGUMENT;
-    t->scan_ctas = (int32_t)(ctx->tune_scan_ctas ? std::min(ctx->tune_scan_ctas, ctx->scan_grid) : ctx->scan_grid);
+    t->region_kib = region_steps(ctx) * kStepBytes / 1024;
+    t->scan_blocks_per_sm = ctx->tune_tables_per_sm;
+    t->emit_blocks_per_sm = ctx->tune_emit_per_sm;
     t->pair_blocks = (int32_t)ctx->tune_pair_blocks;
     t->pair_threads = (int32_t)pair_threads(ctx);
     t->ms = 0.f;
@@ -1176,29 +1221,32 @@ cj_status cj_autotune_staged(cj_context* ctx, int32_t reps, cj_tuning* best, cj_
     if (!ctx || reps < 1) return finish(CJ_ERR_INVALID_ARGUMENT);
     if (!ctx->staged) return finish(CJ_ERR_NOT_STAGED);
     CJ_CUDA(cudaSetDevice(ctx->device));
-    const uint32_t full = ctx->scan_grid, sm = (uint32_t)ctx->sm_count;
+    const uint32_t sm = (uint32_t)ctx->sm_count;
+    // region size (4, 8, 16 KiB) x resident scan blocks per SM (as many as
+    // fit, or 2) x pairing threads per block x pairing blocks
     std::vector<cj_tuning> cand;
-    for (uint32_t scan : {full, std::max(1u, full * 3 / 4), std::max(1u, full / 2)})
-        for (int pt : {128, 256})
-            for (uint32_t pb : {0u, sm * 2, sm * 4}) {
-                cj_tuning t;
-                t.scan_ctas = (int32_t)scan;
-                t.pair_threads = pt;
-                t.pair_blocks = (int32_t)pb;
-                t.ms = 0.f;
-                cand.push_back(t);
-            }
+    for (int rk : {4, 8, 16})
+        for (int tb : {0, 2})
+            for (int pt : {128, 256})
+                for (uint32_t pb : {0u, sm * 4}) {
+                    cj_tuning t;
+                    t.region_kib = rk;
+                    t.scan_blocks_per_sm = tb;
+                    t.emit_blocks_per_sm = tb;
+                    t.pair_threads = pt;
+                    t.pair_blocks = (int32_t)pb;
+                    t.ms = 0.f;
+                    cand.push_back(t);
+                }
     cudaEvent_t e0, e1;
     CJ_CUDA(cudaEventCreate(&e0));
     CJ_CUDA(cudaEventCreate(&e1));
-    cj_tuning keep;
-    cj_context_get_tuning(ctx, &keep);
     float best_ms = 1e30f;
     cj_tuning win = cand[0];
     size_t k = 0;
     for (cj_tuning& t : cand) {
-        cj_context_set_tuning(ctx, &t);
-        cj_status st = run_graph(ctx);   // capture + one untimed replay
+        cj_status st = cj_context_set_tuning(ctx, &t);
+        if (!st) st = run_graph(ctx);   // capture + one untimed replay
         if (st) { cudaEventDestroy(e0); cudaEventDestroy(e1); return finish(st); }
         if (cudaEventRecord(e0, ctx->stream) != cudaSuccess) return finish(CJ_ERR_CUDA);
         for (int r = 0; r < reps; r++)
@@ -1215,7 +1263,8 @@ cj_status cj_autotune_staged(cj_context* ctx, int32_t reps, cj_tuning* best, cj_
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (n_tried) *n_tried = k;
-    cj_context_set_tuning(ctx, &win);
+    cj_status st = cj_context_set_tuning(ctx, &win);
+    if (st) return finish(st);
     if (best) *best = win;
     return finish(CJ_OK);
 }

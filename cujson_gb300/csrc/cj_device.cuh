@@ -16,19 +16,17 @@ namespace cj {
 // ---- tiling ---------------------------------------------------------------
 // A warp step is what one warp classifies at once: 32 lanes x 32 bytes, so a
 // lane owns one 32-bit word of every character-class bitmap (bit j = byte j
-// of its 32 bytes).  Each warp of a CTA owns a contiguous region of
-// kStepsPerWarp steps and carries the escape / string state across its steps
-// by itself; a tile is the kWarps regions of one CTA, and the cross-tile carry
-// (decoupled look-back) runs once per tile.
-constexpr int kWarps = 16;                                // classifying warps per CTA
-constexpr int kCoords = 2;                                // coordinator warps (tickets in turn)
-constexpr int kThreads = (kWarps + kCoords) * 32;
+// of its 32 bytes).  A region is what one warp scans as a unit: kRegionSteps
+// consecutive steps of one segment (the last region of a segment may be
+// shorter).  The scan computes one transfer table per region, composes them
+// in document order, and then emits each region's outputs from its entry
+// value.  The region size is chosen per run from kRegionStepsAllowed.
 constexpr int kBytesPerThread = 32;
-constexpr int kStepBytes = 32 * kBytesPerThread;          // 1 KiB, one TMA copy
-constexpr int kStepsPerWarp = 7;
-constexpr int kWarpBytes = kStepBytes * kStepsPerWarp;    // 7 KiB per warp region
-constexpr int kTileBytes = kWarpBytes * kWarps;           // 112 KiB per tile
+constexpr int kStepBytes = 32 * kBytesPerThread;          // 1 KiB
 constexpr int kPadBytes = kStepBytes;                     // segment padding granule
+constexpr int kRegionStepsAllowed[3] = {4, 8, 16};        // 4, 8 or 16 KiB regions
+constexpr int kRegionStepsDefault = 8;
+constexpr int kPrefixPerBlock = 1024;                     // regions per block of the prefix kernels
 
 // Pairing: one warp matches a chunk of this many bracket records.
 constexpr int kChunk = 512;
@@ -38,7 +36,7 @@ constexpr int kTreeLevels = 6;           // min-tree levels above the chunk arra
 // ---- segments ---------------------------------------------------------------
 // A segment is one standard document or one JSON-Lines chunk.  Segments start
 // on kPadBytes boundaries of the device input and are padded to a whole number
-// of warp steps; tiles are counted per segment.  Escape/string state and depth start
+// of warp steps; regions are counted per segment.  Escape/string state and depth start
 // afresh in every segment; structural and bracket counts continue from the
 // previous segment when kSegContinue is set (JSON-Lines: one merged result),
 // and restart at 0 otherwise (independent documents).
@@ -50,13 +48,13 @@ struct Segment {
     uint64_t logical_off;  // added to byte positions (reference lastChunkIndex)
     uint64_t out_base;     // output index base (independent documents)
     uint64_t brk_base;     // bracket-record base (independent documents)
-    uint32_t first_tile;
-    uint32_t n_tiles;
+    uint32_t first_region;
+    uint32_t n_regions;
     uint32_t flags;
     uint32_t pad;
 };
 
-struct SegmentOut {        // written by the last tile of each segment
+struct SegmentOut {        // written by the prefix kernel for each segment's last region
     uint32_t s_end;        // structural count at segment end (global if continuing)
     uint32_t k_end;        // bracket count at segment end
     int32_t  depth_end;    // nesting depth at segment end (0 when balanced)
@@ -65,30 +63,34 @@ struct SegmentOut {        // written by the last tile of each segment
 
 // Control block, zeroed before every run.
 struct Ctrl {
-    uint32_t tile_ticket;     // tiles handed out in launch order
+    uint32_t n_work;          // regions with structurals to emit (the emit kernel's work list)
     uint32_t error_flags;     // CJ_FLAG_* bits
     uint32_t s_total;
     uint32_t k_total;
     int32_t  neg_min_level;   // max(-level) over brackets; > 0 means a close below depth 0
     int32_t  max_depth;
-    uint32_t n_tiles_done;
-    uint32_t gave_up;         // the first bounded wait that expired (scan kernel's wait codes), 0 if none
+    uint32_t n_regions_done;
+    uint32_t gave_up;         // the first bounded wait that expired (kGave* codes), 0 if none
 };
 
-// ---- look-back descriptors -------------------------------------------------
-// Entry state of a tile: bit1 = previous byte is an unescaped backslash (the
-// first byte is escaped), bit0 = inside a string.  A tile's aggregate maps each
+// where a bounded wait gave up (Ctrl::gave_up)
+enum : uint32_t { kGaveInput = 6 };
+
+// ---- region transfer tables ---------------------------------------------------
+// Entry state of a region: bit1 = previous byte is an unescaped backslash (the
+// first byte is escaped), bit0 = inside a string.  A region's table maps each
 // of the 4 entry states to (exit state, structural count, bracket count, depth
-// delta); bit 2 of `st` marks a depth reset (segment start: depth restarts).
+// delta).  Bit 2 of `st` marks a state and depth reset (a segment's first
+// region: it starts outside strings at depth 0), bit 3 a count reset (an
+// independent document's first region: its counts start at 0).
 struct Ent {
-    uint32_t st;   // bits 0-1 exit state, bit 2 depth reset
+    uint32_t st;   // bits 0-1 exit state, bit 2 state/depth reset, bit 3 count reset
     uint32_t s;
     uint32_t k;
     int32_t  d;
 };
 
-constexpr uint32_t kFlagAgg = 1u;
-constexpr uint32_t kFlagIncl = 2u;
+constexpr uint32_t kResetState = 4u, kResetCounts = 8u;
 
 CJ_HD Ent ent_identity(uint32_t state) { Ent e; e.st = state; e.s = 0; e.k = 0; e.d = 0; return e; }
 
@@ -99,14 +101,14 @@ CJ_HD Ent ent_select(const Ent t[4], uint32_t i) {
     return (i & 2u) ? hi : lo;
 }
 
-// value v (state, counts, absolute depth) followed by tile table t
+// value v (state, counts, absolute depth) followed by table t
 CJ_HD Ent ent_apply(Ent v, const Ent t[4]) {
     const Ent x = ent_select(t, v.st & 3u);
     Ent r;
     r.st = x.st & 3u;
-    r.s = v.s + x.s;
-    r.k = v.k + x.k;
-    r.d = (x.st & 4u) ? x.d : v.d + x.d;
+    r.s = (x.st & kResetCounts) ? x.s : v.s + x.s;
+    r.k = (x.st & kResetCounts) ? x.k : v.k + x.k;
+    r.d = (x.st & kResetState) ? x.d : v.d + x.d;
     return r;
 }
 
@@ -116,10 +118,10 @@ CJ_HD void tab_compose(const Ent a[4], const Ent b[4], Ent out[4]) {
     for (int s = 0; s < 4; s++) {
         const Ent x = a[s];
         const Ent y = ent_select(b, x.st & 3u);
-        tmp[s].st = (y.st & 3u) | ((x.st | y.st) & 4u);
-        tmp[s].s = x.s + y.s;
-        tmp[s].k = x.k + y.k;
-        tmp[s].d = (y.st & 4u) ? y.d : x.d + y.d;
+        tmp[s].st = (y.st & 3u) | ((x.st | y.st) & (kResetState | kResetCounts));
+        tmp[s].s = (y.st & kResetCounts) ? y.s : x.s + y.s;
+        tmp[s].k = (y.st & kResetCounts) ? y.k : x.k + y.k;
+        tmp[s].d = (y.st & kResetState) ? y.d : x.d + y.d;
     }
     for (int s = 0; s < 4; s++) out[s] = tmp[s];
 }

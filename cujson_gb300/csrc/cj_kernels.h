@@ -11,26 +11,39 @@ namespace cj {
 struct ScanParams {
     const uint8_t* in;
     const Segment* segs;
-    const uint32_t* tile_seg;   // tile -> segment (nullptr: one segment)
+    const uint32_t* region_seg; // region -> segment (nullptr: one segment)
     uint32_t n_segs;
-    uint32_t n_tiles;
+    uint32_t n_regions;
     int32_t* pos;
     int32_t* pair;
     uint2* brk;
-    uint32_t* desc_flag;
-    uint4* desc_agg;            // 4 entries per tile (tiles of kTileBytes)
-    uint4* desc_incl;           // 1 entry per tile
+    uint64_t out_cap;           // entries of pos and pair
+    uint64_t brk_cap;           // entries of brk
+    uint4* rtab;                // 4 entries per region: transfer tables
+    uint4* rentry;              // 1 per region: entry value (state | work flag, s, k, depth)
+    uint4* bagg;                // 4 per block of kPrefixPerBlock regions: block tables
+    uint32_t* work;             // regions with structurals to emit (ctrl->n_work of them)
     Ctrl* ctrl;
     SegmentOut* seg_out;
-    uint32_t epoch;
     uint32_t* seg_err;          // per-segment verdict bits (independent documents),
                                 // nullptr: verdicts go to ctrl->error_flags
     // Bytes of the input layout (`in`, from its start) already in device
-    // memory, raised by the host's copies while the scan runs; a tile is
-    // handed out once its bytes are there.  nullptr: all input is present.
+    // memory, raised by the host's copies while the scan runs; a region is
+    // scanned once its bytes are there.  nullptr: all input is present.
     const unsigned long long* ready;
     uint32_t input_wait_limit;  // polls before a wait for input gives up (0: default)
+    int region_steps;           // 1 KiB steps per region: 4, 8 or 16
+    int sm_count;
 };
+
+// Launch shape of the scan kernels (0 = as many blocks as fit).
+struct ScanShape {
+    int tables_blocks_per_sm;
+    int emit_blocks_per_sm;
+};
+
+// scratch sizes of one scan over `n_regions` regions
+inline uint64_t prefix_blocks(uint64_t n_regions) { return (n_regions + kPrefixPerBlock - 1) / kPrefixPerBlock; }
 
 struct PairParams {
     const uint2* brk;
@@ -62,10 +75,12 @@ struct PairParams {
 // cinfo fill of a batch chunk without records (bytes 0x7F): above every level
 constexpr int32_t kNoLevel = 0x7F7F7F7F;
 
-void launch_scan(const ScanParams& p, bool lines, int grid, cudaStream_t stream);
-cudaError_t scan_configure();      // opt in to the scan kernel's dynamic shared memory
-size_t scan_smem_bytes();
-const void* scan_kernel_ptr();     // for occupancy queries
+// tables, (block reduce,) apply, emit: scan_launches(n) kernels on `stream`
+// `ev` (optional): 3 events recorded after the table, prefix and emit kernels
+void launch_scan(const ScanParams& p, bool lines, const ScanShape& shape, cudaStream_t stream,
+                 cudaEvent_t* ev = nullptr);
+int scan_launches(uint32_t n_regions);
+bool region_steps_valid(int r);
 void launch_pair(const PairParams& p, int grid, cudaStream_t stream, int threads = 256);
 void launch_spine(const PairParams& p, int grid, cudaStream_t stream, int threads = 256);
 

@@ -8,8 +8,9 @@
 // stall unrelated streams.  This entry point allocates nothing, on the device
 // or the host.  Its scratch is one file-scope __device__ array sized for
 // documents of up to CJ_NOALLOC_MAX_BYTES; the input and the output are the
-// caller's own device buffers.  It runs the same three kernels as the arena
-// path (scan, pair, spine) plus one that writes the reference layout.
+// caller's own device buffers.  It runs the same kernels as the arena path
+// (the scan's tables, prefix and emit kernels, then pair and spine) plus one
+// that writes the reference layout.
 //
 // The scratch is shared by every call on a device, so calls on one device
 // must not overlap: two calls in flight at once (from two host threads, or on
@@ -31,7 +32,9 @@ constexpr size_t up(size_t x, size_t m) { return (x + m - 1) / m * m; }
 
 constexpr size_t kMax = CJ_NOALLOC_MAX_BYTES;
 constexpr size_t kInBytes = up(kMax, kPadBytes) + kPadBytes;
-constexpr size_t kTiles = kMax / kTileBytes + 2;
+constexpr int kRegionSteps = kRegionStepsDefault;
+constexpr size_t kRegions = kMax / ((size_t)kRegionSteps * kStepBytes) + 2;
+constexpr size_t kPrefixBlocks = (kRegions + kPrefixPerBlock - 1) / kPrefixPerBlock;
 constexpr size_t kScap = kMax + 1;                        // S <= bytes
 constexpr size_t kChunks = (kMax + kChunk - 1) / kChunk + 1;
 
@@ -45,9 +48,10 @@ struct alignas(256) Scratch {
     alignas(256) int32_t pos[kScap];
     alignas(256) int32_t pair[kScap];
     alignas(256) uint2 brk[kScap];
-    alignas(256) uint32_t desc_flag[kTiles];
-    alignas(256) uint4 desc_agg[kTiles * 4];
-    alignas(256) uint4 desc_incl[kTiles];
+    alignas(256) uint4 rtab[kRegions * 4];
+    alignas(256) uint4 rentry[kRegions];
+    alignas(256) uint4 bagg[kPrefixBlocks * 4];
+    alignas(256) uint32_t work[kRegions];
     alignas(256) uint32_t spine[kChunks * kChunk];
     alignas(256) int4 cinfo[kChunks];
     alignas(256) unsigned long long tree[kTree];
@@ -57,15 +61,14 @@ struct alignas(256) Scratch {
 };
 
 // The scratch itself (about 21 MiB for the 1 MiB limit).  Zero at load; the
-// descriptor flags and the min-tree are epoch-tagged, and are cleared again
-// when the epoch wraps and on the first call on a device.
+// pairing min-tree is epoch-tagged, and is cleared again when the epoch wraps
+// and on the first call on a device.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(Scratch)];
 
 struct DeviceState {
     bool ready = false;
     Scratch* scratch = nullptr;
     int sm_count = 0;
-    uint32_t scan_grid = 0;
     uint32_t epoch = 0;
 };
 
@@ -83,8 +86,8 @@ __global__ void noalloc_setup(Scratch* s, uint64_t n)
     seg.logical_off = 0;
     seg.out_base = 0;
     seg.brk_base = 0;
-    seg.first_tile = 0;
-    seg.n_tiles = (uint32_t)((n + kTileBytes - 1) / kTileBytes);
+    seg.first_region = 0;
+    seg.n_regions = (uint32_t)((n + (uint64_t)kRegionSteps * kStepBytes - 1) / ((uint64_t)kRegionSteps * kStepBytes));
     seg.flags = 0;
     seg.pad = 0;
     s->seg = seg;
@@ -129,9 +132,8 @@ cj_status cuda_status(cudaError_t e)
     return e == cudaSuccess ? CJ_OK : CJ_ERR_CUDA;
 }
 
-// One-time setup for the current device: resolve the scratch address, opt
-// the scan kernel in to its shared memory, size the persistent grid, clear
-// the epoch-tagged arrays.
+// One-time setup for the current device: resolve the scratch address and
+// clear the epoch-tagged min-tree.
 cj_status device_setup(int dev, cudaStream_t stream, DeviceState& d)
 {
     void* ptr = nullptr;
@@ -139,21 +141,13 @@ cj_status device_setup(int dev, cudaStream_t stream, DeviceState& d)
     if (e != cudaSuccess || !ptr) return CJ_ERR_CUDA;
     if (cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return CJ_ERR_CUDA;
-    int per_sm = 0;
-    if (scan_configure() != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, scan_kernel_ptr(), kThreads,
-                                                      scan_smem_bytes()) != cudaSuccess ||
-        per_sm < 1)
-        return CJ_ERR_CUDA;
     Scratch* s = static_cast<Scratch*>(ptr);
     // cleared and finished before the call goes on, so no later call, on any
-    // stream, can run beside these clears
-    if (cudaMemsetAsync(s->desc_flag, 0, sizeof(s->desc_flag), stream) != cudaSuccess ||
-        cudaMemsetAsync(s->tree, 0, sizeof(s->tree), stream) != cudaSuccess ||
+    // stream, can run beside this clear
+    if (cudaMemsetAsync(s->tree, 0, sizeof(s->tree), stream) != cudaSuccess ||
         cudaStreamSynchronize(stream) != cudaSuccess)
         return CJ_ERR_CUDA;
     d.scratch = s;
-    d.scan_grid = (uint32_t)(per_sm * d.sm_count);
     d.epoch = 0;
     d.ready = true;
     return CJ_OK;
@@ -182,8 +176,7 @@ cj_status parse_noalloc(const uint8_t* d_data, size_t size, int32_t* d_out, size
         d->epoch = (d->epoch + 1) & 0x3FFFFFFFu;
         if (d->epoch == 0) {
             Scratch* s = d->scratch;
-            if (cudaMemsetAsync(s->desc_flag, 0, sizeof(s->desc_flag), stream) != cudaSuccess ||
-                cudaMemsetAsync(s->tree, 0, sizeof(s->tree), stream) != cudaSuccess ||
+            if (cudaMemsetAsync(s->tree, 0, sizeof(s->tree), stream) != cudaSuccess ||
                 cudaStreamSynchronize(stream) != cudaSuccess)
                 return CJ_ERR_CUDA;
             d->epoch = 1;
@@ -191,7 +184,8 @@ cj_status parse_noalloc(const uint8_t* d_data, size_t size, int32_t* d_out, size
         epoch = d->epoch;
     }
     Scratch* s = d->scratch;
-    const uint32_t n_tiles = (uint32_t)((size + kTileBytes - 1) / kTileBytes);
+    const uint32_t n_regions = (uint32_t)((size + (uint64_t)kRegionSteps * kStepBytes - 1) /
+                                          ((uint64_t)kRegionSteps * kStepBytes));
 
     cj_status st;
     if ((st = cuda_status(cudaMemcpyAsync(s->in, d_data, size, cudaMemcpyDeviceToDevice, stream)))) return st;
@@ -200,19 +194,23 @@ cj_status parse_noalloc(const uint8_t* d_data, size_t size, int32_t* d_out, size
     ScanParams sp{};
     sp.in = s->in;
     sp.segs = &s->seg;
-    sp.tile_seg = nullptr;
+    sp.region_seg = nullptr;
     sp.n_segs = 1;
-    sp.n_tiles = n_tiles;
+    sp.n_regions = n_regions;
     sp.pos = s->pos;
     sp.pair = s->pair;
     sp.brk = s->brk;
-    sp.desc_flag = s->desc_flag;
-    sp.desc_agg = s->desc_agg;
-    sp.desc_incl = s->desc_incl;
+    sp.out_cap = kScap;
+    sp.brk_cap = kScap;
+    sp.rtab = s->rtab;
+    sp.rentry = s->rentry;
+    sp.bagg = s->bagg;
+    sp.work = s->work;
     sp.ctrl = &s->ctrl;
     sp.seg_out = &s->seg_out;
-    sp.epoch = epoch;
-    launch_scan(sp, false, (int)std::min<uint32_t>(n_tiles, d->scan_grid), stream);
+    sp.region_steps = kRegionSteps;
+    sp.sm_count = d->sm_count;
+    launch_scan(sp, false, ScanShape{0, 0}, stream);
 
     PairParams pp{};
     pp.brk = s->brk;
@@ -249,6 +247,7 @@ cj_status parse_noalloc(const uint8_t* d_data, size_t size, int32_t* d_out, size
     if (c.neg_min_level > 0) flags |= CJ_FLAG_BRACKETS;
     cj_status verdict = CJ_OK;
     if (flags & CJ_FLAG_TIMEOUT) verdict = CJ_ERR_TIMEOUT;
+    else if (flags & CJ_FLAG_OVERFLOW) verdict = CJ_ERR_CUDA;     // inconsistent scan counts (a defect)
     else if (flags & CJ_FLAG_UTF8) verdict = CJ_ERR_INVALID_UTF8;
     else if (flags & CJ_FLAG_BRACKETS) verdict = CJ_ERR_INVALID_BRACKETS;
     if (info) {

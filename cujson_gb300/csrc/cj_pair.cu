@@ -33,15 +33,24 @@ namespace cj {
 
 namespace {
 
+// (CJ_EMU: the CPU emulation of the kernels in tests/emu, test infrastructure)
 __device__ __forceinline__ uint32_t lanemask_lt() {
+#ifdef CJ_EMU
+    return (1u << (threadIdx.x & 31)) - 1u;
+#else
     uint32_t m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
     return m;
+#endif
 }
 __device__ __forceinline__ uint32_t lanemask_gt() {
+#ifdef CJ_EMU
+    return ~((2u << (threadIdx.x & 31)) - 1u);
+#else
     uint32_t m;
     asm("mov.u32 %0, %%lanemask_gt;" : "=r"(m));
     return m;
+#endif
 }
 
 __device__ __forceinline__ unsigned long long tree_pack(uint32_t epoch, int32_t level) {
@@ -102,12 +111,18 @@ __device__ __forceinline__ uint32_t doc_of_item(const PairParams& P, uint64_t w)
 
 __global__ void __launch_bounds__(256) pair_chunks(PairParams P)
 {
+#ifdef CJ_EMU
+    uint32_t* s_heads_all = reinterpret_cast<uint32_t*>(cj_emu::g_dyn_smem.data());
+#else
     extern __shared__ uint32_t s_heads_all[];
+#endif
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     uint32_t* heads = s_heads_all + wib * kHeads;
     const uint32_t FULL = 0xFFFFFFFFu;
     const bool batch = P.rchunk_off != nullptr;
+    // a scan whose emitted records disagree with its counts is not paired
+    if (__ldcg(&P.ctrl->error_flags) & CJ_FLAG_OVERFLOW) return;
     const uint32_t K = batch ? 0u : P.ctrl->k_total;
     const uint64_t items = batch ? __ldcg(P.rchunk_off + P.n_bsegs) : ((uint64_t)K + kChunk - 1) / kChunk;
     const uint64_t gwarp = (uint64_t)blockIdx.x * (blockDim.x >> 5) + wib;
@@ -117,7 +132,7 @@ __global__ void __launch_bounds__(256) pair_chunks(PairParams P)
     for (uint64_t w = gwarp; w < items; w += nwarps) {
         uint64_t c = w;
         int cnt;
-        uint32_t segi = 0;
+        uint32_t segi = 0, S;
         int32_t* __restrict__ pair = P.pair;
         if (batch) {
             segi = doc_of_item(P, w);
@@ -126,8 +141,10 @@ __global__ void __launch_bounds__(256) pair_chunks(PairParams P)
             const uint64_t left = (uint64_t)__ldcg(&P.seg_out[segi].k_end) - local * kChunk;
             cnt = (int)min((uint64_t)kChunk, left);
             pair += __ldg(&P.segs[segi].out_base);
+            S = __ldcg(&P.seg_out[segi].s_end);
         } else {
             cnt = (int)min((uint64_t)kChunk, (uint64_t)K - c * kChunk);
+            S = P.ctrl->s_total;
         }
         const uint64_t base = c * kChunk;
         uint32_t err = 0;
@@ -180,7 +197,8 @@ __global__ void __launch_bounds__(256) pair_chunks(PairParams P)
                 }
                 if (partner != kEmpty) {
                     if ((partner ^ rec.x) & kCurly) err |= CJ_FLAG_BRACKETS;
-                    pair[partner & ~kCurly] = (int32_t)((rec.x & ~kCurly) + 1u);
+                    if ((partner & ~kCurly) < S) pair[partner & ~kCurly] = (int32_t)((rec.x & ~kCurly) + 1u);
+                    else err |= CJ_FLAG_BRACKETS;
                 }
             }
             __syncwarp();
@@ -234,6 +252,7 @@ __global__ void __launch_bounds__(256) pair_spine(PairParams P)
 {
     const int lane = threadIdx.x & 31;
     const bool batch = P.rchunk_off != nullptr;
+    if (__ldcg(&P.ctrl->error_flags) & CJ_FLAG_OVERFLOW) return;
     const uint32_t K = batch ? 0u : P.ctrl->k_total;
     const uint64_t nch = batch ? P.n_chunks : ((uint64_t)K + kChunk - 1) / kChunk;
     const uint64_t items = batch ? __ldcg(P.rchunk_off + P.n_bsegs) : nch;
@@ -285,12 +304,22 @@ void launch_pair(const PairParams& p, int grid, cudaStream_t stream, int threads
     // one bucket-head table per warp: 4.1 KB each, 32.8 KB at 256 threads
     // (threads <= 256 stays under the 48 KB default)
     const size_t smem = sizeof(uint32_t) * kHeads * (size_t)(threads / 32);
+#ifdef CJ_EMU
+    (void)stream;
+    cj_emu::launch(grid, threads, smem, [&] { pair_chunks(p); });
+#else
     pair_chunks<<<grid, threads, smem, stream>>>(p);
+#endif
 }
 
 void launch_spine(const PairParams& p, int grid, cudaStream_t stream, int threads)
 {
+#ifdef CJ_EMU
+    (void)stream;
+    cj_emu::launch(grid, threads, 0, [&] { pair_spine(p); });
+#else
     pair_spine<<<grid, threads, 0, stream>>>(p);
+#endif
 }
 
 }  // namespace cj

@@ -58,11 +58,10 @@ typedef enum cj_status {
 #define CJ_FLAG_UTF8        0x01u
 #define CJ_FLAG_BRACKETS    0x02u
 #define CJ_FLAG_TIMEOUT     0x04u
-#define CJ_FLAG_OVERFLOW    0x08u
-/* with CJ_FLAG_TIMEOUT: bits 16-23 say which bounded wait of the scan kernel
- * expired first (1 tile hand-out, 2 end of a tile's phase A, 3 a tile's entry
- * value, 4 look-back, 5 input copy to shared memory, 6 input bytes from the
- * host) */
+#define CJ_FLAG_OVERFLOW    0x08u   /* an output index past its buffer (never with
+                                       consistent counts; the write is dropped) */
+/* with CJ_FLAG_TIMEOUT: bits 16-23 say which bounded wait of the scan expired
+ * first (6: input bytes from the host, the only wait of the scan kernels) */
 #define CJ_TIMEOUT_WAIT(flags) (((flags) >> 16) & 0xFFu)
 
 /* Largest input in bytes: positions are int32 (reference, cujson_types.h:26). */
@@ -176,7 +175,7 @@ cj_status cj_run_staged_graph(cj_context* ctx);
 
 /* Failure-detection check (no reference counterpart): runs the staged input
  * while the device count of input bytes present stays at zero, so the scan's
- * bounded wait for input gives up after `polls` polls per tile; the kernel
+ * bounded wait for input gives up after `polls` polls; the kernel
  * sets its timeout flag, finishes, and the context stays usable.  Returns the
  * run's verdict: CJ_ERR_TIMEOUT. */
 cj_status cj_run_staged_starved(cj_context* ctx, uint32_t polls, cj_parse_info* info);
@@ -228,7 +227,7 @@ cj_status cj_stage_batch_packed(cj_context* ctx, const uint8_t* packed, const si
  * offsets[i] from cj_batch_padded_offsets (1 KiB-aligned, back to back),
  * `*total` bytes in all.  cj_parse_batch_padded launches the run at once and
  * copies the buffer (pinned for the overlap) in chunks behind it: the scan
- * takes a tile as soon as its bytes have arrived, so copy and parse overlap.
+ * takes a region as soon as its bytes have arrived, so copy and parse overlap.
  * Results as after cj_run_staged (cj_batch_info, cj_copy_batch_result). */
 cj_status cj_batch_padded_offsets(const size_t* sizes, size_t n_docs, size_t* offsets, size_t* total);
 cj_status cj_parse_batch_padded(cj_context* ctx, const uint8_t* padded, const size_t* sizes, size_t n_docs,
@@ -238,15 +237,20 @@ cj_status cj_batch_info(cj_context* ctx, int32_t* status, int64_t* n_structural,
 cj_status cj_copy_batch_result(cj_context* ctx, int32_t* host_out, size_t out_cap);
 
 /* ---- launch shapes and the autotuner ----------------------------------------
- * scan_ctas: persistent scan CTAs (at most one per SM fits); pair_blocks and
- * pair_threads (64, 128 or 256): the pairing kernels' grid.  0 = default.
- * cj_autotune_staged times `reps` graph replays of the staged input for each
- * candidate shape, keeps the fastest in the context and reports it (and,
- * optionally, every candidate tried with its mean milliseconds). */
+ * No counterpart in the reference (its launch shapes are constants).  The
+ * scan cuts each document into regions of region_kib; the scan kernels run
+ * scan_blocks_per_sm / emit_blocks_per_sm blocks per SM; the pairing kernels
+ * pair_blocks blocks of pair_threads.  0 = default.  Setting a tuning on a
+ * context with a staged input re-cuts that input into regions of the new
+ * size.  cj_autotune_staged times `reps` graph replays of the staged input
+ * for each candidate shape, keeps the fastest in the context and reports it
+ * (and, optionally, every candidate tried with its mean milliseconds). */
 typedef struct cj_tuning {
-    int32_t scan_ctas;
-    int32_t pair_blocks;
-    int32_t pair_threads;
+    int32_t region_kib;          /* bytes one warp scans as a unit: 4, 8 or 16 KiB (0: 8) */
+    int32_t scan_blocks_per_sm;  /* resident 256-thread blocks per SM of the scan's table and */
+    int32_t emit_blocks_per_sm;  /* emit kernels (0: as many as fit) */
+    int32_t pair_blocks;         /* pairing grid (0: sized to the bracket count) */
+    int32_t pair_threads;        /* pairing threads per block: 64, 128 or 256 (0: 256) */
     float   ms;                  /* mean replay time when measured */
 } cj_tuning;
 cj_status cj_context_set_tuning(cj_context* ctx, const cj_tuning* tuning);   /* NULL: defaults */
@@ -308,6 +312,11 @@ cj_status cj_server_replay(cj_server* s, const uint8_t* const* docs, const size_
 cj_status cj_context_timing(cj_context* ctx, int enable);
 cj_status cj_context_phase_ms(cj_context* ctx, double* scan_ms, double* pair_ms,
                               double* spine_ms, int64_t* runs);
+/* The scan's own split over the same runs: its table kernel (one read of the
+ * input), its prefix kernels and its emit kernel (positions and bracket
+ * records); their sum is the scan time of cj_context_phase_ms. */
+cj_status cj_context_scan_phase_ms(cj_context* ctx, double* tables_ms, double* prefix_ms,
+                                   double* emit_ms, int64_t* runs);
 /* Milliseconds from the first recorded run's start to the last one's end. */
 cj_status cj_context_span_ms(cj_context* ctx, double* ms);
 /* Pinned host memory (cudaMallocHost / cudaFreeHost) for callers without the

@@ -1,0 +1,46 @@
+"""Builds the CPU emulation of the parse kernels: cujson_gb300/csrc/cj_scan.cu
+and cj_pair.cu compiled with g++ against tests/emu/cj_emu.h, with
+tests/emu/cj_emu_driver.cpp, into tests/emu/_build/libcj_emu.so.  Test
+infrastructure only."""
+from __future__ import annotations
+
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+CSRC = ROOT / "cujson_gb300" / "csrc"
+BUILD = HERE / "_build"
+LIB = BUILD / "libcj_emu.so"
+UNITS = [CSRC / "cj_scan.cu", CSRC / "cj_pair.cu", HERE / "cj_emu_driver.cpp"]
+DEPS = UNITS + [HERE / "cj_emu.h", HERE / "shim" / "cuda_runtime.h", CSRC / "cj_device.cuh",
+                CSRC / "cj_kernels.h", ROOT / "include" / "cujson_gb300.h"]
+FLAGS = ["-O1", "-g", "-std=c++17", "-fPIC", "-w", "-DCJ_EMU=1", f"-I{HERE / 'shim'}", f"-I{CSRC}",
+         f"-I{ROOT / 'include'}", "-include", str(HERE / "cj_emu.h")]
+
+
+def _compile(src: Path) -> Path:
+    obj = BUILD / (src.stem + ".o")
+    cmd = ["g++", *FLAGS, "-x", "c++", "-c", str(src), "-o", str(obj)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode:
+        raise RuntimeError(f"emulation build failed for {src.name}:\n{r.stderr[-4000:]}")
+    return obj
+
+
+def build(force: bool = False) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    newest = max(p.stat().st_mtime for p in DEPS)
+    if not force and LIB.exists() and LIB.stat().st_mtime >= newest:
+        return LIB
+    with ThreadPoolExecutor(3) as ex:
+        objs = list(ex.map(_compile, UNITS))
+    r = subprocess.run(["g++", "-shared", "-o", str(LIB), *map(str, objs)], capture_output=True, text=True)
+    if r.returncode:
+        raise RuntimeError(r.stderr)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force=True))

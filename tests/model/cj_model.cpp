@@ -1,10 +1,13 @@
 // cj_model.cpp -- sequential CPU model of the parse kernels (test helper).
 //
-// Runs the scan kernel's algorithm tile by tile and thread by thread, with the
-// same bit functions (cujson_gb300/csrc/cj_device.cuh), the same transfer
-// tables and the same look-back composition, then the pairing kernels' chunk
-// and spine logic with __match_any_sync emulated per 32-record round.  Tests
-// compare it with the oracle to check the algorithm itself without a GPU.
+// Runs the scan kernels' algorithm region by region, with the same bit
+// functions (cujson_gb300/csrc/cj_device.cuh): the per-region transfer tables
+// (computed as if each region were entered outside strings and escapes), their
+// composition in randomly sized blocks (checked against the running value),
+// and the emit pass from each region's exact entry state; then the pairing
+// kernels' chunk and spine logic with __match_any_sync emulated per 32-record
+// round.  Tests compare it with the oracle to check the algorithm itself
+// without a GPU.
 #include <algorithm>
 #include <array>
 #include <climits>
@@ -82,161 +85,174 @@ extern "C" int cjm_parse(const uint8_t* data, size_t n, int lines, const size_t*
     uint32_t flags = 0;
     std::vector<int32_t> pos, pair;
     std::vector<uint2> brk;
-    std::vector<Ent> incl_hist;                    // inclusive value per tile
-    std::vector<std::array<Ent, 4>> agg_hist;      // aggregate table per tile
-    std::vector<bool> immediate_hist;
+    // region size as the tuned kernels choose it (4, 8 or 16 KiB), drawn per call
+    const int R = kRegionStepsAllowed[rng() % 3];
+    const uint64_t RB = (uint64_t)R * kStepBytes;
+    constexpr int W = 16 * kStepBytes / 32;    // 32-byte words of the largest region
 
-    for (const Seg& sg : segs) {
+    // ---- scan_tables: one transfer table per region ------------------------------
+    struct RegionRef { size_t seg; uint64_t off; int len; bool first; };
+    std::vector<RegionRef> regions;
+    std::vector<std::array<Ent, 4>> tabs;
+    for (size_t si = 0; si < segs.size(); si++) {
+        const Seg& sg = segs[si];
         const uint8_t* sb = data + sg.off;
-        uint64_t ntiles = (sg.len + kTileBytes - 1) / kTileBytes;
-        for (uint64_t tin = 0; tin < ntiles; tin++) {
-            const uint64_t tile_off = tin * kTileBytes;
-            const int tile_len = (int)std::min<uint64_t>(kTileBytes, sg.len - tile_off);
-            const bool seg_first = tin == 0, seg_last = tin + 1 == ntiles;
-            const bool immediate = seg_first && !sg.cont;
-            constexpr int W = kTileBytes / 32;    // 32-byte words per tile
+        const uint64_t nreg = (sg.len + RB - 1) / RB;
+        for (uint64_t ri = 0; ri < nreg; ri++) {
+            const uint64_t off = ri * RB;
+            const int len = (int)std::min<uint64_t>(RB, sg.len - off);
+            const bool first = ri == 0;
+            regions.push_back({si, off, len, first});
             static Classes c[W];
             static uint32_t cout0[W];
             static bool all_bs[W];
-            uint32_t ucarry = 0;
-            for (int t = 0; t < W; t++) {
+            const int nw = (len + 31) / 32;
+            // UTF-8 as the kernel checks it: on the bit planes, the carry handed
+            // lane to lane and step to step, and taken afresh from the 4 bytes
+            // before each region
+            uint32_t pw = 0;
+            for (int b = 0; b < 4; b++) {
+                const int64_t o = (int64_t)off - 4 + b;
+                if (o >= 0) pw |= (uint32_t)sb[o] << (8 * b);
+            }
+            uint32_t ucarry = utf8_carry_word(pw);
+            for (int t = 0; t < nw; t++) {
                 uint32_t w[8];
                 for (int k = 0; k < 8; k++) {
                     uint32_t v = 0;
                     for (int b = 0; b < 4; b++) {
-                        int off = t * 32 + k * 4 + b;
-                        if (off < tile_len) v |= (uint32_t)sb[tile_off + off] << (8 * b);
+                        const int o = t * 32 + k * 4 + b;
+                        if (o < len) v |= (uint32_t)sb[off + o] << (8 * b);
                     }
                     w[k] = v;
                 }
                 uint32_t P[8];
                 bit_planes32(w, P);
                 c[t] = lines ? classify_planes<true>(P) : classify_planes<false>(P);
-                {
-                    // UTF-8 as the kernel checks it: on the bit planes, the
-                    // carry handed lane to lane and step to step, and taken
-                    // afresh from the 4 bytes before each warp region
-                    const int64_t o0 = (int64_t)tile_off + t * 32;
-                    if ((t * 32) % kWarpBytes == 0) {
-                        uint32_t pw = 0;   // previous 4 bytes of the segment (zero before its start)
-                        for (int b = 0; b < 4; b++) {
-                            const int64_t o = o0 - 4 + b;
-                            if (o >= 0 && (uint64_t)o < sg.len) pw |= (uint32_t)sb[o] << (8 * b);
-                        }
-                        ucarry = utf8_carry_word(pw);
-                    }
-                    const bool seg_end = (uint64_t)(o0 + 32) >= sg.len;
-                    const uint32_t next = utf8_carry_planes(P);
-                    if (utf8_errors_planes(P, ucarry, seg_end)) flags |= 1;
-                    ucarry = next;
-                }
+                const bool seg_end = off + (uint64_t)t * 32 + 32 >= sg.len;
+                const uint32_t next = utf8_carry_planes(P);
+                if (utf8_errors_planes(P, ucarry, seg_end)) flags |= 1;
+                ucarry = next;
                 escaped32(c[t].bs, 0, &cout0[t]);
                 all_bs[t] = c[t].bs == 0xFFFFFFFFu;
             }
-            // carries (tile entered without escape), parities, masks, counts
-            static uint32_t M[W], own1[W], own2[W], own3[W];
+            // the region entered without escape and outside strings
             uint32_t carry = 0, par = 0;
             bool tall = true;
             uint32_t tflip = 0, tcout = 0;
-            for (int t = 0; t < W; t++) {
+            int32_t C0 = 0, Ct = 0, K0 = 0, Kt = 0, O0 = 0, Ot = 0;
+            for (int t = 0; t < nw; t++) {
                 uint32_t dummy;
-                uint32_t esc = escaped32(c[t].bs, carry, &dummy);
-                uint32_t rq = c[t].q & ~esc;
-                M[t] = prefix_xor(rq) ^ (par ? 0xFFFFFFFFu : 0u);
+                const uint32_t esc = escaped32(c[t].bs, carry, &dummy);
+                const uint32_t rq = c[t].q & ~esc;
+                const uint32_t M = prefix_xor(rq) ^ (par ? 0xFFFFFFFFu : 0u);
                 par ^= __builtin_popcount(rq) & 1;
                 if (!all_bs[t]) {
-                    if (tall) {
-                        int fnb = __builtin_ctz(~c[t].bs);
-                        tflip = (c[t].q >> fnb) & 1;
-                    }
+                    if (tall) tflip = (c[t].q >> __builtin_ctz(~c[t].bs)) & 1;
                     tall = false;
                     carry = cout0[t];
                     tcout = cout0[t];
                 }
-                uint32_t br = c[t].br;
-                own1[t] = __builtin_popcount(c[t].st & ~M[t]) | (__builtin_popcount(c[t].st) << 16);
-                own2[t] = __builtin_popcount(br & ~M[t]) | (__builtin_popcount(br) << 16);
-                own3[t] = __builtin_popcount(c[t].op & ~M[t]) | (__builtin_popcount(c[t].op) << 16);
+                C0 += __builtin_popcount(c[t].st & ~M); Ct += __builtin_popcount(c[t].st);
+                K0 += __builtin_popcount(c[t].br & ~M); Kt += __builtin_popcount(c[t].br);
+                O0 += __builtin_popcount(c[t].op & ~M); Ot += __builtin_popcount(c[t].op);
             }
-            uint32_t tqpar = par;
-            int32_t C0 = 0, Ct = 0, K0 = 0, Kt = 0, O0 = 0, Ot = 0;
-            for (int t = 0; t < W; t++) {
-                C0 += own1[t] & 0xFFFF; Ct += own1[t] >> 16;
-                K0 += own2[t] & 0xFFFF; Kt += own2[t] >> 16;
-                O0 += own3[t] & 0xFFFF; Ot += own3[t] >> 16;
-            }
-            int32_t D0 = 2 * O0 - K0, Dt = 2 * Ot - Kt;
+            const int32_t D0 = 2 * O0 - K0, Dt = 2 * Ot - Kt;
             std::array<Ent, 4> T;
-            uint32_t Tev[4];
-            for (uint32_t s = 0; s < 4; s++) {
-                uint32_t escin = seg_first ? 0 : (s >> 1), instr = seg_first ? 0 : (s & 1);
-                uint32_t e = instr ^ (escin & tflip);
-                uint32_t oesc = tall ? escin : tcout;
-                T[s].st = (oesc << 1) | (e ^ tqpar) | (seg_first ? 4u : 0u);
-                T[s].s = e ? Ct - C0 : C0;
-                T[s].k = e ? Kt - K0 : K0;
-                T[s].d = e ? Dt - D0 : D0;
-                Tev[s] = e;
+            for (uint32_t st = 0; st < 4; st++) {
+                const uint32_t s0 = first ? 0 : st;
+                const uint32_t escin = s0 >> 1, instr = s0 & 1;
+                const uint32_t e = instr ^ (escin & tflip);
+                T[st].st = ((tall ? escin : tcout) << 1) | (e ^ par);
+                if (first) T[st].st |= kResetState | (sg.cont ? 0u : kResetCounts);
+                T[st].s = e ? Ct - C0 : C0;
+                T[st].k = e ? Kt - K0 : K0;
+                T[st].d = e ? Dt - D0 : D0;
             }
-            size_t tile = agg_hist.size();
-            Ent excl = ent_identity(0);
-            if (!immediate) {
-                // look back through a random number of aggregate-only tiles
-                size_t back = 1 + rng() % 40;
-                size_t lo = tile;
-                while (lo > 0 && tile - lo < back && !immediate_hist[lo - 1]) lo--;
-                // tiles [lo, tile) contribute aggregates; tile lo-1 its inclusive value
-                Ent acc[4];
-                tab_identity(acc);
-                for (size_t u = lo; u < tile; u++) tab_compose(acc, agg_hist[u].data(), acc);
-                Ent base = (lo > 0) ? incl_hist[lo - 1] : ent_identity(0);
-                excl = ent_apply(base, acc);
-                Ent direct = incl_hist[tile - 1];
-                if (excl.st != direct.st || excl.s != direct.s || excl.k != direct.k || excl.d != direct.d)
-                    flags |= 0x100;   // composition disagrees with the running value
+            tabs.push_back(T);
+        }
+    }
+
+    // ---- prefix: entry values by composing tables in random blocks -------------
+    // (the prefix kernels compose per-thread runs, warp scans and block
+    // aggregates; any grouping must give the running value)
+    const size_t NR = regions.size();
+    std::vector<Ent> entry(NR);
+    {
+        Ent run = ent_identity(0);
+        size_t r = 0;
+        Ent base = ent_identity(0);
+        while (r < NR) {
+            const size_t blk = 1 + rng() % 37;
+            const size_t hi = std::min(NR, r + blk);
+            Ent acc[4];
+            tab_identity(acc);
+            for (size_t u = r; u < hi; u++) {
+                // the value before region u from the block start: base, then acc
+                const Ent v = ent_apply(base, acc);
+                if (v.st != run.st || v.s != run.s || v.k != run.k || v.d != run.d) flags |= 0x100;
+                entry[u] = v;
+                run = ent_apply(run, tabs[u].data());
+                tab_compose(acc, tabs[u].data(), acc);
             }
-            Ent incl = ent_apply(excl, T.data());
-            agg_hist.push_back(T);
-            incl_hist.push_back(incl);
-            immediate_hist.push_back(immediate);
-            Ent entry = excl;
-            if (seg_first) { entry.st = 0; entry.d = 0; }
-            uint32_t e = Tev[entry.st & 3];
-            if (seg_last && incl.d != 0) flags |= 2;
-            // outputs
-            uint32_t pre1lo = 0, pre1hi = 0, pre2lo = 0, pre2hi = 0, pre3lo = 0, pre3hi = 0;
-            for (int t = 0; t < W; t++) {
-                uint32_t Mf = M[t] ^ (e ? 0xFFFFFFFFu : 0u);
-                uint32_t stm = c[t].st & ~Mf, brm = c[t].br & ~Mf, opm = c[t].op & ~Mf;
-                uint32_t p1lo = pre1lo, p1hi = pre1hi, p2lo = pre2lo, p2hi = pre2hi;
-                uint32_t p3lo = pre3lo, p3hi = pre3hi;
-                uint32_t sidx = entry.s + (e ? p1hi - p1lo : p1lo);
-                uint32_t kidx = entry.k + (e ? p2hi - p2lo : p2lo);
-                int32_t d0 = 2 * (int32_t)p3lo - (int32_t)p2lo, dt = 2 * (int32_t)p3hi - (int32_t)p2hi;
-                int32_t depth = entry.d + (e ? dt - d0 : d0);
-                uint64_t pos0 = sg.logical + tile_off + t * 32 + 1;
-                while (stm) {
-                    int j = __builtin_ctz(stm);
-                    stm &= stm - 1;
-                    if (pos.size() != sidx) flags |= 0x200;
-                    pos.push_back((int32_t)(pos0 + j));
-                    pair.push_back(0);
-                    if ((brm >> j) & 1) {
-                        uint32_t op = (opm >> j) & 1;
-                        int32_t lvl = op ? depth : depth - 1;
-                        depth += op ? 1 : -1;
-                        uint32_t cur = ((c[t].cur >> j) & 1) ? kCurly : 0;
-                        if (brk.size() != kidx) flags |= 0x400;
-                        brk.push_back({sidx | cur, ((uint32_t)lvl << 1) | op});
-                        kidx++;
-                    }
-                    sidx++;
+            base = ent_apply(base, acc);
+            r = hi;
+        }
+    }
+
+    // ---- scan_emit: every region again, from its exact entry state --------------
+    for (size_t ri = 0; ri < NR; ri++) {
+        const RegionRef& rr = regions[ri];
+        const Seg& sg = segs[rr.seg];
+        const uint8_t* sb = data + sg.off;
+        const Ent& T0 = tabs[ri][0];
+        Ent e = entry[ri];
+        if (T0.st & kResetState) { e.st = 0; e.d = 0; }
+        if (T0.st & kResetCounts) { e.s = 0; e.k = 0; }
+        uint32_t carry = (e.st >> 1) & 1, par = e.st & 1;
+        uint32_t sidx = e.s, kidx = e.k;
+        int32_t depth = e.d;
+        if (sidx != pos.size()) flags |= 0x200;
+        if (kidx != brk.size()) flags |= 0x400;
+        const int nw = (rr.len + 31) / 32;
+        for (int t = 0; t < nw; t++) {
+            uint32_t w[8];
+            for (int k = 0; k < 8; k++) {
+                uint32_t v = 0;
+                for (int b = 0; b < 4; b++) {
+                    const int o = t * 32 + k * 4 + b;
+                    if (o < rr.len) v |= (uint32_t)sb[rr.off + o] << (8 * b);
                 }
-                pre1lo += own1[t] & 0xFFFF; pre1hi += own1[t] >> 16;
-                pre2lo += own2[t] & 0xFFFF; pre2hi += own2[t] >> 16;
-                pre3lo += own3[t] & 0xFFFF; pre3hi += own3[t] >> 16;
+                w[k] = v;
+            }
+            const Classes c = lines ? classify32<true>(w) : classify32<false>(w);
+            const uint32_t esc = escaped32(c.bs, carry, &carry);
+            const uint32_t rq = c.q & ~esc;
+            const uint32_t M = prefix_xor(rq) ^ (par ? 0xFFFFFFFFu : 0u);
+            par ^= __builtin_popcount(rq) & 1;
+            uint32_t stm = c.st & ~M;
+            const uint32_t brm = c.br & stm, opm = c.op & stm;
+            const uint64_t pos0 = sg.logical + rr.off + (uint64_t)t * 32 + 1;
+            while (stm) {
+                const int j = __builtin_ctz(stm);
+                stm &= stm - 1;
+                pos.push_back((int32_t)(pos0 + j));
+                pair.push_back(0);
+                if ((brm >> j) & 1) {
+                    const uint32_t op = (opm >> j) & 1;
+                    const int32_t lvl = op ? depth : depth - 1;
+                    depth += op ? 1 : -1;
+                    const uint32_t cur = ((c.cur >> j) & 1) ? kCurly : 0;
+                    brk.push_back({sidx | cur, ((uint32_t)lvl << 1) | op});
+                }
+                sidx++;
             }
         }
+        // the region's end agrees with the next region's entry value
+        const Ent nv = ent_apply(entry[ri], tabs[ri].data());
+        if (nv.s != sidx || nv.d != depth) flags |= 0x800;
+        const bool seg_last = ri + 1 == NR || regions[ri + 1].seg != rr.seg;
+        if (seg_last && nv.d != 0) flags |= 2;
     }
 
     // ---- pairing: chunks of kChunk records, rounds of 32 --------------------------
