@@ -508,6 +508,7 @@ def run_other_configs(args, local, peak):
         for _ in range(args.steps):
             ctx.run()
         scan_ms, pair_ms, spine_ms, runs = ctx.phase_ms()
+        tables_ms, prefix_ms, emit_ms, _ = ctx.scan_phase_ms()
         span = ctx.span_ms() / args.steps
         ctx.timing(False)
         N = data.size
@@ -535,6 +536,8 @@ def run_other_configs(args, local, peak):
             "config": config, "workload": f"{info['kind']} {N} B (seed {synth.CONFIG_SEED_BASE + config:#x})",
             "structurals": S, "GBps": round(N / (span / 1e3) / 1e9, 1), "ms_per_parse": round(span, 4),
             "scan_ms": round(scan_ms / runs, 4), "scan_roofline_frac": round(B / (scan_ms / runs / 1e3) / 1e9 / peak, 4),
+            "scan_split_ms": {"tables": round(tables_ms / runs, 4), "prefix": round(prefix_ms / runs, 4),
+                              "emit": round(emit_ms / runs, 4)},
             "l2": "input larger than L2" if N > (129 << 20) else "input 64 MiB < 129 MB L2 (no flush: warm-L2 figure)",
             "e2e": e2e,
             "plan": plan_timing(cj, ctx, data, local) if info["kind"] == "lines" else None,

@@ -53,8 +53,9 @@ struct cj_context {
     DevBuf<uint8_t> in;
     DevBuf<int32_t> pos, pair;
     DevBuf<uint2> brk;
-    DevBuf<uint4> rtab, rentry, bagg;   // region tables, entry values, prefix block tables
-    DevBuf<uint32_t> work;              // regions the emit kernel visits
+    DevBuf<uint4> rtab, bagg;           // region and prefix-block transfer tables
+    DevBuf<uint4> work;                 // the emit kernel's work items (2 per region)
+    DevBuf<uint4> masks;                // per region step: mask words for the emit kernel
     DevBuf<Segment> segs;
     DevBuf<SegmentOut> seg_out;
     DevBuf<uint32_t> region_seg;
@@ -178,8 +179,7 @@ cj_status reserve_regions(cj_context* ctx, size_t regions)
 {
     cj_status st;
     if ((st = ensure(ctx, ctx->rtab, regions * 4))) return st;
-    if ((st = ensure(ctx, ctx->rentry, regions))) return st;
-    if ((st = ensure(ctx, ctx->work, regions))) return st;
+    if ((st = ensure(ctx, ctx->work, regions * 2))) return st;
     if ((st = ensure(ctx, ctx->region_seg, regions))) return st;
     if ((st = ensure(ctx, ctx->bagg, prefix_blocks(regions) * 4))) return st;
     return CJ_OK;
@@ -198,6 +198,7 @@ cj_status reserve(cj_context* ctx, size_t bytes, size_t segs)
     if ((st = ensure(ctx, ctx->pair, s_cap))) return st;
     if ((st = ensure(ctx, ctx->brk, s_cap))) return st;
     if ((st = reserve_regions(ctx, max_regions(bytes, segs)))) return st;
+    if ((st = ensure(ctx, ctx->masks, masks_cap(bytes, segs)))) return st;
     if ((st = ensure(ctx, ctx->segs, segs))) return st;
     if ((st = ensure(ctx, ctx->seg_out, segs))) return st;
     if ((st = ensure(ctx, ctx->spine, chunks * (size_t)kChunk))) return st;
@@ -359,8 +360,8 @@ cj_status enqueue(cj_context* ctx, bool graph)
     sp.out_cap = ctx->pos.cap;
     sp.brk_cap = ctx->brk.cap;
     sp.rtab = ctx->rtab.p;
-    sp.rentry = ctx->rentry.p;
     sp.bagg = ctx->bagg.p;
+    sp.masks = ctx->masks.p;
     sp.work = ctx->work.p;
     sp.ctrl = ctx->d_ctrl;
     sp.seg_out = ctx->seg_out.p;
@@ -653,6 +654,7 @@ cj_status reserve_batch(cj_context* ctx, uint64_t in_bytes, uint64_t out_cap, ui
     if ((st = ensure(ctx, ctx->pair, out_cap))) return st;
     if ((st = ensure(ctx, ctx->brk, brk_cap + 1))) return st;
     if ((st = reserve_regions(ctx, regions))) return st;
+    if ((st = ensure(ctx, ctx->masks, masks_cap(in_bytes, n)))) return st;
     if ((st = ensure(ctx, ctx->segs, n))) return st;
     if ((st = ensure(ctx, ctx->seg_out, n))) return st;
     if ((st = ensure(ctx, ctx->spine, chunks * (size_t)kChunk))) return st;
@@ -896,7 +898,7 @@ void cj_context_destroy(cj_context* ctx)
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     release(ctx->in); release(ctx->pos); release(ctx->pair); release(ctx->brk);
-    release(ctx->rtab); release(ctx->rentry); release(ctx->bagg); release(ctx->work);
+    release(ctx->rtab); release(ctx->bagg); release(ctx->work); release(ctx->masks);
     release(ctx->segs); release(ctx->seg_out); release(ctx->region_seg);
     release(ctx->spine); release(ctx->cinfo); release(ctx->tree);
     release(ctx->seg_err); release(ctx->seg_depth); release(ctx->rchunk_off);

@@ -20,9 +20,11 @@ struct ScanParams {
     uint64_t out_cap;           // entries of pos and pair
     uint64_t brk_cap;           // entries of brk
     uint4* rtab;                // 4 entries per region: transfer tables
-    uint4* rentry;              // 1 per region: entry value (state | work flag, s, k, depth)
     uint4* bagg;                // 4 per block of kPrefixPerBlock regions: block tables
-    uint32_t* work;             // regions with structurals to emit (ctrl->n_work of them)
+    uint4* masks;               // per region and step, 32 lanes: the 4 mask words of the steps
+                                // that hold structural characters (masks_cap(...) entries)
+    uint4* work;                // 2 per region with structurals to emit (ctrl->n_work of them):
+                                // {region, stored steps | flip << 31, s, k}, {depth, end s, end k, end depth}
     Ctrl* ctrl;
     SegmentOut* seg_out;
     uint32_t* seg_err;          // per-segment verdict bits (independent documents),
@@ -44,6 +46,8 @@ struct ScanShape {
 
 // scratch sizes of one scan over `n_regions` regions
 inline uint64_t prefix_blocks(uint64_t n_regions) { return (n_regions + kPrefixPerBlock - 1) / kPrefixPerBlock; }
+// mask entries (uint4) for `bytes` of input in `segs` segments, any region size
+inline uint64_t masks_cap(uint64_t bytes, uint64_t segs) { return (bytes / 1024 + (segs + 1) * 16) * 32; }
 
 struct PairParams {
     const uint2* brk;

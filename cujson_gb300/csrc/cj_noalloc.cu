@@ -49,9 +49,9 @@ struct alignas(256) Scratch {
     alignas(256) int32_t pair[kScap];
     alignas(256) uint2 brk[kScap];
     alignas(256) uint4 rtab[kRegions * 4];
-    alignas(256) uint4 rentry[kRegions];
     alignas(256) uint4 bagg[kPrefixBlocks * 4];
-    alignas(256) uint32_t work[kRegions];
+    alignas(256) uint4 work[kRegions * 2];
+    alignas(256) uint4 masks[kRegions * kRegionSteps * 32];
     alignas(256) uint32_t spine[kChunks * kChunk];
     alignas(256) int4 cinfo[kChunks];
     alignas(256) unsigned long long tree[kTree];
@@ -60,7 +60,7 @@ struct alignas(256) Scratch {
     alignas(256) Ctrl ctrl;
 };
 
-// The scratch itself (about 21 MiB for the 1 MiB limit).  Zero at load; the
+// The scratch itself (about 22 MiB for the 1 MiB limit).  Zero at load; the
 // pairing min-tree is epoch-tagged, and is cleared again when the epoch wraps
 // and on the first call on a device.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(Scratch)];
@@ -203,8 +203,8 @@ cj_status parse_noalloc(const uint8_t* d_data, size_t size, int32_t* d_out, size
     sp.out_cap = kScap;
     sp.brk_cap = kScap;
     sp.rtab = s->rtab;
-    sp.rentry = s->rentry;
     sp.bagg = s->bagg;
+    sp.masks = s->masks;
     sp.work = s->work;
     sp.ctrl = &s->ctrl;
     sp.seg_out = &s->seg_out;

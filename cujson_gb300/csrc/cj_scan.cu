@@ -1,6 +1,6 @@
 // cj_scan.cu -- the structural scan: UTF-8 validation, tokenization (quote,
 // backslash and structural classes, escape carry, in-string mask), structural
-// compaction and bracket levels, in four launches with no waits between
+// compaction and bracket levels, in three or four launches with no waits between
 // thread blocks:
 //
 //   scan_tables  (one warp per region, regions of 4/8/16 KiB in grid-stride
@@ -9,23 +9,28 @@
 //                 in-string mask, and the region's transfer table -- for each
 //                 of the 4 entry states (escape pending, inside a string): the
 //                 exit state, structural count, bracket count and depth delta.
-//   prefix_reduce (1024 regions per block) composes each block's tables.
-//   prefix_apply  composes the blocks before its own, scans its regions'
-//                 tables and writes every region's entry value (state, counts
-//                 and depth before it), the segment ends, the totals, and the
-//                 list of regions that hold structurals outside strings.
-//   scan_emit    (one warp per listed region) reads such a region again (with
-//                 its entry state now known, the in-string mask is exact) and
-//                 writes its 1-based positions, zeroed pair entries and
-//                 bracket records (structural index, level, open flag, brace or
-//                 bracket) through a per-warp staging buffer in shared memory,
-//                 so that every global store is coalesced.
+//   prefix_reduce (1024 regions per block, one per thread) composes each
+//                 block's tables (only when there is more than one block).
+//   prefix_apply  (the same blocks) composes the blocks before its own, the
+//                 warps (chunks of 32 regions) before each warp and the regions
+//                 before each region, and writes the segment ends, the totals,
+//                 and the work list: every region that holds structurals
+//                 outside strings, with its entry and end values.
+//   scan_emit    (one warp per listed region) reads the mask words the table
+//                 kernel stored for the region's steps that hold structural
+//                 characters (opens, closes, braces and other structurals, and
+//                 the structurals inside strings for an entry outside one),
+//                 flips the in-string part by the region's now known entry
+//                 state, and writes the 1-based positions, zeroed pair entries
+//                 and bracket records (structural index, level, open flag,
+//                 brace or bracket) through a per-warp staging buffer in shared
+//                 memory, so that every global store is coalesced.
 //
-// Regions whose bytes are all inside strings (or hold no structural) are never
-// read twice, so on documents made mostly of long strings the input crosses
-// HBM about once; dense regions are read twice (the second read partly from
-// L2).  Nothing spins on another block: the only wait is for input bytes still
-// being copied (an overlapped one-shot parse), bounded, with a timeout flag.
+// The input crosses HBM once; the masks (512 bytes per KiB, only for steps
+// with structural characters) are written once and read back only for the
+// regions that hold structurals outside strings.  Nothing spins on another
+// block: the only wait is for input bytes still being copied (an overlapped
+// one-shot parse), bounded, with a timeout flag.
 //
 // This replaces the reference's stage 1 (checkAscii + checkUTF8,
 // cujson/parse_standard_json.cu:186-327) and stage 2 (bitMapCreatorSimd :446,
@@ -48,11 +53,14 @@ constexpr uint32_t FULL = 0xFFFFFFFFu;
 constexpr int kThreads = 256;                  // 8 warps per block (tables, emit, prefix)
 constexpr int kWarpsPerBlock = kThreads / 32;
 constexpr uint32_t kInputWaitLimit = 1u << 22; // polls (>= 256 ns each) for input bytes
-constexpr uint32_t kWork = 0x80000000u;        // rentry.st: the region has structurals to emit
 // emit staging, per warp: positions and bracket records of the steps since the
 // last flush (a step whose counts exceed them is written directly)
-constexpr int kPosStage = 256;
-constexpr int kBrkStage = 128;
+constexpr int kPosStage = 512;
+constexpr int kBrkStage = 256;
+// Bits of a region table's `st` that the table algebra ignores (it reads bits
+// 0-3 only): the region's wflip, and which of its steps have stored masks.
+constexpr int kTabFlipBit = 4;
+constexpr int kTabStepsShift = 16;
 
 // (CJ_EMU: the CPU emulation of the kernels in tests/emu, test infrastructure)
 __device__ __forceinline__ uint32_t lanemask_lt() {
@@ -147,59 +155,18 @@ __device__ __forceinline__ bool wait_input(const ScanParams& P, const Region& g)
 }
 
 // ---- per-warp step stream ---------------------------------------------------------
-// A warp's regions (every nw-th region from its first, or the entries of a work
-// list) are read as one stream of 1 KiB steps: each lane copies its own 32
-// bytes of the step kDepth steps ahead into its own slots of a shared-memory
-// ring with cp.async (no registers held for loads in flight, no waits across
-// lanes), so the reads of the next region start during the last steps of the
-// current one.
-constexpr int kDepth = 2;                      // steps in flight beyond the current one
-constexpr int kRing = kDepth + 1;
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-#ifdef CJ_EMU
-    return 0;
-#else
-    return (uint32_t)__cvta_generic_to_shared(p);
-#endif
-}
-
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-#ifdef CJ_EMU
-    memcpy(dst, src, 16);
-#else
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
-#endif
-}
-
-__device__ __forceinline__ void cp_async_commit() {
-#ifndef CJ_EMU
-    asm volatile("cp.async.commit_group;" ::: "memory");
-#endif
-}
-
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-#ifndef CJ_EMU
-    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-#endif
-}
-
-// one lane's slots: kRing steps of 32 bytes
-struct LaneRing {
-    uint4 v[kRing][2];
-};
-
-// The producer side of a warp's stream: which step of which region it copies
-// next.  Its cursor is a region number or a work-list index; `walk.next(c)`
-// gives the cursor after c (kNoRegion: none), `walk.region(c)` its region.
+// A warp's regions (every nw-th region from its first) are read as one stream of 1 KiB steps: each lane holds its own 32 bytes
+// of the next step in registers, loaded while the current step is processed,
+// so the reads of the next region start during the last step of the current
+// one.  (Plain loads streamed at ~97 % of the measured HBM bandwidth in a
+// probe on this GPU; 16-byte cp.async copies into shared memory reached ~57 %.)
 constexpr uint32_t kNoRegion = 0xFFFFFFFFu;
 
-struct Producer {
-    uint32_t c;            // cursor being copied (kNoRegion: done)
-    int j, n;              // its next step and its step count
+struct Stream {
+    uint4 a, b;            // the lane's 32 bytes of the next step
+    uint32_t c;            // cursor of the region of the next step (kNoRegion: none)
+    int j, n;              // that step's number in its region, the region's step count
     const uint8_t* src;    // the lane's bytes of step 0 of that region
-    int slot;              // ring slot of the next copy
 };
 
 // every nw-th region from the warp's first
@@ -209,41 +176,91 @@ struct StrideWalk {
     __device__ __forceinline__ uint32_t region(uint32_t c) const { return c; }
 };
 
-// every nw-th entry of the work list from the warp's first
-struct WorkWalk {
-    const uint32_t* work;
-    uint32_t nw, n;
-    __device__ __forceinline__ uint32_t next(uint32_t c) const { return (c + nw < n && c + nw > c) ? c + nw : kNoRegion; }
-    __device__ __forceinline__ uint32_t region(uint32_t c) const { return __ldcg(work + c); }
-};
-
-template <int R, typename Walk>
-__device__ __forceinline__ void producer_enter(const ScanParams& P, Producer& pr, uint32_t c, int lane,
-                                               const Walk& walk) {
-    pr.c = c;
-    pr.j = 0;
-    if (c == kNoRegion) { pr.n = 0; return; }
-    Region g;
-    region_of(P, walk.region(c), R * kStepBytes, g);
-    bool ok = true;
-    if (P.ready) ok = __shfl_sync(FULL, lane == 0 ? wait_input(P, g) : true, 0);
-    if (!ok) { pr.c = kNoRegion; pr.n = 0; return; }
-    pr.n = (g.len + kStepBytes - 1) / kStepBytes;
-    pr.src = g.base + g.off + lane * kBytesPerThread;
+__device__ __forceinline__ void stream_load(Stream& st) {
+    const uint4* p = reinterpret_cast<const uint4*>(st.src + (size_t)st.j * kStepBytes);
+    st.a = __ldcg(p);
+    st.b = __ldcg(p + 1);
 }
 
-// copy the producer's next step (if any) and commit one group either way
+// point the stream at step 0 of cursor c's region and load it (after the wait
+// for its input bytes of an overlapped parse; a wait that gives up ends the
+// stream)
 template <int R, typename Walk>
-__device__ __forceinline__ void producer_issue(const ScanParams& P, Producer& pr, LaneRing& ring, int lane,
-                                               const Walk& walk) {
-    if (pr.c != kNoRegion) {
-        const uint8_t* s = pr.src + (size_t)pr.j * kStepBytes;
-        cp_async16(&ring.v[pr.slot][0], s);
-        cp_async16(&ring.v[pr.slot][1], s + 16);
-        if (++pr.j == pr.n) producer_enter<R>(P, pr, walk.next(pr.c), lane, walk);
+__device__ __forceinline__ void stream_enter(const ScanParams& P, Stream& st, uint32_t c, int lane,
+                                             const Walk& walk) {
+    st.c = c;
+    st.j = 0;
+    st.n = 0;
+    if (c == kNoRegion) return;
+    Region g;
+    region_of(P, walk.region(c), R * kStepBytes, g);
+    if (P.ready && !__shfl_sync(FULL, lane == 0 ? wait_input(P, g) : true, 0)) { st.c = kNoRegion; return; }
+    st.n = (g.len + kStepBytes - 1) / kStepBytes;
+    st.src = g.base + g.off + lane * kBytesPerThread;
+    stream_load(st);
+}
+
+// take the next step (lo, hi) and load the one after it
+template <int R, typename Walk>
+__device__ __forceinline__ void stream_take(const ScanParams& P, Stream& st, uint4& lo, uint4& hi, int lane,
+                                            const Walk& walk) {
+    lo = st.a;
+    hi = st.b;
+    if (st.c == kNoRegion) return;
+    if (++st.j < st.n) stream_load(st);
+    else stream_enter<R>(P, st, walk.next(st.c), lane, walk);
+}
+
+// ---- transfer-table helpers ---------------------------------------------------------
+
+__device__ __forceinline__ void load_tab(const uint4* p, Ent t[4]) {
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+        const uint4 v = __ldcg(p + s);
+        t[s].st = v.x; t[s].s = v.y; t[s].k = v.z; t[s].d = (int32_t)v.w;
     }
-    pr.slot = pr.slot + 1 == kRing ? 0 : pr.slot + 1;
-    cp_async_commit();
+}
+
+__device__ __forceinline__ void store_tab(uint4* p, const Ent t[4]) {
+#pragma unroll
+    for (int s = 0; s < 4; s++) p[s] = make_uint4(t[s].st, t[s].s, t[s].k, (uint32_t)t[s].d);
+}
+
+__device__ __forceinline__ void shfl_tab(const Ent t[4], Ent u[4], int src_delta, bool up) {
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+        if (up) {
+            u[s].st = __shfl_up_sync(FULL, t[s].st, src_delta);
+            u[s].s = __shfl_up_sync(FULL, t[s].s, src_delta);
+            u[s].k = __shfl_up_sync(FULL, t[s].k, src_delta);
+            u[s].d = __shfl_up_sync(FULL, t[s].d, src_delta);
+        } else {
+            u[s].st = __shfl_down_sync(FULL, t[s].st, src_delta);
+            u[s].s = __shfl_down_sync(FULL, t[s].s, src_delta);
+            u[s].k = __shfl_down_sync(FULL, t[s].k, src_delta);
+            u[s].d = __shfl_down_sync(FULL, t[s].d, src_delta);
+        }
+    }
+}
+
+// inclusive scan of tables over the lanes of a warp, in lane order
+__device__ __forceinline__ void warp_scan_tab(Ent t[4], int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        Ent u[4];
+        shfl_tab(t, u, o, true);
+        if (lane >= o) tab_compose(u, t, t);
+    }
+}
+
+// composition of the 32 lanes' tables in lane order, in lane 0
+__device__ __forceinline__ void warp_reduce_tab(Ent t[4], int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        Ent u[4];
+        shfl_tab(t, u, o, false);
+        if ((lane & (2 * o - 1)) == 0 && lane + o < 32) tab_compose(t, u, t);
+    }
 }
 
 // ---- scan_tables --------------------------------------------------------------
@@ -254,26 +271,24 @@ __device__ __forceinline__ void producer_issue(const ScanParams& P, Producer& pr
 // entry only matters when the first byte after the region's leading backslash
 // run is a quote (`wflip`), and entering inside a string flips the in-string
 // mask of the whole region, which swaps the counts of structurals outside and
-// inside strings.  The steps come from the warp's stream (`pr`, `ring`, `cs`).
+// inside strings.  The steps come from the warp's stream `st`.
 template <bool LINES, int R, typename Walk>
-__device__ __forceinline__ void region_table(const ScanParams& P, const Region& g, uint4* out, int lane,
-                                             uint32_t lt, Producer& pr, LaneRing& ring, int& cs, const Walk& walk)
+__device__ __forceinline__ void region_table(const ScanParams& P, const Region& g, uint4* out, uint4* mout,
+                                             int lane, uint32_t lt, Stream& st, const Walk& walk)
 {
     const int nsteps = (g.len + kStepBytes - 1) / kStepBytes;
+    // the 4 bytes before the region (their UTF-8 leads carry in): loaded now,
+    // used only once the first step is classified
+    const uint32_t pw = g.off > 0 ? __ldcg(reinterpret_cast<const uint32_t*>(g.base + g.off) - 1) : 0u;
     uint32_t ucarry = 0;                   // UTF-8 carry into the step (warp uniform)
-    if (g.off > 0) {
-        const uint32_t pw = __ldcg(reinterpret_cast<const uint32_t*>(g.base + g.off) - 1);
-        if (pw & 0x80808000u) ucarry = utf8_carry_word(pw);
-    }
     uint32_t carry = 0, par = 0;           // escape carry / quote parity (warp uniform)
     uint32_t started = 0, wflip = 0;       // first non-all-backslash lane seen / its flip
     uint32_t in_run = 0;                   // the previous step ended in 32 backslashes
+    uint32_t steps = 0;                    // steps whose mask words were stored
     uint32_t n_c0 = 0, n_ct = 0, n_k0 = 0, n_kt = 0, n_o0 = 0, n_ot = 0;   // per lane
     for (int j = 0; j < nsteps; j++) {
-        producer_issue<R>(P, pr, ring, lane, walk);
-        cp_async_wait<kDepth>();
-        uint4 lo = ring.v[cs][0], hi = ring.v[cs][1];
-        cs = cs + 1 == kRing ? 0 : cs + 1;
+        uint4 lo, hi;
+        stream_take<R>(P, st, lo, hi, lane, walk);
         const int step_len = min(kStepBytes, g.len - j * kStepBytes);
         const int valid = min(kBytesPerThread, step_len - lane * kBytesPerThread);
         if (valid < kBytesPerThread) {
@@ -296,6 +311,7 @@ __device__ __forceinline__ void region_table(const ScanParams& P, const Region& 
 
         // UTF-8 on the bit planes, on steps that hold a non-ASCII byte or
         // continue a sequence from the bytes before them
+        if (j == 0 && (pw & 0x80808000u)) ucarry = utf8_carry_word(pw);
         if (__any_sync(FULL, c.hi != 0u) || ucarry != 0u) {
             const uint32_t cout = utf8_carry_planes(planes);
             uint32_t cin = __shfl_up_sync(FULL, cout, 1);
@@ -351,6 +367,14 @@ __device__ __forceinline__ void region_table(const ScanParams& P, const Region& 
         n_c0 += __popc(c.st & ~M); n_ct += __popc(c.st);
         n_k0 += __popc(c.br & ~M); n_kt += __popc(c.br);
         n_o0 += __popc(c.op & ~M); n_ot += __popc(c.op);
+        // the step's four mask words for the emit kernel, when it holds any
+        // structural character: opens, closes, `x` (braces among brackets and
+        // every other structural) and the structurals inside strings for an
+        // entry outside one
+        if (__any_sync(FULL, c.st != 0u)) {
+            __stcg(mout + (size_t)j * 32, make_uint4(c.op, c.br & ~c.op, c.cur | (c.st & ~c.br), c.st & M));
+            steps |= 1u << j;
+        }
     }
     const int32_t C0 = (int32_t)__reduce_add_sync(FULL, n_c0), Ct = (int32_t)__reduce_add_sync(FULL, n_ct);
     const int32_t K0 = (int32_t)__reduce_add_sync(FULL, n_k0), Kt = (int32_t)__reduce_add_sync(FULL, n_kt);
@@ -363,7 +387,8 @@ __device__ __forceinline__ void region_table(const ScanParams& P, const Region& 
         const uint32_t s = first ? 0u : (uint32_t)lane;
         const uint32_t escin = s >> 1, instr = s & 1u;
         const uint32_t e = instr ^ (escin & wflip);
-        uint32_t st = ((started ? carry : escin) << 1) | (e ^ par);
+        uint32_t st = ((started ? carry : escin) << 1) | (e ^ par) | (wflip << kTabFlipBit) |
+                      (steps << kTabStepsShift);
         if (first) st |= kResetState | ((g.seg_flags & kSegContinue) ? 0u : kResetCounts);
         out[lane] = make_uint4(st, (uint32_t)(e ? Ct - C0 : C0), (uint32_t)(e ? Kt - K0 : K0),
                                (uint32_t)(e ? Dt - D0 : D0));
@@ -371,9 +396,8 @@ __device__ __forceinline__ void region_table(const ScanParams& P, const Region& 
 }
 
 template <bool LINES, int R>
-__global__ void __launch_bounds__(kThreads) scan_tables(ScanParams P)
+__global__ void __launch_bounds__(kThreads, 4) scan_tables(ScanParams P)
 {
-    __shared__ LaneRing s_ring[kThreads];
     const int lane = threadIdx.x & 31;
     const uint32_t lt = lanemask_lt();
     const uint32_t nw = gridDim.x * kWarpsPerBlock;
@@ -381,168 +405,121 @@ __global__ void __launch_bounds__(kThreads) scan_tables(ScanParams P)
     if (first >= P.n_regions) return;
     const uint32_t n = P.n_regions;
     const StrideWalk walk{nw, n};
-    LaneRing& ring = s_ring[threadIdx.x];
-    Producer pr;
-    pr.slot = 0;
-    producer_enter<R>(P, pr, first, lane, walk);
-    for (int d = 0; d < kDepth; d++) producer_issue<R>(P, pr, ring, lane, walk);
-    int cs = 0;
+    Stream st;
+    stream_enter<R>(P, st, first, lane, walk);
     for (uint32_t r = first; r < n; r += nw) {
-        if (aborted(P.ctrl)) break;
+        if (P.ready && aborted(P.ctrl)) break;     // the wait for input bytes gave up
         Region g;
         region_of(P, r, R * kStepBytes, g);
-        region_table<LINES, R>(P, g, P.rtab + (size_t)r * 4, lane, lt, pr, ring, cs, walk);
-    }
-    cp_async_wait<0>();
-}
-
-// ---- prefix over the region tables -----------------------------------------------
-
-__device__ __forceinline__ void load_tab(const uint4* p, Ent t[4]) {
-#pragma unroll
-    for (int s = 0; s < 4; s++) {
-        const uint4 v = __ldcg(p + s);
-        t[s].st = v.x; t[s].s = v.y; t[s].k = v.z; t[s].d = (int32_t)v.w;
+        region_table<LINES, R>(P, g, P.rtab + (size_t)r * 4, P.masks + (size_t)r * R * 32 + lane, lane, lt, st,
+                               walk);
     }
 }
 
-__device__ __forceinline__ void store_tab(uint4* p, const Ent t[4]) {
-#pragma unroll
-    for (int s = 0; s < 4; s++) p[s] = make_uint4(t[s].st, t[s].s, t[s].k, (uint32_t)t[s].d);
-}
+// ---- prefix over the region tables --------------------------------------------------
+// Blocks of 1024 regions, one per thread; a warp's 32 regions are a chunk.
+// Both kernels are shallow: a warp scan or reduction of tables per level.
 
-__device__ __forceinline__ void shfl_tab(const Ent t[4], Ent u[4], int src_delta, bool up) {
-#pragma unroll
-    for (int s = 0; s < 4; s++) {
-        if (up) {
-            u[s].st = __shfl_up_sync(FULL, t[s].st, src_delta);
-            u[s].s = __shfl_up_sync(FULL, t[s].s, src_delta);
-            u[s].k = __shfl_up_sync(FULL, t[s].k, src_delta);
-            u[s].d = __shfl_up_sync(FULL, t[s].d, src_delta);
-        } else {
-            u[s].st = __shfl_down_sync(FULL, t[s].st, src_delta);
-            u[s].s = __shfl_down_sync(FULL, t[s].s, src_delta);
-            u[s].k = __shfl_down_sync(FULL, t[s].k, src_delta);
-            u[s].d = __shfl_down_sync(FULL, t[s].d, src_delta);
-        }
-    }
-}
-
-// inclusive scan of tables over the lanes of a warp, in lane order
-__device__ __forceinline__ void warp_scan_tab(Ent t[4], int lane) {
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        Ent u[4];
-        shfl_tab(t, u, o, true);
-        if (lane >= o) tab_compose(u, t, t);
-    }
-}
-
-// composition of the tables of regions [lo, hi), one thread's run of them
-__device__ __forceinline__ void compose_run(const uint4* rtab, uint32_t lo, uint32_t hi, Ent t[4]) {
-    tab_identity(t);
-    for (uint32_t r = lo; r < hi; r++) {
-        Ent u[4];
-        load_tab(rtab + (size_t)r * 4, u);
-        tab_compose(t, u, t);
-    }
-}
-
-// Block b: the composition of the tables of regions [b * kPrefixPerBlock, ...).
-__global__ void __launch_bounds__(kThreads) prefix_reduce(ScanParams P)
+// Block b: the composition of its regions' tables.
+__global__ void __launch_bounds__(kPrefixPerBlock) prefix_reduce(ScanParams P)
 {
-    __shared__ Ent s_tab[kWarpsPerBlock][4];
+    __shared__ Ent s_w[32][4];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    constexpr int per = kPrefixPerBlock / kThreads;
-    const uint32_t lo = blockIdx.x * kPrefixPerBlock + threadIdx.x * per;
+    const uint32_t r = blockIdx.x * (uint32_t)kPrefixPerBlock + threadIdx.x;
     Ent t[4];
-    compose_run(P.rtab, min(lo, P.n_regions), min(lo + per, P.n_regions), t);
-    warp_scan_tab(t, lane);
-    if (lane == 31) {
+    if (r < P.n_regions) load_tab(P.rtab + (size_t)r * 4, t);
+    else tab_identity(t);
+    warp_reduce_tab(t, lane);
+    if (lane == 0) {
 #pragma unroll
-        for (int s = 0; s < 4; s++) s_tab[warp][s] = t[s];
+        for (int k = 0; k < 4; k++) s_w[warp][k] = t[k];
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        Ent a[4];
-        tab_identity(a);
-        for (int w = 0; w < kWarpsPerBlock; w++) tab_compose(a, s_tab[w], a);
-        store_tab(P.bagg + (size_t)blockIdx.x * 4, a);
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) t[k] = s_w[lane][k];
+        warp_reduce_tab(t, lane);
+        if (lane == 0) store_tab(P.bagg + (size_t)blockIdx.x * 4, t);
     }
 }
 
-// Block b: entry values of its regions, segment ends, totals and the emit
-// work list.
-__global__ void __launch_bounds__(kThreads) prefix_apply(ScanParams P)
+// Block b: entry values, segment ends, totals and the emit work list.
+__global__ void __launch_bounds__(kPrefixPerBlock) prefix_apply(ScanParams P)
 {
-    __shared__ Ent s_tab[kWarpsPerBlock][4];
-    __shared__ Ent s_base;
-    __shared__ uint32_t s_cnt[kWarpsPerBlock];
-    __shared__ uint32_t s_work_base;
+    __shared__ Ent s_chunk[32][4];         // per warp: its total, then its exclusive prefix table
+    __shared__ Ent s_base;                 // the value before the block
+    __shared__ uint32_t s_cnt[32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (aborted(P.ctrl)) return;          // a timed-out run writes no outputs
-    constexpr int per = kPrefixPerBlock / kThreads;
+    const uint32_t n = P.n_regions;
+    const uint32_t b = blockIdx.x;
 
-    // the value before this block: the blocks before it, composed by warp 0
-    if (warp == 0) {
-        const uint32_t nb = blockIdx.x;
-        const uint32_t q = (nb + 31) / 32;
+    if (warp == 1) {
+        // the blocks before this one
+        const uint32_t q = (b + 31) / 32;
         Ent t[4];
         tab_identity(t);
-        for (uint32_t b = lane * q; b < min(nb, (uint32_t)(lane + 1) * q); b++) {
+        for (uint32_t i = lane * q; i < min(b, (uint32_t)(lane + 1) * q); i++) {
             Ent u[4];
-            load_tab(P.bagg + (size_t)b * 4, u);
+            load_tab(P.bagg + (size_t)i * 4, u);
             tab_compose(t, u, t);
         }
-        warp_scan_tab(t, lane);
-        if (lane == 31) s_base = ent_apply(ent_identity(0), t);
+        warp_reduce_tab(t, lane);
+        if (lane == 0) s_base = ent_apply(ent_identity(0), t);
     }
 
-    // this thread's regions, and the block's exclusive scan over threads
-    const uint32_t lo = blockIdx.x * kPrefixPerBlock + threadIdx.x * per;
-    const uint32_t hi = min(lo + per, P.n_regions);
-    Ent tabs[per][4];
-    Ent a[4];
-    tab_identity(a);
-#pragma unroll
-    for (int i = 0; i < per; i++) {
-        if (lo + i < hi) load_tab(P.rtab + (size_t)(lo + i) * 4, tabs[i]);
-        else tab_identity(tabs[i]);
-        tab_compose(a, tabs[i], a);
-    }
+    // this warp's chunk: the regions before each region, and the chunk's total
+    const uint32_t r = b * (uint32_t)kPrefixPerBlock + threadIdx.x;
+    Ent t[4];
+    if (r < n) load_tab(P.rtab + (size_t)r * 4, t);
+    else tab_identity(t);
     Ent incl[4];
 #pragma unroll
-    for (int s = 0; s < 4; s++) incl[s] = a[s];
+    for (int k = 0; k < 4; k++) incl[k] = t[k];
     warp_scan_tab(incl, lane);
     if (lane == 31) {
 #pragma unroll
-        for (int s = 0; s < 4; s++) s_tab[warp][s] = incl[s];
+        for (int k = 0; k < 4; k++) s_chunk[warp][k] = incl[k];
     }
     Ent ex[4];
     shfl_tab(incl, ex, 1, true);
     if (lane == 0) tab_identity(ex);
     __syncthreads();
-    Ent wpre[4];
-    tab_identity(wpre);
-    for (int w = 0; w < warp; w++) tab_compose(wpre, s_tab[w], wpre);
-    tab_compose(wpre, ex, wpre);
-    Ent v = ent_apply(s_base, wpre);
-
-    uint32_t work_bits = 0;
+    if (warp == 0) {
+        // the chunks before each chunk
+        Ent c[4];
 #pragma unroll
-    for (int i = 0; i < per; i++) {
-        const uint32_t r = lo + i;
-        if (r >= hi) break;
-        const Ent x = ent_select(tabs[i], v.st & 3u);
-        const Ent nv = ent_apply(v, tabs[i]);
+        for (int k = 0; k < 4; k++) c[k] = s_chunk[lane][k];
+        warp_scan_tab(c, lane);
+        Ent cx[4];
+        shfl_tab(c, cx, 1, true);
+        if (lane == 0) tab_identity(cx);
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < 4; k++) s_chunk[lane][k] = cx[k];
+    }
+    __syncthreads();
+    const Ent v = ent_apply(ent_apply(s_base, s_chunk[warp]), ex);
+
+    bool work = false;
+    Ent e = v, nv = v;
+    uint32_t steps_flip = 0;
+    if (r < n) {
+        const uint32_t raw = t[0].st;           // the region's own table: wflip, stored steps
+        const Ent x = ent_select(t, v.st & 3u);
+        nv = ent_apply(v, t);
         // the entry value as the region starts: a segment's first region starts
         // in state 0 at depth 0 (and at count 0 for an independent document)
-        Ent e = v;
         if (x.st & kResetState) { e.st = 0; e.d = 0; }
         if (x.st & kResetCounts) { e.s = 0; e.k = 0; }
-        const bool work = x.s != 0u;
-        work_bits |= (work ? 1u : 0u) << i;
-        P.rentry[r] = make_uint4(e.st | (work ? kWork : 0u), e.s, e.k, (uint32_t)e.d);
+        work = x.s != 0u;
+        // whether the region's in-string mask (computed for an entry outside
+        // strings and escapes) is flipped: entering inside a string, or with an
+        // escape pending before a leading quote; a segment's first region is
+        // entered in state 0
+        const uint32_t instr = e.st & 1u, escin = (e.st >> 1) & 1u;
+        const uint32_t flip = instr ^ (escin & ((raw >> kTabFlipBit) & 1u));
+        steps_flip = (raw >> kTabStepsShift) | (flip << 31);
         const uint32_t segi = P.region_seg ? __ldg(P.region_seg + r) : 0u;
         const Segment* sp = P.segs + segi;
         if (r + 1 == __ldg(&sp->first_region) + __ldg(&sp->n_regions)) {
@@ -557,33 +534,36 @@ __global__ void __launch_bounds__(kThreads) prefix_apply(ScanParams P)
                 else atomicOr(&P.ctrl->error_flags, CJ_FLAG_BRACKETS);
             }
         }
-        if (r + 1 == P.n_regions) {
+        if (r + 1 == n) {
             P.ctrl->s_total = nv.s;
             P.ctrl->k_total = nv.k;
         }
-        v = nv;
     }
 
     // the block's regions with structurals go to the work list (one atomic per block)
-    const uint32_t cnt = __popc(work_bits);
-    uint32_t wincl = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t u = __shfl_up_sync(FULL, wincl, o);
-        if (lane >= o) wincl += u;
-    }
-    if (lane == 31) s_cnt[warp] = wincl;
+    const uint32_t bal = __ballot_sync(FULL, work);
+    if (lane == 0) s_cnt[warp] = __popc(bal);
     __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t tot = 0;
-        for (int w = 0; w < kWarpsPerBlock; w++) { const uint32_t c = s_cnt[w]; s_cnt[w] = tot; tot += c; }
-        s_work_base = tot ? atomicAdd(&P.ctrl->n_work, tot) : 0u;
+    if (warp == 0) {
+        const uint32_t cnt = s_cnt[lane];
+        uint32_t x = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, x, o);
+            if (lane >= o) x += y;
+        }
+        const uint32_t tot = __shfl_sync(FULL, x, 31);
+        uint32_t base = 0;
+        if (lane == 0 && tot) base = atomicAdd(&P.ctrl->n_work, tot);
+        base = __shfl_sync(FULL, base, 0);
+        s_cnt[lane] = base + x - cnt;
     }
     __syncthreads();
-    uint32_t o = s_work_base + s_cnt[warp] + wincl - cnt;
-#pragma unroll
-    for (int i = 0; i < per; i++)
-        if ((work_bits >> i) & 1u) P.work[o++] = lo + i;
+    if (work) {
+        const uint32_t o = s_cnt[warp] + __popc(bal & lanemask_lt());
+        P.work[2 * (size_t)o] = make_uint4(r, steps_flip, e.s, e.k);
+        P.work[2 * (size_t)o + 1] = make_uint4((uint32_t)e.d, nv.s, nv.k, (uint32_t)nv.d);
+    }
 }
 
 // ---- scan_emit --------------------------------------------------------------------
@@ -618,65 +598,29 @@ __device__ __forceinline__ void emit_flush(const ScanParams& P, const Region& g,
     __syncwarp();
 }
 
-template <bool LINES, int R>
-__device__ __forceinline__ void emit_region(const ScanParams& P, const Region& g, uint4 entry, EmitStage& st,
-                                            uint32_t expect_s, uint32_t expect_k, int32_t expect_d, int lane,
-                                            uint32_t lt, Producer& pr, LaneRing& ring, int& cs, const WorkWalk& walk)
+// One listed region: the steps whose mask words were stored, with the
+// region's in-string mask flipped (`flip` all ones) or not by its entry state.
+__device__ __forceinline__ void emit_region(const ScanParams& P, const Region& g, const uint4* mk,
+                                            uint32_t steps, uint32_t flip, uint32_t s_base, uint32_t k_base,
+                                            int32_t d_base, EmitStage& st, uint32_t expect_s, uint32_t expect_k,
+                                            int32_t expect_d, int lane)
 {
-    const int nsteps = (g.len + kStepBytes - 1) / kStepBytes;
-    uint32_t carry = (entry.x >> 1) & 1u, par = entry.x & 1u;
-    uint32_t s_base = entry.y, k_base = entry.z;
-    int32_t d_base = (int32_t)entry.w;
     uint32_t s_flush = s_base, k_flush = k_base;   // output indices of stage[0]
-    uint32_t in_run = 0;
     const uint64_t pos_lane = g.seg_log + g.off + (uint64_t)lane * kBytesPerThread + 1u;
-    for (int j = 0; j < nsteps; j++) {
-        producer_issue<R>(P, pr, ring, lane, walk);
-        cp_async_wait<kDepth>();
-        uint4 lo = ring.v[cs][0], hi = ring.v[cs][1];
-        cs = cs + 1 == kRing ? 0 : cs + 1;
-        const int step_len = min(kStepBytes, g.len - j * kStepBytes);
-        const int valid = min(kBytesPerThread, step_len - lane * kBytesPerThread);
-        if (valid < kBytesPerThread) {
-            if (16 > valid) mask_chunk(lo, valid);
-            mask_chunk(hi, valid - 16);
-        }
-        const uint32_t w[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
-        if (in_run) {
-            uint32_t d = 0;
-#pragma unroll
-            for (int k = 0; k < 8; k++) d |= w[k] ^ 0x5C5C5C5Cu;
-            if (__all_sync(FULL, d == 0u)) continue;      // 1 KiB of backslashes: an even run
-        }
-        uint32_t planes[8];
-        bit_planes32(w, planes);
-        const Classes c = classify_planes<LINES>(planes);
-        // escapes, with the exact carry into the step
-        uint32_t lane_carry;
-        if (!__any_sync(FULL, (int32_t)c.bs < 0)) {
-            lane_carry = (lane == 0) ? carry : 0u;
-            carry = 0;
-            in_run = 0;
-        } else {
-            const uint32_t nonall = __ballot_sync(FULL, c.bs != FULL);
-            const uint32_t couts = __ballot_sync(FULL, escape_cout(c.bs) != 0u);
-            const uint32_t prior = nonall & lt;
-            lane_carry = prior ? (couts >> (31 - __clz(prior))) & 1u : carry;
-            if (!nonall) { in_run = 1; continue; }
-            carry = (couts >> (31 - __clz(nonall))) & 1u;
-            in_run = (nonall >> 31) ^ 1u;
-        }
-        uint32_t dummy;
-        const uint32_t esc = escaped32(c.bs, lane_carry, &dummy);
-        const uint32_t rq = c.q & ~esc;
-        const uint32_t qb = __ballot_sync(FULL, __popc(rq) & 1u);
-        const uint32_t lpar = par ^ (__popc(qb & lt) & 1u);
-        par ^= __popc(qb) & 1u;
-        const uint32_t M = prefix_xor(rq) ^ (lpar ? FULL : 0u);
-        const uint32_t stm = c.st & ~M;
+    uint32_t rem = steps;
+    uint4 nm = make_uint4(0, 0, 0, 0);
+    if (rem) nm = __ldcg(mk + (size_t)(__ffs(rem) - 1) * 32);
+    while (rem) {
+        const int j = __ffs(rem) - 1;
+        rem &= rem - 1u;
+        const uint4 m = nm;
+        if (rem) nm = __ldcg(mk + (size_t)(__ffs(rem) - 1) * 32);   // the next stored step
+        const uint32_t opw = m.x, brw = m.x | m.y, xw = m.z;
+        const uint32_t stm = (brw | xw) & ~(m.w ^ flip);
         if (!__any_sync(FULL, stm)) continue;           // nothing outside strings in this step
-        const uint32_t brm = c.br & stm;
-        const uint32_t opm = c.op & stm;
+        const uint32_t brm = brw & stm;
+        const uint32_t opm = opw & stm;
+        const uint32_t curm = xw & brw;
         // the three counts (each <= 32 per lane) packed in 10-bit fields: one
         // scan.  The exclusive prefixes stay <= 31 * 32 < 1024 per field; a
         // step's totals (up to 1024) are taken field by field from lane 31's
@@ -712,17 +656,17 @@ __device__ __forceinline__ void emit_region(const ScanParams& P, const Region& g
             const uint64_t pcap = P.out_cap - min(P.out_cap, g.out_base);
             const uint64_t bcap = P.brk_cap - min(P.brk_cap, g.brk_base);
             uint32_t r = s_base + e1, kr = k_base + e2;
-            uint32_t m = stm;
+            uint32_t mm = stm;
             bool bad = false;
-            while (m) {
-                const int b = __ffs(m) - 1;
-                m &= m - 1u;
+            while (mm) {
+                const int b = __ffs(mm) - 1;
+                mm &= mm - 1u;
                 if (r < pcap) { pos[r] = (int32_t)(pos0 + (uint32_t)b); pair[r] = 0; } else bad = true;
                 if ((brm >> b) & 1u) {
                     const uint32_t is_open = (opm >> b) & 1u;
                     const int32_t lvl = is_open ? depth : depth - 1;
                     depth += is_open ? 1 : -1;
-                    const uint32_t cur = ((c.cur >> b) & 1u) ? kCurly : 0u;
+                    const uint32_t cur = ((curm >> b) & 1u) ? kCurly : 0u;
                     if (kr < bcap) brk[kr] = make_uint2(r | cur, ((uint32_t)lvl << 1) | is_open); else bad = true;
                     kr++;
                 }
@@ -734,24 +678,24 @@ __device__ __forceinline__ void emit_region(const ScanParams& P, const Region& g
         } else {
             // positions into the stage
             uint32_t i = staged_s + e1;
-            uint32_t m = stm;
-            while (m) {
-                const int b = __ffs(m) - 1;
-                m &= m - 1u;
+            uint32_t mm = stm;
+            while (mm) {
+                const int b = __ffs(mm) - 1;
+                mm &= mm - 1u;
                 st.pos[i++] = (int32_t)(pos0 + (uint32_t)b);
             }
             // bracket records into the stage
             uint32_t kk = staged_k + e2;
             const uint32_t sl = s_base + e1;   // structural index of the lane's first structural
-            m = brm;
-            while (m) {
-                const int b = __ffs(m) - 1;
-                m &= m - 1u;
+            mm = brm;
+            while (mm) {
+                const int b = __ffs(mm) - 1;
+                mm &= mm - 1u;
                 const uint32_t is_open = (opm >> b) & 1u;
                 const int32_t lvl = is_open ? depth : depth - 1;
                 depth += is_open ? 1 : -1;
                 const uint32_t sidx = sl + (uint32_t)__popc(stm & ((1u << b) - 1u));
-                const uint32_t cur = ((c.cur >> b) & 1u) ? kCurly : 0u;
+                const uint32_t cur = ((curm >> b) & 1u) ? kCurly : 0u;
                 st.brk[kk++] = make_uint2(sidx | cur, ((uint32_t)lvl << 1) | is_open);
             }
         }
@@ -766,38 +710,21 @@ __device__ __forceinline__ void emit_region(const ScanParams& P, const Region& g
         atomicOr(&P.ctrl->error_flags, CJ_FLAG_OVERFLOW);
 }
 
-template <bool LINES, int R>
-__global__ void __launch_bounds__(kThreads) scan_emit(ScanParams P)
+template <int R>
+__global__ void __launch_bounds__(kThreads, 4) scan_emit(ScanParams P)
 {
     __shared__ EmitStage s_stage[kWarpsPerBlock];
-    __shared__ LaneRing s_ring[kThreads];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t lt = lanemask_lt();
     if (aborted(P.ctrl)) return;
     const uint32_t n = *reinterpret_cast<const volatile uint32_t*>(&P.ctrl->n_work);
     const uint32_t nw = gridDim.x * kWarpsPerBlock;
-    const uint32_t first = blockIdx.x * kWarpsPerBlock + warp;
-    if (first >= n) return;
-    const WorkWalk walk{P.work, nw, n};
-    LaneRing& ring = s_ring[threadIdx.x];
-    Producer pr;
-    pr.slot = 0;
-    producer_enter<R>(P, pr, first, lane, walk);
-    for (int d = 0; d < kDepth; d++) producer_issue<R>(P, pr, ring, lane, walk);
-    int cs = 0;
-    for (uint32_t i = first; i < n; i += nw) {
-        const uint32_t r = __ldcg(P.work + i);
-        const uint4 e = __ldcg(P.rentry + r);
-        Ent t[4];
-        load_tab(P.rtab + (size_t)r * 4, t);
-        Ent v;
-        v.st = e.x & 3u; v.s = e.y; v.k = e.z; v.d = (int32_t)e.w;
-        const Ent x = ent_apply(v, t);          // the region's end value
+    for (uint32_t i = blockIdx.x * kWarpsPerBlock + warp; i < n; i += nw) {
+        const uint4 a = __ldcg(P.work + 2 * (size_t)i), b = __ldcg(P.work + 2 * (size_t)i + 1);
         Region g;
-        region_of(P, r, R * kStepBytes, g);
-        emit_region<LINES, R>(P, g, e, s_stage[warp], x.s, x.k, x.d, lane, lt, pr, ring, cs, walk);
+        region_of(P, a.x, R * kStepBytes, g);
+        emit_region(P, g, P.masks + (size_t)a.x * R * 32 + lane, a.y & 0xFFFFu, (a.y >> 31) ? FULL : 0u, a.z, a.w,
+                    (int32_t)b.x, s_stage[warp], b.y, b.z, (int32_t)b.w, lane);
     }
-    cp_async_wait<0>();
 }
 
 template <int R>
@@ -808,18 +735,17 @@ void launch_r(const ScanParams& p, bool lines, int tables_grid, int emit_grid, c
 #ifdef CJ_EMU
     (void)stream; (void)ev;
     cj_emu::launch(tables_grid, kThreads, 0, [&] { if (lines) scan_tables<true, R>(p); else scan_tables<false, R>(p); });
-    if (nb > 1) cj_emu::launch(nb, kThreads, 0, [&] { prefix_reduce(p); });
-    cj_emu::launch(nb, kThreads, 0, [&] { prefix_apply(p); });
-    cj_emu::launch(emit_grid, kThreads, 0, [&] { if (lines) scan_emit<true, R>(p); else scan_emit<false, R>(p); });
+    if (nb > 1) cj_emu::launch(nb, kPrefixPerBlock, 0, [&] { prefix_reduce(p); });
+    cj_emu::launch(nb, kPrefixPerBlock, 0, [&] { prefix_apply(p); });
+    cj_emu::launch(emit_grid, kThreads, 0, [&] { scan_emit<R>(p); });
 #else
     if (lines) scan_tables<true, R><<<tables_grid, kThreads, 0, stream>>>(p);
     else scan_tables<false, R><<<tables_grid, kThreads, 0, stream>>>(p);
     if (ev) cudaEventRecord(ev[0], stream);
-    if (nb > 1) prefix_reduce<<<nb, kThreads, 0, stream>>>(p);
-    prefix_apply<<<nb, kThreads, 0, stream>>>(p);
+    if (nb > 1) prefix_reduce<<<nb, kPrefixPerBlock, 0, stream>>>(p);
+    prefix_apply<<<nb, kPrefixPerBlock, 0, stream>>>(p);
     if (ev) cudaEventRecord(ev[1], stream);
-    if (lines) scan_emit<true, R><<<emit_grid, kThreads, 0, stream>>>(p);
-    else scan_emit<false, R><<<emit_grid, kThreads, 0, stream>>>(p);
+    scan_emit<R><<<emit_grid, kThreads, 0, stream>>>(p);
     if (ev) cudaEventRecord(ev[2], stream);
 #endif
 }
@@ -833,8 +759,7 @@ int blocks_per_sm(bool lines, bool emit)
 #else
     int n = 0;
     cudaError_t e;
-    if (emit) e = lines ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, scan_emit<true, R>, kThreads, 0)
-                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, scan_emit<false, R>, kThreads, 0);
+    if (emit) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, scan_emit<R>, kThreads, 0);
     else e = lines ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, scan_tables<true, R>, kThreads, 0)
                    : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, scan_tables<false, R>, kThreads, 0);
     return (e == cudaSuccess && n > 0) ? n : 1;
@@ -848,7 +773,7 @@ bool region_steps_valid(int r) { return r == 4 || r == 8 || r == 16; }
 int scan_launches(uint32_t n_regions)
 {
     if (n_regions == 0) return 0;
-    return (n_regions > (uint32_t)kPrefixPerBlock) ? 4 : 3;
+    return n_regions > (uint32_t)kPrefixPerBlock ? 4 : 3;
 }
 
 void launch_scan(const ScanParams& p, bool lines, const ScanShape& shape, cudaStream_t stream, cudaEvent_t* ev)

@@ -43,15 +43,16 @@ using Clock = std::chrono::steady_clock;
 // Device bytes one document of `size` bytes adds to a batch arena: input
 // padded to 1 KiB, int32 positions and pair row, 8-byte bracket records and
 // 4-byte spine slots per chunk-aligned byte, the int32 result layout, region
-// tables, entry values and work list (104 bytes per region of the smallest
-// size); times the arena's 1/8 growth headroom.
+// tables and work list (104 bytes per region of the smallest size), the emit
+// masks (half a byte per input byte and 8 KiB per document); times the arena's
+// 1/8 growth headroom.
 uint64_t doc_device_bytes(size_t size)
 {
     const uint64_t b = size;
     const uint64_t chunked = (b + 511) / 512 * 512 + 512;
     const uint64_t regions = b / ((uint64_t)cj::kRegionStepsAllowed[0] * cj::kStepBytes) + 2;
     const uint64_t raw = (b + 1024) + 8 * (b + 1) + 8 * chunked + 4 * chunked + 4 * (2 * b + 4) +
-                         104 * regions + 64;
+                         104 * regions + b / 2 + 8192 + 64;
     return raw + raw / 8;
 }
 

@@ -134,7 +134,7 @@ cj_status cj_parse_into(cj_context* ctx, const uint8_t* host_data, size_t size, 
  * (a cudaStream_t; NULL is the default stream) of the current device.  It
  * allocates nothing, on the device or the host: its scratch is a fixed
  * __device__ array of the library, sized for documents of at most
- * CJ_NOALLOC_MAX_BYTES (about 21 MiB of device memory).  Larger documents are
+ * CJ_NOALLOC_MAX_BYTES (about 22 MiB of device memory).  Larger documents are
  * refused with CJ_ERR_TOO_LARGE; an `out_cap` under 2*(S+2) with
  * CJ_ERR_CAPACITY.  Returns once the parse has finished, with `info` filled
  * and the verdict as the status.  `d_out` is written only when the status is

@@ -105,9 +105,9 @@ int run(const uint8_t* data, const size_t* sizes, size_t n, bool lines, bool bat
     uint32_t* d_region_seg = galloc<uint32_t>(std::max<size_t>(regions, 1));
     std::copy(region_seg.begin(), region_seg.end(), d_region_seg);
     uint4* rtab = galloc<uint4>((size_t)regions * 4);
-    uint4* rentry = galloc<uint4>(regions);
     uint4* bagg = galloc<uint4>(prefix_blocks(regions) * 4);
-    uint32_t* work = galloc<uint32_t>(regions);
+    uint4* work = galloc<uint4>((size_t)regions * 2);
+    uint4* masks = galloc<uint4>((size_t)regions * region_steps * 32);
     Ctrl* ctrl = galloc<Ctrl>(1);
     SegmentOut* seg_out = galloc<SegmentOut>(n);
     uint32_t* seg_err = batch ? galloc<uint32_t>(n) : nullptr;
@@ -136,8 +136,8 @@ int run(const uint8_t* data, const size_t* sizes, size_t n, bool lines, bool bat
     sp.out_cap = s_cap;
     sp.brk_cap = b_cap;
     sp.rtab = rtab;
-    sp.rentry = rentry;
     sp.bagg = bagg;
+    sp.masks = masks;
     sp.work = work;
     sp.ctrl = ctrl;
     sp.seg_out = seg_out;

@@ -133,3 +133,15 @@ def test_batch(emu, oracle):
         elif r.flags & oracle.ERR_BRACKETS:
             assert dfl[i] & 2, i
         o += int(dS[i])
+
+
+@pytest.mark.parametrize("lines", [False, True])
+def test_multi_block_prefix(emu, oracle, cj, lines):
+    """More than 1024 regions: the prefix composes several blocks."""
+    if lines:
+        d, _ = synth.synth_lines(synth.CONFIG_SEED_BASE + 3, 5 << 20)
+        check(emu, oracle, d, lines=True, chunks=cj.plan_lines_count(d, 3), region_kib=4)
+    else:
+        d = synth.synth_document(0x601D7777, (5 << 20) + 12345, max_depth=12, huge_string_frac=0.02,
+                                 huge_string_min=20000, huge_string_max=90000)
+        check(emu, oracle, d, region_kib=4)
