@@ -200,15 +200,29 @@ __device__ __forceinline__ void stream_enter(const ScanParams& P, Stream& st, ui
     stream_load(st);
 }
 
-// take the next step (lo, hi) and load the one after it
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+#ifndef CJ_EMU
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+#else
+    (void)p;
+#endif
+}
+
+// take the next step (lo, hi), load the one after it, and ask for the one
+// after that to be brought into L2 (within the region), so that the load
+// issued one step ahead mostly waits for L2, not HBM
 template <int R, typename Walk>
 __device__ __forceinline__ void stream_take(const ScanParams& P, Stream& st, uint4& lo, uint4& hi, int lane,
                                             const Walk& walk) {
     lo = st.a;
     hi = st.b;
     if (st.c == kNoRegion) return;
-    if (++st.j < st.n) stream_load(st);
-    else stream_enter<R>(P, st, walk.next(st.c), lane, walk);
+    if (++st.j < st.n) {
+        stream_load(st);
+        if (st.j + 1 < st.n) prefetch_l2(st.src + (size_t)(st.j + 1) * kStepBytes);
+    } else {
+        stream_enter<R>(P, st, walk.next(st.c), lane, walk);
+    }
 }
 
 // ---- transfer-table helpers ---------------------------------------------------------
@@ -283,9 +297,11 @@ __device__ __forceinline__ void region_table(const ScanParams& P, const Region& 
     uint32_t ucarry = 0;                   // UTF-8 carry into the step (warp uniform)
     uint32_t carry = 0, par = 0;           // escape carry / quote parity (warp uniform)
     uint32_t started = 0, wflip = 0;       // first non-all-backslash lane seen / its flip
-    uint32_t in_run = 0;                   // the previous step ended in 32 backslashes
+    uint32_t in_run = 0;                   // the previous step ended in a backslash
     uint32_t steps = 0;                    // steps whose mask words were stored
-    uint32_t n_c0 = 0, n_ct = 0, n_k0 = 0, n_kt = 0, n_o0 = 0, n_ot = 0;   // per lane
+    // per lane, two counts per register (low half: outside strings for an entry
+    // outside one; high half: all): structurals, brackets, opens (<= 512 each)
+    uint32_t n_c = 0, n_k = 0, n_o = 0;
     for (int j = 0; j < nsteps; j++) {
         uint4 lo, hi;
         stream_take<R>(P, st, lo, hi, lane, walk);
@@ -297,9 +313,10 @@ __device__ __forceinline__ void region_table(const ScanParams& P, const Region& 
         }
         const uint32_t w[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
         if (in_run) {
-            // inside a long backslash run: a step of 1 KiB of backslashes is an
-            // even run (the escape carry passes through), opens no UTF-8
-            // sequence, and has no quote or structural byte -- nothing changes
+            // after a step that ended in a backslash: a step of 1 KiB of
+            // backslashes (inside a long run) is an even run (the escape carry
+            // passes through), opens no UTF-8 sequence, and has no quote or
+            // structural byte -- nothing changes
             uint32_t d = 0;
 #pragma unroll
             for (int k = 0; k < 8; k++) d |= w[k] ^ 0x5C5C5C5Cu;
@@ -330,9 +347,10 @@ __device__ __forceinline__ void region_table(const ScanParams& P, const Region& 
 
         // escapes: carry from the nearest earlier lane that is not all backslashes
         uint32_t lane_carry;
-        if (!__any_sync(FULL, (int32_t)c.bs < 0)) {
+        const uint32_t ends_bs = __ballot_sync(FULL, (int32_t)c.bs < 0);   // lanes ending in a backslash
+        in_run = ends_bs >> 31;
+        if (!ends_bs) {
             lane_carry = (lane == 0) ? carry : 0u;
-            in_run = 0;
             if (!started) {
                 wflip = __shfl_sync(FULL, (c.q >> (__ffs(~c.bs) - 1)) & 1u, 0);
                 started = 1;
@@ -351,9 +369,7 @@ __device__ __forceinline__ void region_table(const ScanParams& P, const Region& 
                     started = 1;
                 }
                 carry = (couts >> (31 - __clz(nonall))) & 1u;
-                in_run = (nonall >> 31) ^ 1u;
             } else {
-                in_run = 1;
                 continue;
             }
         }
@@ -364,9 +380,9 @@ __device__ __forceinline__ void region_table(const ScanParams& P, const Region& 
         const uint32_t lpar = par ^ (__popc(qb & lt) & 1u);
         par ^= __popc(qb) & 1u;
         const uint32_t M = prefix_xor(rq) ^ (lpar ? FULL : 0u);
-        n_c0 += __popc(c.st & ~M); n_ct += __popc(c.st);
-        n_k0 += __popc(c.br & ~M); n_kt += __popc(c.br);
-        n_o0 += __popc(c.op & ~M); n_ot += __popc(c.op);
+        n_c += (uint32_t)__popc(c.st & ~M) | ((uint32_t)__popc(c.st) << 16);
+        n_k += (uint32_t)__popc(c.br & ~M) | ((uint32_t)__popc(c.br) << 16);
+        n_o += (uint32_t)__popc(c.op & ~M) | ((uint32_t)__popc(c.op) << 16);
         // the step's four mask words for the emit kernel, when it holds any
         // structural character: opens, closes, `x` (braces among brackets and
         // every other structural) and the structurals inside strings for an
@@ -376,9 +392,9 @@ __device__ __forceinline__ void region_table(const ScanParams& P, const Region& 
             steps |= 1u << j;
         }
     }
-    const int32_t C0 = (int32_t)__reduce_add_sync(FULL, n_c0), Ct = (int32_t)__reduce_add_sync(FULL, n_ct);
-    const int32_t K0 = (int32_t)__reduce_add_sync(FULL, n_k0), Kt = (int32_t)__reduce_add_sync(FULL, n_kt);
-    const int32_t O0 = (int32_t)__reduce_add_sync(FULL, n_o0), Ot = (int32_t)__reduce_add_sync(FULL, n_ot);
+    const int32_t C0 = (int32_t)__reduce_add_sync(FULL, n_c & 0xFFFFu), Ct = (int32_t)__reduce_add_sync(FULL, n_c >> 16);
+    const int32_t K0 = (int32_t)__reduce_add_sync(FULL, n_k & 0xFFFFu), Kt = (int32_t)__reduce_add_sync(FULL, n_k >> 16);
+    const int32_t O0 = (int32_t)__reduce_add_sync(FULL, n_o & 0xFFFFu), Ot = (int32_t)__reduce_add_sync(FULL, n_o >> 16);
     const int32_t D0 = 2 * O0 - K0, Dt = 2 * Ot - Kt;
     if (lane < 4) {
         // a segment's first region is entered outside strings at depth 0 whatever

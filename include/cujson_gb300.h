@@ -246,7 +246,7 @@ cj_status cj_copy_batch_result(cj_context* ctx, int32_t* host_out, size_t out_ca
  * for each candidate shape, keeps the fastest in the context and reports it
  * (and, optionally, every candidate tried with its mean milliseconds). */
 typedef struct cj_tuning {
-    int32_t region_kib;          /* bytes one warp scans as a unit: 4, 8 or 16 KiB (0: 8) */
+    int32_t region_kib;          /* bytes one warp scans as a unit: 4, 8 or 16 KiB (0: 16) */
     int32_t scan_blocks_per_sm;  /* resident 256-thread blocks per SM of the scan's table and */
     int32_t emit_blocks_per_sm;  /* emit kernels (0: as many as fit) */
     int32_t pair_blocks;         /* pairing grid (0: sized to the bracket count) */
