@@ -26,7 +26,7 @@ constexpr int kStepBytes = 32 * kBytesPerThread;          // 1 KiB
 constexpr int kPadBytes = kStepBytes;                     // segment padding granule
 constexpr int kRegionStepsAllowed[3] = {4, 8, 16};        // 4, 8 or 16 KiB regions
 constexpr int kRegionStepsDefault = 16;
-constexpr int kPrefixPerBlock = 1024;                     // regions per block of the prefix kernels
+constexpr int kPrefixPerBlock = 256;                      // regions per block of the prefix kernels
 
 // Pairing: one warp matches a chunk of this many bracket records.
 constexpr int kChunk = 512;

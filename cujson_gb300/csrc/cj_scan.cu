@@ -433,13 +433,17 @@ __global__ void __launch_bounds__(kThreads, 4) scan_tables(ScanParams P)
 }
 
 // ---- prefix over the region tables --------------------------------------------------
-// Blocks of 1024 regions, one per thread; a warp's 32 regions are a chunk.
-// Both kernels are shallow: a warp scan or reduction of tables per level.
+// Blocks of kPrefixPerBlock regions, one per thread; a warp's 32 regions are a
+// chunk.  Both kernels are shallow -- a warp scan or reduction of tables per
+// level -- and use small blocks, so that the table compositions spread over
+// every SM.
+
+constexpr int kPrefixWarps = kPrefixPerBlock / 32;
 
 // Block b: the composition of its regions' tables.
 __global__ void __launch_bounds__(kPrefixPerBlock) prefix_reduce(ScanParams P)
 {
-    __shared__ Ent s_w[32][4];
+    __shared__ Ent s_w[kPrefixWarps][4];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t r = blockIdx.x * (uint32_t)kPrefixPerBlock + threadIdx.x;
     Ent t[4];
@@ -452,8 +456,12 @@ __global__ void __launch_bounds__(kPrefixPerBlock) prefix_reduce(ScanParams P)
     }
     __syncthreads();
     if (warp == 0) {
+        if (lane < kPrefixWarps) {
 #pragma unroll
-        for (int k = 0; k < 4; k++) t[k] = s_w[lane][k];
+            for (int k = 0; k < 4; k++) t[k] = s_w[lane][k];
+        } else {
+            tab_identity(t);
+        }
         warp_reduce_tab(t, lane);
         if (lane == 0) store_tab(P.bagg + (size_t)blockIdx.x * 4, t);
     }
@@ -462,26 +470,42 @@ __global__ void __launch_bounds__(kPrefixPerBlock) prefix_reduce(ScanParams P)
 // Block b: entry values, segment ends, totals and the emit work list.
 __global__ void __launch_bounds__(kPrefixPerBlock) prefix_apply(ScanParams P)
 {
-    __shared__ Ent s_chunk[32][4];         // per warp: its total, then its exclusive prefix table
-    __shared__ Ent s_base;                 // the value before the block
-    __shared__ uint32_t s_cnt[32];
+    __shared__ Ent s_chunk[kPrefixWarps][4];   // per warp: a partial, its total, then its exclusive prefix
+    __shared__ Ent s_base;                     // the value before the block
+    __shared__ uint32_t s_cnt[kPrefixWarps];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (aborted(P.ctrl)) return;          // a timed-out run writes no outputs
     const uint32_t n = P.n_regions;
     const uint32_t b = blockIdx.x;
 
-    if (warp == 1) {
-        // the blocks before this one
-        const uint32_t q = (b + 31) / 32;
+    // the blocks before this one: every thread composes a run of them
+    {
+        const uint32_t q = (b + kPrefixPerBlock - 1) / kPrefixPerBlock;
         Ent t[4];
         tab_identity(t);
-        for (uint32_t i = lane * q; i < min(b, (uint32_t)(lane + 1) * q); i++) {
+        const uint32_t lo = threadIdx.x * q, hi = min(b, lo + q);
+        for (uint32_t i = lo; i < hi; i++) {
             Ent u[4];
             load_tab(P.bagg + (size_t)i * 4, u);
             tab_compose(t, u, t);
         }
         warp_reduce_tab(t, lane);
-        if (lane == 0) s_base = ent_apply(ent_identity(0), t);
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < 4; k++) s_chunk[warp][k] = t[k];
+        }
+        __syncthreads();
+        if (warp == 0) {
+            if (lane < kPrefixWarps) {
+#pragma unroll
+                for (int k = 0; k < 4; k++) t[k] = s_chunk[lane][k];
+            } else {
+                tab_identity(t);
+            }
+            warp_reduce_tab(t, lane);
+            if (lane == 0) s_base = ent_apply(ent_identity(0), t);
+        }
+        __syncthreads();
     }
 
     // this warp's chunk: the regions before each region, and the chunk's total
@@ -504,15 +528,21 @@ __global__ void __launch_bounds__(kPrefixPerBlock) prefix_apply(ScanParams P)
     if (warp == 0) {
         // the chunks before each chunk
         Ent c[4];
+        if (lane < kPrefixWarps) {
 #pragma unroll
-        for (int k = 0; k < 4; k++) c[k] = s_chunk[lane][k];
+            for (int k = 0; k < 4; k++) c[k] = s_chunk[lane][k];
+        } else {
+            tab_identity(c);
+        }
         warp_scan_tab(c, lane);
         Ent cx[4];
         shfl_tab(c, cx, 1, true);
         if (lane == 0) tab_identity(cx);
         __syncwarp();
+        if (lane < kPrefixWarps) {
 #pragma unroll
-        for (int k = 0; k < 4; k++) s_chunk[lane][k] = cx[k];
+            for (int k = 0; k < 4; k++) s_chunk[lane][k] = cx[k];
+        }
     }
     __syncthreads();
     const Ent v = ent_apply(ent_apply(s_base, s_chunk[warp]), ex);
@@ -561,7 +591,7 @@ __global__ void __launch_bounds__(kPrefixPerBlock) prefix_apply(ScanParams P)
     if (lane == 0) s_cnt[warp] = __popc(bal);
     __syncthreads();
     if (warp == 0) {
-        const uint32_t cnt = s_cnt[lane];
+        const uint32_t cnt = lane < kPrefixWarps ? s_cnt[lane] : 0u;
         uint32_t x = cnt;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -572,7 +602,7 @@ __global__ void __launch_bounds__(kPrefixPerBlock) prefix_apply(ScanParams P)
         uint32_t base = 0;
         if (lane == 0 && tot) base = atomicAdd(&P.ctrl->n_work, tot);
         base = __shfl_sync(FULL, base, 0);
-        s_cnt[lane] = base + x - cnt;
+        if (lane < kPrefixWarps) s_cnt[lane] = base + x - cnt;
     }
     __syncthreads();
     if (work) {
@@ -623,6 +653,9 @@ __device__ __forceinline__ void emit_region(const ScanParams& P, const Region& g
 {
     uint32_t s_flush = s_base, k_flush = k_base;   // output indices of stage[0]
     const uint64_t pos_lane = g.seg_log + g.off + (uint64_t)lane * kBytesPerThread + 1u;
+    // every stored step into L2 now, so that the one-ahead loads below wait
+    // for L2, not HBM
+    for (uint32_t m = steps; m; m &= m - 1u) prefetch_l2(mk + (size_t)(__ffs(m) - 1) * 32);
     uint32_t rem = steps;
     uint4 nm = make_uint4(0, 0, 0, 0);
     if (rem) nm = __ldcg(mk + (size_t)(__ffs(rem) - 1) * 32);
