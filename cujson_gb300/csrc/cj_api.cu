@@ -106,6 +106,7 @@ struct cj_context {
     // CUDA graph of the staged run, replayed by cj_run_staged_graph
     cudaGraphExec_t graph_exec = nullptr;
     bool graph_valid = false;
+    int64_t graph_launches = 0;         // kernels one replay launches
     uint64_t arena_gen = 0;             // bumped whenever a device buffer is (re)allocated
 
     // one-shot parses of large inputs: copies on copy_stream overlap the scan,
@@ -119,6 +120,22 @@ struct cj_context {
     // cuStreamWriteValue64 when the driver offers it (no kernel needs to run
     // beside the scan to raise d_ready); else a one-thread kernel does it
     CUresult (*write64)(CUstream, CUdeviceptr, cuuint64_t, unsigned int) = nullptr;
+
+    // streamed one-shot parses into pinned host memory: the scan runs in waves
+    // of wave_regions regions (0: one scan over all), each wave leaving its end
+    // value in wave_carry[w] and, written by the kernel, in pinned h_wave[w],
+    // and recording wave_ev[w], so that the positions of a finished wave go to
+    // the host on d2h_stream while later input bytes are still arriving
+    cudaStream_t d2h_stream = nullptr;
+    uint32_t wave_regions = 0;
+    uint32_t n_waves = 0;
+    DevBuf<uint4> wave_carry;
+    DevBuf<uint32_t> wave_nwork;
+    uint4* h_wave = nullptr;
+    uint4* d_h_wave = nullptr;          // h_wave as the device addresses it
+    size_t h_wave_cap = 0;
+    std::vector<cudaEvent_t> wave_ev;
+    cudaEvent_t ev_d2h = nullptr;
 
     // queries over a staged JSON-Lines result
     DevBuf<unsigned long long> q_count;
@@ -135,6 +152,9 @@ struct cj_context {
     int tune_emit_per_sm = 0;
     uint32_t tune_pair_blocks = 0;
     uint32_t tune_pair_threads = 0;
+    int tune_wave_mib = 0;
+    int tune_stream_wave_mib = 0;
+    bool wave_stream = false;           // the waves of this run report to the host (streamed parse)
 };
 
 namespace {
@@ -371,8 +391,29 @@ cj_status enqueue(cj_context* ctx, bool graph)
     sp.region_steps = ctx->run_region_steps;
     sp.sm_count = ctx->sm_count;
     ScanShape shape{ctx->tune_tables_per_sm, ctx->tune_emit_per_sm};
-    launch_scan(sp, ctx->lines, shape, ctx->stream, ev ? ev + 1 : nullptr);
-    ctx->launches += scan_launches(ctx->n_regions);
+    if (ctx->n_waves > 1) {
+        // waves: each scans its regions from the previous wave's end value,
+        // with its own work list (work items of wave w start at 2 * r_begin)
+        CJ_CUDA(cudaMemsetAsync(ctx->wave_nwork.p, 0, ctx->n_waves * sizeof(uint32_t), ctx->stream));
+        for (uint32_t w = 0; w < ctx->n_waves; w++) {
+            ScanParams wp = sp;
+            wp.r_begin = w * ctx->wave_regions;
+            wp.r_end = std::min<uint32_t>(ctx->n_regions, wp.r_begin + ctx->wave_regions);
+            wp.carry_in = w ? ctx->wave_carry.p + (w - 1) : nullptr;
+            wp.carry_out = ctx->wave_carry.p + w;
+            wp.carry_host = ctx->wave_stream ? ctx->d_h_wave + w : nullptr;
+            wp.n_work = ctx->wave_nwork.p + w;
+            wp.work = ctx->work.p + 2 * (size_t)wp.r_begin;
+            launch_scan(wp, ctx->lines, shape, ctx->stream, ev ? ev + 1 : nullptr);
+            ctx->launches += scan_launches(wp.r_end - wp.r_begin);
+            // no copy on the stream between waves: a copy queued behind a
+            // scan that waits for input bytes could hold up the input's copies
+            if (ctx->wave_stream) CJ_CUDA(cudaEventRecord(ctx->wave_ev[w], ctx->stream));
+        }
+    } else {
+        launch_scan(sp, ctx->lines, shape, ctx->stream, ev ? ev + 1 : nullptr);
+        ctx->launches += scan_launches(ctx->n_regions);
+    }
     if (ctx->batch) {
         launch_batch_prefix(ctx->segs.p, ctx->seg_out.p, ctx->n_segs, ctx->layout_off.p, ctx->rchunk_off.p,
                             ctx->stream);
@@ -419,11 +460,27 @@ cj_status enqueue(cj_context* ctx, bool graph)
     return CJ_OK;
 }
 
+cj_status prepare_waves(cj_context* ctx, uint64_t wave_bytes, bool streaming);
+
+// Waves for a staged run, as tuned (none for a run that fits one wave).
+cj_status tuned_waves(cj_context* ctx)
+{
+    ctx->n_waves = 0;
+    ctx->wave_stream = false;
+    if (!ctx->tune_wave_mib) return CJ_OK;
+    const uint64_t wb = (uint64_t)ctx->tune_wave_mib << 20;
+    if ((uint64_t)ctx->n_regions * ctx->run_region_steps * kStepBytes <= wb) return CJ_OK;
+    return prepare_waves(ctx, wb, false);
+}
+
 cj_status run(cj_context* ctx)
 {
     if (!ctx->staged) return CJ_ERR_NOT_STAGED;
     CJ_CUDA(cudaSetDevice(ctx->device));
-    return enqueue(ctx, false);
+    cj_status st = tuned_waves(ctx);
+    if (!st) st = enqueue(ctx, false);
+    ctx->n_waves = 0;
+    return st;
 }
 
 // Capture the staged run once into a CUDA graph, then replay it.
@@ -435,11 +492,15 @@ cj_status run_graph(cj_context* ctx)
         if (ctx->graph_exec) { cudaGraphExecDestroy(ctx->graph_exec); ctx->graph_exec = nullptr; }
         ctx->epoch = (ctx->epoch + 1) & 0x3FFFFFFFu;
         if (ctx->epoch == 0) ctx->epoch = 1;
+        cj_status st = tuned_waves(ctx);
+        if (st) return st;
         CJ_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
         const int64_t launches0 = ctx->launches;
-        cj_status st = enqueue(ctx, true);
+        st = enqueue(ctx, true);
+        ctx->n_waves = 0;
         cudaGraph_t g = nullptr;
         cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+        ctx->graph_launches = ctx->launches - launches0;
         ctx->launches = launches0;
         if (st) { if (g) cudaGraphDestroy(g); return st; }
         if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return CJ_ERR_CUDA; }
@@ -449,7 +510,7 @@ cj_status run_graph(cj_context* ctx)
         ctx->graph_valid = true;
     }
     CJ_CUDA(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
-    ctx->launches += scan_launches(ctx->n_regions) + 2 + (ctx->batch ? 2 : 0);
+    ctx->launches += ctx->graph_launches;
     ctx->batch_read = false;
     return CJ_OK;
 }
@@ -466,12 +527,61 @@ __global__ void mark_ready(unsigned long long* ready, unsigned long long bytes)
 
 constexpr size_t kOverlapMin = 64ull << 20;     // smaller inputs: one copy, then the run
 constexpr size_t kOverlapChunk = 64ull << 20;   // copy granularity of an overlapped run (16 / 32 / 64 / 128 MiB measured: 64 best)
+constexpr size_t kWaveBytes = 128ull << 20;     // default input bytes per scan wave of a streamed parse
+
+// input bytes per wave of a streamed parse (0: not streamed)
+uint64_t stream_wave_bytes(const cj_context* ctx)
+{
+    if (ctx->tune_stream_wave_mib < 0) return 0;
+    return ctx->tune_stream_wave_mib ? (uint64_t)ctx->tune_stream_wave_mib << 20 : kWaveBytes;
+}
+
+// Wave layout over the placed regions: waves of `wave_bytes` of regions with
+// their end values, and for a streamed parse (`streaming`) the pinned mirror
+// of the end values and one event per wave.  Allocates: call it outside a
+// stream capture.
+cj_status prepare_waves(cj_context* ctx, uint64_t wave_bytes, bool streaming)
+{
+    const uint64_t rb = (uint64_t)ctx->run_region_steps * kStepBytes;
+    ctx->wave_regions = (uint32_t)std::max<uint64_t>(1, wave_bytes / rb);
+    const uint32_t nw = (uint32_t)((ctx->n_regions + (uint64_t)ctx->wave_regions - 1) / ctx->wave_regions);
+    cj_status st;
+    if ((st = ensure(ctx, ctx->wave_carry, nw))) return st;
+    if ((st = ensure(ctx, ctx->wave_nwork, nw))) return st;
+    ctx->n_waves = nw;
+    ctx->wave_stream = streaming;
+    if (!streaming) return CJ_OK;
+    if (ctx->h_wave_cap < nw) {
+        if (ctx->h_wave) cudaFreeHost(ctx->h_wave);
+        ctx->h_wave = nullptr;
+        ctx->h_wave_cap = 0;
+        const size_t want = std::max<size_t>(nw, 32);
+        CJ_CUDA(cudaMallocHost((void**)&ctx->h_wave, want * sizeof(uint4)));
+        ctx->h_wave_cap = want;
+        if (cudaHostGetDevicePointer((void**)&ctx->d_h_wave, ctx->h_wave, 0) != cudaSuccess) {
+            cudaGetLastError();
+            cudaFreeHost(ctx->h_wave);
+            ctx->h_wave = nullptr;
+            ctx->d_h_wave = nullptr;
+            ctx->h_wave_cap = 0;
+            return CJ_ERR_CUDA;
+        }
+    }
+    while (ctx->wave_ev.size() < nw) {
+        cudaEvent_t e;
+        CJ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ctx->wave_ev.push_back(e);
+    }
+    // an aborted wave leaves its end value zero (below the previous one)
+    memset(ctx->h_wave, 0, nw * sizeof(uint4));
+    return CJ_OK;
+}
 
 // Stage and run in one go, the input's copy overlapping the scan: the small
 // tables go first, then the scan is launched and the input follows in chunks
 // on the copy stream, each chunk raising d_ready.
 cj_status stage_overlapped(cj_context* ctx, const uint8_t* const* chunks, const size_t* sizes, size_t n,
-                           bool lines)
+                           bool lines, bool waves = false)
 {
     ctx->staged = false;
     ctx->graph_valid = false;
@@ -500,6 +610,9 @@ cj_status stage_overlapped(cj_context* ctx, const uint8_t* const* chunks, const 
         logical += sizes[i];
     }
     if ((st = place_regions(ctx))) return st;
+    ctx->n_waves = 0;
+    ctx->wave_stream = false;
+    if (waves && (st = prepare_waves(ctx, stream_wave_bytes(ctx), true))) return st;
     CJ_CUDA(cudaMemsetAsync(ctx->d_ready, 0, sizeof(unsigned long long), ctx->stream));
     CJ_CUDA(cudaEventRecord(ctx->ev_reset, ctx->stream));
     ctx->n_bytes = total;
@@ -510,7 +623,7 @@ cj_status stage_overlapped(cj_context* ctx, const uint8_t* const* chunks, const 
     ctx->overlap_run = true;
     st = enqueue(ctx, false);
     ctx->overlap_run = false;
-    if (st) return st;
+    if (st) { ctx->n_waves = 0; return st; }
     CJ_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_reset, 0));
     for (size_t i = 0; i < n; i++) {
         const Segment& g = ctx->h_segs[i];
@@ -533,7 +646,63 @@ cj_status stage_overlapped(cj_context* ctx, const uint8_t* const* chunks, const 
     CJ_CUDA(cudaGetLastError());
     CJ_CUDA(cudaEventRecord(ctx->ev_copied, ctx->copy_stream));
     CJ_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_copied, 0));
+    // the scan spins on these copies: make sure they are submitted now, not
+    // when the host next waits on a stream that depends on them (the streamed
+    // parse waits on each wave's event, which does not)
+    const cudaError_t q = cudaStreamQuery(ctx->copy_stream);
+    if (q != cudaSuccess && q != cudaErrorNotReady) return CJ_ERR_CUDA;
     return CJ_OK;
+}
+
+bool is_pinned(const void* p);
+cj_status read_info(cj_context* ctx, cj_parse_info* info);
+
+// One-shot parse of a large pinned input into pinned host memory, streamed:
+// the input's copy, the scan (in waves) and the positions' copy back overlap.
+// Each wave's positions go to host_out as soon as the wave is scanned (while
+// the copy engine still brings in later bytes); the pair row follows the
+// pairing, which needs every bracket.  On a non-OK status host_out may hold
+// part of a result.
+cj_status parse_streamed(cj_context* ctx, const uint8_t* const* chunks, const size_t* sizes, size_t n,
+                         bool lines, int32_t* out, size_t cap, cj_parse_info* info)
+{
+    cj_status st = stage_overlapped(ctx, chunks, sizes, n, lines, true);
+    if (st) return st;
+    const uint32_t nw = ctx->n_waves;
+    ctx->n_waves = 0;                     // later runs of the staged input follow the tuning
+    ctx->wave_stream = false;
+    uint64_t s_prev = 0;
+    for (uint32_t w = 0; w < nw; w++) {
+        CJ_CUDA(cudaEventSynchronize(ctx->wave_ev[w]));
+        const uint64_t s_w = ctx->h_wave[w].y;
+        // an aborted or failed wave (end value below the last one, or past the
+        // input) ends the streaming; the verdict below reports it
+        if (s_w < s_prev || s_w > ctx->n_bytes || 2 * s_w + 4 > cap) break;
+        if (s_w > s_prev)
+            CJ_CUDA(cudaMemcpyAsync(out + 1 + s_prev, ctx->pos.p + s_prev, (s_w - s_prev) * sizeof(int32_t),
+                                    cudaMemcpyDeviceToHost, ctx->d2h_stream));
+        s_prev = s_w;
+    }
+    cj_parse_info local;
+    if (!info) info = &local;
+    st = read_info(ctx, info);
+    if (!st && info->status != CJ_OK) st = (cj_status)info->status;
+    const uint64_t S = (uint64_t)info->n_structural;
+    if (!st && 2 * S + 4 > cap) st = CJ_ERR_CAPACITY;
+    if (!st) {
+        if (S > s_prev)
+            CJ_CUDA(cudaMemcpyAsync(out + 1 + s_prev, ctx->pos.p + s_prev, (S - s_prev) * sizeof(int32_t),
+                                    cudaMemcpyDeviceToHost, ctx->d2h_stream));
+        if (S > 0)
+            CJ_CUDA(cudaMemcpyAsync(out + S + 2, ctx->pair.p, S * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                    ctx->d2h_stream));
+        out[0] = 0;
+        out[S + 1] = (int32_t)(S + 1);
+        out[2 * S + 2] = 0;
+        out[2 * S + 3] = 0;
+    }
+    CJ_CUDA(cudaStreamSynchronize(ctx->d2h_stream));
+    return st;
 }
 
 bool is_pinned(const void* p)
@@ -870,10 +1039,22 @@ cj_status cj_context_create(int device, cj_context** out)
         cudaEventCreateWithFlags(&ctx->ev_reset, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_copied, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_plan, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_d2h, cudaEventDisableTiming) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->d2h_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMalloc((void**)&ctx->d_ready, sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc((void**)&ctx->d_ctrl, sizeof(Ctrl)) != cudaSuccess) {
         cj_context_destroy(ctx);
         return CJ_ERR_CUDA;
+    }
+    {
+        // every kernel an overlapped run launches behind a waiting scan
+        cudaFuncAttributes a;
+        if (preload_scan_kernels() != cudaSuccess || preload_pair_kernels() != cudaSuccess ||
+            preload_batch_kernels() != cudaSuccess ||
+            cudaFuncGetAttributes(&a, (const void*)mark_ready) != cudaSuccess) {
+            cj_context_destroy(ctx);
+            return CJ_ERR_CUDA;
+        }
     }
     {
         void* fn = nullptr;
@@ -912,6 +1093,14 @@ void cj_context_destroy(cj_context* ctx)
     if (ctx->ev_copied) cudaEventDestroy(ctx->ev_copied);
     if (ctx->ev_plan) cudaEventDestroy(ctx->ev_plan);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    if (ctx->d2h_stream) {
+        cudaStreamSynchronize(ctx->d2h_stream);
+        cudaStreamDestroy(ctx->d2h_stream);
+    }
+    if (ctx->ev_d2h) cudaEventDestroy(ctx->ev_d2h);
+    for (cudaEvent_t e : ctx->wave_ev) cudaEventDestroy(e);
+    release(ctx->wave_carry); release(ctx->wave_nwork);
+    if (ctx->h_wave) cudaFreeHost(ctx->h_wave);
     if (ctx->d_ctrl) cudaFree(ctx->d_ctrl);
     if (ctx->h_ctrl) cudaFreeHost(ctx->h_ctrl);
     if (ctx->h_seg_out) cudaFreeHost(ctx->h_seg_out);
@@ -1055,6 +1244,11 @@ cj_status cj_parse_into(cj_context* ctx, const uint8_t* data, size_t size, int l
     if (!ctx || !data || size == 0 || !host_out) return finish(CJ_ERR_INVALID_ARGUMENT);
     const uint8_t* chunks[1] = {data};
     size_t sizes[1] = {size};
+    // streamed when the input makes at least two waves
+    const uint64_t wb = stream_wave_bytes(ctx);
+    if (wb && size >= 2 * wb && size >= kOverlapMin && size <= CJ_MAX_INPUT_BYTES && is_pinned(data) &&
+        is_pinned(host_out))
+        return finish(parse_streamed(ctx, chunks, sizes, 1, lines_mode != 0, host_out, out_cap, info));
     cj_status st = stage_run(ctx, chunks, sizes, 1, lines_mode != 0);
     cj_parse_info local;
     if (!info) info = &local;
@@ -1183,6 +1377,8 @@ cj_status cj_context_set_tuning(cj_context* ctx, const cj_tuning* t)
 {
     if (!ctx) return CJ_ERR_INVALID_ARGUMENT;
     const int rk = t ? std::max(0, t->region_kib) : 0;
+    const int wm = t ? std::max(0, t->wave_mib) : 0;
+    const int sw = t ? std::max(-1, t->stream_wave_mib) : 0;
     const int tb = t ? std::max(0, t->scan_blocks_per_sm) : 0;
     const int eb = t ? std::max(0, t->emit_blocks_per_sm) : 0;
     const uint32_t pb = t ? (uint32_t)std::max(0, t->pair_blocks) : 0u;
@@ -1194,6 +1390,8 @@ cj_status cj_context_set_tuning(cj_context* ctx, const cj_tuning* t)
     ctx->tune_emit_per_sm = eb;
     ctx->tune_pair_blocks = pb;
     ctx->tune_pair_threads = pt;
+    ctx->tune_wave_mib = wm;
+    ctx->tune_stream_wave_mib = sw;
     ctx->graph_valid = false;
     if (ctx->staged && ctx->run_region_steps != region_steps(ctx)) {
         // the staged input is cut into regions of the new size
@@ -1213,6 +1411,8 @@ cj_status cj_context_get_tuning(cj_context* ctx, cj_tuning* t)
     t->emit_blocks_per_sm = ctx->tune_emit_per_sm;
     t->pair_blocks = (int32_t)ctx->tune_pair_blocks;
     t->pair_threads = (int32_t)pair_threads(ctx);
+    t->wave_mib = ctx->tune_wave_mib;
+    t->stream_wave_mib = ctx->tune_stream_wave_mib;
     t->ms = 0.f;
     return CJ_OK;
 }
@@ -1237,6 +1437,8 @@ cj_status cj_autotune_staged(cj_context* ctx, int32_t reps, cj_tuning* best, cj_
                     t.emit_blocks_per_sm = tb;
                     t.pair_threads = pt;
                     t.pair_blocks = (int32_t)pb;
+                    t.wave_mib = 0;
+                    t.stream_wave_mib = ctx->tune_stream_wave_mib;
                     t.ms = 0.f;
                     cand.push_back(t);
                 }

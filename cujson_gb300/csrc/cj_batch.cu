@@ -197,6 +197,15 @@ __global__ void __launch_bounds__(256) batch_layout(const Segment* __restrict__ 
     }
 }
 
+cudaError_t preload_batch_kernels()
+{
+    cudaFuncAttributes a;
+    cudaError_t e = cudaFuncGetAttributes(&a, (const void*)batch_scatter);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, (const void*)batch_prefix);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, (const void*)batch_layout);
+    return e;
+}
+
 void launch_batch_scatter(const uint8_t* packed, const uint64_t* src_off, const uint64_t* word_off,
                           const Segment* segs, uint32_t n, uint64_t total_words, uint8_t* in, int sm_count,
                           cudaStream_t stream)

@@ -36,6 +36,18 @@ struct ScanParams {
     uint32_t input_wait_limit;  // polls before a wait for input gives up (0: default)
     int region_steps;           // 1 KiB steps per region: 4, 8 or 16
     int sm_count;
+    // A wave: the launch scans regions [r_begin, r_end) only (r_end 0: all),
+    // starting from the value in carry_in (nullptr: the document start) and
+    // leaving the value after r_end - 1 in carry_out (nullptr: not kept);
+    // its work items are counted in n_work (nullptr: ctrl->n_work).  The end
+    // value also goes to carry_host (nullptr: not), a device-visible pointer
+    // into pinned host memory, so that the host reads it once the wave's
+    // kernels are done without a copy between them on the stream.
+    uint32_t r_begin, r_end;
+    const uint4* carry_in;
+    uint4* carry_out;
+    uint4* carry_host;
+    uint32_t* n_work;
 };
 
 // Launch shape of the scan kernels (0 = as many blocks as fit).
@@ -87,6 +99,15 @@ int scan_launches(uint32_t n_regions);
 bool region_steps_valid(int r);
 void launch_pair(const PairParams& p, int grid, cudaStream_t stream, int threads = 256);
 void launch_spine(const PairParams& p, int grid, cudaStream_t stream, int threads = 256);
+
+// Load the kernels of a file now (cudaFuncGetAttributes on each).  With lazy
+// module loading a kernel is loaded at its first launch, and that load can
+// wait for the kernels already running; an overlapped run queues kernels
+// behind a scan that waits for input bytes the host has not yet queued, so
+// every kernel such a run launches must be loaded before its first one.
+cudaError_t preload_scan_kernels();
+cudaError_t preload_pair_kernels();
+cudaError_t preload_batch_kernels();
 
 // key/value queries over a staged JSON-Lines result (cj_query.cu)
 // JSON-Lines chunk plan of a device buffer (cj_plan.cu); scratch: nb =

@@ -299,6 +299,18 @@ __global__ void __launch_bounds__(256) pair_spine(PairParams P)
     }
 }
 
+cudaError_t preload_pair_kernels()
+{
+#ifdef CJ_EMU
+    return cudaSuccess;
+#else
+    cudaFuncAttributes a;
+    cudaError_t e = cudaFuncGetAttributes(&a, (const void*)pair_chunks);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, (const void*)pair_spine);
+    return e;
+#endif
+}
+
 void launch_pair(const PairParams& p, int grid, cudaStream_t stream, int threads)
 {
     // one bucket-head table per warp: 4.1 KB each, 32.8 KB at 256 threads

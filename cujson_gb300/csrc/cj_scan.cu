@@ -417,9 +417,9 @@ __global__ void __launch_bounds__(kThreads, 4) scan_tables(ScanParams P)
     const int lane = threadIdx.x & 31;
     const uint32_t lt = lanemask_lt();
     const uint32_t nw = gridDim.x * kWarpsPerBlock;
-    const uint32_t first = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
-    if (first >= P.n_regions) return;
-    const uint32_t n = P.n_regions;
+    const uint32_t n = P.r_end;
+    const uint32_t first = P.r_begin + blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    if (first >= n) return;
     const StrideWalk walk{nw, n};
     Stream st;
     stream_enter<R>(P, st, first, lane, walk);
@@ -445,9 +445,9 @@ __global__ void __launch_bounds__(kPrefixPerBlock) prefix_reduce(ScanParams P)
 {
     __shared__ Ent s_w[kPrefixWarps][4];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t r = blockIdx.x * (uint32_t)kPrefixPerBlock + threadIdx.x;
+    const uint32_t r = P.r_begin + blockIdx.x * (uint32_t)kPrefixPerBlock + threadIdx.x;
     Ent t[4];
-    if (r < P.n_regions) load_tab(P.rtab + (size_t)r * 4, t);
+    if (r < P.r_end) load_tab(P.rtab + (size_t)r * 4, t);
     else tab_identity(t);
     warp_reduce_tab(t, lane);
     if (lane == 0) {
@@ -503,15 +503,23 @@ __global__ void __launch_bounds__(kPrefixPerBlock) prefix_apply(ScanParams P)
                 tab_identity(t);
             }
             warp_reduce_tab(t, lane);
-            if (lane == 0) s_base = ent_apply(ent_identity(0), t);
+            if (lane == 0) {
+                Ent v0 = ent_identity(0);
+                if (P.carry_in) {
+                    const uint4 c = __ldcg(P.carry_in);
+                    v0.st = c.x; v0.s = c.y; v0.k = c.z; v0.d = (int32_t)c.w;
+                }
+                s_base = ent_apply(v0, t);
+            }
         }
         __syncthreads();
     }
 
     // this warp's chunk: the regions before each region, and the chunk's total
-    const uint32_t r = b * (uint32_t)kPrefixPerBlock + threadIdx.x;
+    const uint32_t r = P.r_begin + b * (uint32_t)kPrefixPerBlock + threadIdx.x;
+    const bool in_range = r < P.r_end;
     Ent t[4];
-    if (r < n) load_tab(P.rtab + (size_t)r * 4, t);
+    if (in_range) load_tab(P.rtab + (size_t)r * 4, t);
     else tab_identity(t);
     Ent incl[4];
 #pragma unroll
@@ -550,7 +558,7 @@ __global__ void __launch_bounds__(kPrefixPerBlock) prefix_apply(ScanParams P)
     bool work = false;
     Ent e = v, nv = v;
     uint32_t steps_flip = 0;
-    if (r < n) {
+    if (in_range) {
         const uint32_t raw = t[0].st;           // the region's own table: wflip, stored steps
         const Ent x = ent_select(t, v.st & 3u);
         nv = ent_apply(v, t);
@@ -584,6 +592,14 @@ __global__ void __launch_bounds__(kPrefixPerBlock) prefix_apply(ScanParams P)
             P.ctrl->s_total = nv.s;
             P.ctrl->k_total = nv.k;
         }
+        if (r + 1 == P.r_end) {
+            const uint4 c = make_uint4(nv.st, nv.s, nv.k, (uint32_t)nv.d);
+            if (P.carry_out) *P.carry_out = c;
+            if (P.carry_host) {
+                __stcg(P.carry_host, c);
+                __threadfence_system();
+            }
+        }
     }
 
     // the block's regions with structurals go to the work list (one atomic per block)
@@ -600,7 +616,7 @@ __global__ void __launch_bounds__(kPrefixPerBlock) prefix_apply(ScanParams P)
         }
         const uint32_t tot = __shfl_sync(FULL, x, 31);
         uint32_t base = 0;
-        if (lane == 0 && tot) base = atomicAdd(&P.ctrl->n_work, tot);
+        if (lane == 0 && tot) base = atomicAdd(P.n_work ? P.n_work : &P.ctrl->n_work, tot);
         base = __shfl_sync(FULL, base, 0);
         if (lane < kPrefixWarps) s_cnt[lane] = base + x - cnt;
     }
@@ -765,7 +781,7 @@ __global__ void __launch_bounds__(kThreads, 4) scan_emit(ScanParams P)
     __shared__ EmitStage s_stage[kWarpsPerBlock];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (aborted(P.ctrl)) return;
-    const uint32_t n = *reinterpret_cast<const volatile uint32_t*>(&P.ctrl->n_work);
+    const uint32_t n = *reinterpret_cast<const volatile uint32_t*>(P.n_work ? P.n_work : &P.ctrl->n_work);
     const uint32_t nw = gridDim.x * kWarpsPerBlock;
     for (uint32_t i = blockIdx.x * kWarpsPerBlock + warp; i < n; i += nw) {
         const uint4 a = __ldcg(P.work + 2 * (size_t)i), b = __ldcg(P.work + 2 * (size_t)i + 1);
@@ -780,7 +796,7 @@ template <int R>
 void launch_r(const ScanParams& p, bool lines, int tables_grid, int emit_grid, cudaStream_t stream,
               cudaEvent_t* ev)
 {
-    const uint32_t nb = (p.n_regions + kPrefixPerBlock - 1) / kPrefixPerBlock;
+    const uint32_t nb = (p.r_end - p.r_begin + kPrefixPerBlock - 1) / kPrefixPerBlock;
 #ifdef CJ_EMU
     (void)stream; (void)ev;
     cj_emu::launch(tables_grid, kThreads, 0, [&] { if (lines) scan_tables<true, R>(p); else scan_tables<false, R>(p); });
@@ -819,15 +835,37 @@ int blocks_per_sm(bool lines, bool emit)
 
 bool region_steps_valid(int r) { return r == 4 || r == 8 || r == 16; }
 
+cudaError_t preload_scan_kernels()
+{
+#ifdef CJ_EMU
+    return cudaSuccess;
+#else
+    cudaFuncAttributes a;
+    const void* fns[] = {
+        (const void*)scan_tables<false, 4>, (const void*)scan_tables<false, 8>, (const void*)scan_tables<false, 16>,
+        (const void*)scan_tables<true, 4>,  (const void*)scan_tables<true, 8>,  (const void*)scan_tables<true, 16>,
+        (const void*)scan_emit<4>,          (const void*)scan_emit<8>,          (const void*)scan_emit<16>,
+        (const void*)prefix_reduce,         (const void*)prefix_apply,
+    };
+    for (const void* f : fns) {
+        const cudaError_t e = cudaFuncGetAttributes(&a, f);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+#endif
+}
+
 int scan_launches(uint32_t n_regions)
 {
     if (n_regions == 0) return 0;
     return n_regions > (uint32_t)kPrefixPerBlock ? 4 : 3;
 }
 
-void launch_scan(const ScanParams& p, bool lines, const ScanShape& shape, cudaStream_t stream, cudaEvent_t* ev)
+void launch_scan(const ScanParams& p0, bool lines, const ScanShape& shape, cudaStream_t stream, cudaEvent_t* ev)
 {
-    if (p.n_regions == 0) {
+    ScanParams p = p0;
+    if (p.r_end == 0 || p.r_end > p.n_regions) p.r_end = p.n_regions;
+    if (p.r_begin >= p.r_end) {
         for (int i = 0; ev && i < 3; i++) cudaEventRecord(ev[i], stream);
         return;
     }
@@ -835,7 +873,7 @@ void launch_scan(const ScanParams& p, bool lines, const ScanShape& shape, cudaSt
     const int sm = p.sm_count > 0 ? p.sm_count : 1;
     auto grid = [&](int per_sm_occ, int want_per_sm) {
         const int per_sm = want_per_sm > 0 ? (want_per_sm < per_sm_occ ? want_per_sm : per_sm_occ) : per_sm_occ;
-        const uint32_t need = (p.n_regions + kWarpsPerBlock - 1) / kWarpsPerBlock;
+        const uint32_t need = (p.r_end - p.r_begin + kWarpsPerBlock - 1) / kWarpsPerBlock;
         const uint32_t cap = (uint32_t)(per_sm * sm);
         return (int)(need < cap ? need : cap);
     };

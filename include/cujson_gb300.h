@@ -251,6 +251,11 @@ typedef struct cj_tuning {
     int32_t emit_blocks_per_sm;  /* emit kernels (0: as many as fit) */
     int32_t pair_blocks;         /* pairing grid (0: sized to the bracket count) */
     int32_t pair_threads;        /* pairing threads per block: 64, 128 or 256 (0: 256) */
+    int32_t wave_mib;            /* staged runs scan in waves of this many MiB of input, so a
+                                    wave's mask words are still in L2 for its emit (0: one scan) */
+    int32_t stream_wave_mib;     /* cj_parse_into of >= 2 waves of pinned input into pinned
+                                    output: waves of this many MiB whose positions are copied
+                                    back while later input arrives (0: 128; -1: not streamed) */
     float   ms;                  /* mean replay time when measured */
 } cj_tuning;
 cj_status cj_context_set_tuning(cj_context* ctx, const cj_tuning* tuning);   /* NULL: defaults */

@@ -62,9 +62,11 @@ constexpr size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
 // The whole run: segments laid out as the library lays them, scan, pairing.
 // `batch`: independent documents (own output and bracket bases, per-document
 // verdicts); otherwise one document or JSON-Lines chunks continuing counts.
+// `wave_regions` > 0: the scan runs in waves of that many regions, each from
+// the previous wave's end value, as a streamed parse runs it.
 int run(const uint8_t* data, const size_t* sizes, size_t n, bool lines, bool batch, int region_steps,
         int32_t* out_pos, int32_t* out_pair, size_t cap, int64_t* out_S, uint32_t* out_flags,
-        uint32_t* doc_flags, int64_t* doc_S)
+        uint32_t* doc_flags, int64_t* doc_S, uint32_t wave_regions = 0)
 {
     size_t total = 0, padded = 0;
     for (size_t i = 0; i < n; i++) { total += sizes[i]; padded += round_up(sizes[i], kPadBytes); }
@@ -144,7 +146,26 @@ int run(const uint8_t* data, const size_t* sizes, size_t n, bool lines, bool bat
     sp.seg_err = seg_err;
     sp.region_steps = region_steps;
     sp.sm_count = 3;
-    launch_scan(sp, lines, ScanShape{0, 0}, nullptr);
+    if (wave_regions) {
+        const uint32_t nw = (regions + wave_regions - 1) / wave_regions;
+        uint4* carry = galloc<uint4>(nw);
+        uint32_t* nwork = galloc<uint32_t>(nw);
+        for (uint32_t w = 0; w < nw; w++) {
+            ScanParams wp = sp;
+            wp.r_begin = w * wave_regions;
+            wp.r_end = std::min(regions, wp.r_begin + wave_regions);
+            wp.carry_in = w ? carry + (w - 1) : nullptr;
+            wp.carry_out = carry + w;
+            wp.n_work = nwork + w;
+            wp.work = work + 2 * (size_t)wp.r_begin;
+            launch_scan(wp, lines, ScanShape{0, 0}, nullptr);
+            // the wave's end value holds the counts through its last region
+            if (wp.r_end == regions && !batch && (carry[w].y != ctrl->s_total || carry[w].z != ctrl->k_total))
+                ctrl->error_flags |= CJ_FLAG_OVERFLOW;
+        }
+    } else {
+        launch_scan(sp, lines, ScanShape{0, 0}, nullptr);
+    }
 
     uint64_t* rchunk_off = nullptr;
     if (batch) {
@@ -212,6 +233,14 @@ extern "C" int cje_parse(const uint8_t* data, const size_t* sizes, size_t n, int
 {
     return run(data, sizes, n, lines != 0, false, region_steps, out_pos, out_pair, cap, out_S, out_flags,
                nullptr, seg_S);
+}
+
+extern "C" int cje_parse_waves(const uint8_t* data, const size_t* sizes, size_t n, int lines, int region_steps,
+                               uint32_t wave_regions, int32_t* out_pos, int32_t* out_pair, size_t cap,
+                               int64_t* out_S, uint32_t* out_flags)
+{
+    return run(data, sizes, n, lines != 0, false, region_steps, out_pos, out_pair, cap, out_S, out_flags,
+               nullptr, nullptr, wave_regions);
 }
 
 extern "C" int cje_parse_batch(const uint8_t* data, const size_t* sizes, size_t n, int region_steps,

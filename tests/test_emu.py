@@ -27,10 +27,14 @@ def emu():
                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                   ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_uint32),
                                   ctypes.c_void_p, ctypes.c_void_p]
+    L.cje_parse_waves.restype = ctypes.c_int
+    L.cje_parse_waves.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int,
+                                  ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                  ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_uint32)]
     return L
 
 
-def emu_parse(emu, data, lines=False, chunks=None, region_kib=8):
+def emu_parse(emu, data, lines=False, chunks=None, region_kib=8, wave_regions=0):
     buf = np.ascontiguousarray(np.frombuffer(bytes(data), np.uint8) if isinstance(data, bytes) else data)
     sizes = np.asarray(chunks if chunks is not None else [buf.size], np.uint64)
     cap = buf.size + 1
@@ -38,13 +42,17 @@ def emu_parse(emu, data, lines=False, chunks=None, region_kib=8):
     pair = np.zeros(cap, np.int32)
     S = ctypes.c_int64()
     fl = ctypes.c_uint32()
-    emu.cje_parse(buf.ctypes.data, sizes.ctypes.data, sizes.size, int(lines), region_kib, pos.ctypes.data,
-                  pair.ctypes.data, cap, ctypes.byref(S), ctypes.byref(fl), None)
+    if wave_regions:
+        emu.cje_parse_waves(buf.ctypes.data, sizes.ctypes.data, sizes.size, int(lines), region_kib, wave_regions,
+                            pos.ctypes.data, pair.ctypes.data, cap, ctypes.byref(S), ctypes.byref(fl))
+    else:
+        emu.cje_parse(buf.ctypes.data, sizes.ctypes.data, sizes.size, int(lines), region_kib, pos.ctypes.data,
+                      pair.ctypes.data, cap, ctypes.byref(S), ctypes.byref(fl), None)
     return pos[:S.value], pair[:S.value], fl.value
 
 
-def check(emu, oracle, data, lines=False, chunks=None, region_kib=8):
-    p, q, fl = emu_parse(emu, data, lines, chunks, region_kib)
+def check(emu, oracle, data, lines=False, chunks=None, region_kib=8, wave_regions=0):
+    p, q, fl = emu_parse(emu, data, lines, chunks, region_kib, wave_regions)
     r = oracle.parse(data, lines=lines, chunk_sizes=chunks)
     assert fl & 0x0C == 0, hex(fl)                      # no timeout, no count mismatch
     assert bool(fl & 1) == bool(r.flags & oracle.ERR_UTF8)
@@ -145,3 +153,23 @@ def test_multi_block_prefix(emu, oracle, cj, lines):
         d = synth.synth_document(0x601D7777, (5 << 20) + 12345, max_depth=12, huge_string_frac=0.02,
                                  huge_string_min=20000, huge_string_max=90000)
         check(emu, oracle, d, region_kib=4)
+
+
+@pytest.mark.parametrize("wave_regions", [1, 3, 256, 300, 600])
+@pytest.mark.parametrize("lines", [False, True])
+def test_waves(emu, oracle, cj, lines, wave_regions):
+    """The scan in waves of regions, each wave starting from the previous
+    wave's end value (a streamed parse): the same result as one scan, with wave
+    boundaries inside strings, escapes and JSON-Lines records, and waves of
+    more than one prefix block."""
+    if lines:
+        d, _ = synth.synth_lines(synth.CONFIG_SEED_BASE + 13, (2 << 20) + 777)
+        check(emu, oracle, d, lines=True, region_kib=4, wave_regions=wave_regions)
+        check(emu, oracle, d, lines=True, chunks=cj.plan_lines_count(d, 3), region_kib=4,
+              wave_regions=wave_regions)
+    else:
+        d = synth.synth_document(0x3A7E5, (2 << 20) + 4321, max_depth=12, huge_string_frac=0.05,
+                                 huge_string_min=5000, huge_string_max=30000)
+        check(emu, oracle, d, region_kib=4, wave_regions=wave_regions)
+        b = synth.synth_backslash_string(7, 300000)
+        check(emu, oracle, b, region_kib=4, wave_regions=wave_regions)
