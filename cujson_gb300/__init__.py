@@ -70,14 +70,14 @@ class Tuning(ctypes.Structure):
     """Launch shapes (cj_tuning): 0 = default."""
     _fields_ = [("region_kib", ctypes.c_int32), ("scan_blocks_per_sm", ctypes.c_int32),
                 ("emit_blocks_per_sm", ctypes.c_int32), ("pair_blocks", ctypes.c_int32),
-                ("pair_threads", ctypes.c_int32), ("wave_mib", ctypes.c_int32),
-                ("stream_wave_mib", ctypes.c_int32), ("ms", ctypes.c_float)]
+                ("pair_threads", ctypes.c_int32), ("stream_wave_mib", ctypes.c_int32),
+                ("ms", ctypes.c_float)]
 
     def as_dict(self):
         return {"region_kib": self.region_kib, "scan_blocks_per_sm": self.scan_blocks_per_sm,
                 "emit_blocks_per_sm": self.emit_blocks_per_sm, "pair_blocks": self.pair_blocks,
-                "pair_threads": self.pair_threads, "wave_mib": self.wave_mib,
-                "stream_wave_mib": self.stream_wave_mib, "ms": round(float(self.ms), 4)}
+                "pair_threads": self.pair_threads, "stream_wave_mib": self.stream_wave_mib,
+                "ms": round(float(self.ms), 4)}
 
 
 _lib: Optional[ctypes.CDLL] = None
@@ -429,9 +429,8 @@ class Context:
 
     # ---- launch shapes -------------------------------------------------------------
     def set_tuning(self, region_kib: int = 0, scan_blocks_per_sm: int = 0, emit_blocks_per_sm: int = 0,
-                   pair_blocks: int = 0, pair_threads: int = 0, wave_mib: int = 0,
-                   stream_wave_mib: int = 0) -> None:
-        t = Tuning(region_kib, scan_blocks_per_sm, emit_blocks_per_sm, pair_blocks, pair_threads, wave_mib,
+                   pair_blocks: int = 0, pair_threads: int = 0, stream_wave_mib: int = 0) -> None:
+        t = Tuning(region_kib, scan_blocks_per_sm, emit_blocks_per_sm, pair_blocks, pair_threads,
                    stream_wave_mib, 0.0)
         _check(lib().cj_context_set_tuning(self._h, ctypes.byref(t)), "set_tuning")
 

@@ -152,7 +152,6 @@ struct cj_context {
     int tune_emit_per_sm = 0;
     uint32_t tune_pair_blocks = 0;
     uint32_t tune_pair_threads = 0;
-    int tune_wave_mib = 0;
     int tune_stream_wave_mib = 0;
     bool wave_stream = false;           // the waves of this run report to the host (streamed parse)
 };
@@ -460,27 +459,11 @@ cj_status enqueue(cj_context* ctx, bool graph)
     return CJ_OK;
 }
 
-cj_status prepare_waves(cj_context* ctx, uint64_t wave_bytes, bool streaming);
-
-// Waves for a staged run, as tuned (none for a run that fits one wave).
-cj_status tuned_waves(cj_context* ctx)
-{
-    ctx->n_waves = 0;
-    ctx->wave_stream = false;
-    if (!ctx->tune_wave_mib) return CJ_OK;
-    const uint64_t wb = (uint64_t)ctx->tune_wave_mib << 20;
-    if ((uint64_t)ctx->n_regions * ctx->run_region_steps * kStepBytes <= wb) return CJ_OK;
-    return prepare_waves(ctx, wb, false);
-}
-
 cj_status run(cj_context* ctx)
 {
     if (!ctx->staged) return CJ_ERR_NOT_STAGED;
     CJ_CUDA(cudaSetDevice(ctx->device));
-    cj_status st = tuned_waves(ctx);
-    if (!st) st = enqueue(ctx, false);
-    ctx->n_waves = 0;
-    return st;
+    return enqueue(ctx, false);
 }
 
 // Capture the staged run once into a CUDA graph, then replay it.
@@ -492,12 +475,9 @@ cj_status run_graph(cj_context* ctx)
         if (ctx->graph_exec) { cudaGraphExecDestroy(ctx->graph_exec); ctx->graph_exec = nullptr; }
         ctx->epoch = (ctx->epoch + 1) & 0x3FFFFFFFu;
         if (ctx->epoch == 0) ctx->epoch = 1;
-        cj_status st = tuned_waves(ctx);
-        if (st) return st;
         CJ_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
         const int64_t launches0 = ctx->launches;
-        st = enqueue(ctx, true);
-        ctx->n_waves = 0;
+        cj_status st = enqueue(ctx, true);
         cudaGraph_t g = nullptr;
         cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
         ctx->graph_launches = ctx->launches - launches0;
@@ -536,11 +516,10 @@ uint64_t stream_wave_bytes(const cj_context* ctx)
     return ctx->tune_stream_wave_mib ? (uint64_t)ctx->tune_stream_wave_mib << 20 : kWaveBytes;
 }
 
-// Wave layout over the placed regions: waves of `wave_bytes` of regions with
-// their end values, and for a streamed parse (`streaming`) the pinned mirror
-// of the end values and one event per wave.  Allocates: call it outside a
-// stream capture.
-cj_status prepare_waves(cj_context* ctx, uint64_t wave_bytes, bool streaming)
+// Wave layout of a streamed parse over the placed regions: waves of
+// `wave_bytes` of regions, their end values on the device and in pinned host
+// memory, and one event per wave.
+cj_status prepare_waves(cj_context* ctx, uint64_t wave_bytes)
 {
     const uint64_t rb = (uint64_t)ctx->run_region_steps * kStepBytes;
     ctx->wave_regions = (uint32_t)std::max<uint64_t>(1, wave_bytes / rb);
@@ -549,8 +528,7 @@ cj_status prepare_waves(cj_context* ctx, uint64_t wave_bytes, bool streaming)
     if ((st = ensure(ctx, ctx->wave_carry, nw))) return st;
     if ((st = ensure(ctx, ctx->wave_nwork, nw))) return st;
     ctx->n_waves = nw;
-    ctx->wave_stream = streaming;
-    if (!streaming) return CJ_OK;
+    ctx->wave_stream = true;
     if (ctx->h_wave_cap < nw) {
         if (ctx->h_wave) cudaFreeHost(ctx->h_wave);
         ctx->h_wave = nullptr;
@@ -612,7 +590,7 @@ cj_status stage_overlapped(cj_context* ctx, const uint8_t* const* chunks, const 
     if ((st = place_regions(ctx))) return st;
     ctx->n_waves = 0;
     ctx->wave_stream = false;
-    if (waves && (st = prepare_waves(ctx, stream_wave_bytes(ctx), true))) return st;
+    if (waves && (st = prepare_waves(ctx, stream_wave_bytes(ctx)))) return st;
     CJ_CUDA(cudaMemsetAsync(ctx->d_ready, 0, sizeof(unsigned long long), ctx->stream));
     CJ_CUDA(cudaEventRecord(ctx->ev_reset, ctx->stream));
     ctx->n_bytes = total;
@@ -669,9 +647,9 @@ cj_status parse_streamed(cj_context* ctx, const uint8_t* const* chunks, const si
     cj_status st = stage_overlapped(ctx, chunks, sizes, n, lines, true);
     if (st) return st;
     const uint32_t nw = ctx->n_waves;
-    ctx->n_waves = 0;                     // later runs of the staged input follow the tuning
+    ctx->n_waves = 0;                     // later runs of the staged input scan in one go
     ctx->wave_stream = false;
-    uint64_t s_prev = 0;
+    uint64_t s_prev = 0, s_pair = UINT64_MAX;
     for (uint32_t w = 0; w < nw; w++) {
         CJ_CUDA(cudaEventSynchronize(ctx->wave_ev[w]));
         const uint64_t s_w = ctx->h_wave[w].y;
@@ -682,6 +660,14 @@ cj_status parse_streamed(cj_context* ctx, const uint8_t* const* chunks, const si
             CJ_CUDA(cudaMemcpyAsync(out + 1 + s_prev, ctx->pos.p + s_prev, (s_w - s_prev) * sizeof(int32_t),
                                     cudaMemcpyDeviceToHost, ctx->d2h_stream));
         s_prev = s_w;
+        if (w + 1 == nw && s_w > 0) {
+            // the last wave gives S, so the pair row's place in host_out: its
+            // copy follows the pairing kernels on the stream, with no round
+            // trip through the host (the input's copies are all done by now)
+            CJ_CUDA(cudaMemcpyAsync(out + s_w + 2, ctx->pair.p, s_w * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+            s_pair = s_w;
+        }
     }
     cj_parse_info local;
     if (!info) info = &local;
@@ -693,7 +679,7 @@ cj_status parse_streamed(cj_context* ctx, const uint8_t* const* chunks, const si
         if (S > s_prev)
             CJ_CUDA(cudaMemcpyAsync(out + 1 + s_prev, ctx->pos.p + s_prev, (S - s_prev) * sizeof(int32_t),
                                     cudaMemcpyDeviceToHost, ctx->d2h_stream));
-        if (S > 0)
+        if (S > 0 && S != s_pair)
             CJ_CUDA(cudaMemcpyAsync(out + S + 2, ctx->pair.p, S * sizeof(int32_t), cudaMemcpyDeviceToHost,
                                     ctx->d2h_stream));
         out[0] = 0;
@@ -1377,7 +1363,6 @@ cj_status cj_context_set_tuning(cj_context* ctx, const cj_tuning* t)
 {
     if (!ctx) return CJ_ERR_INVALID_ARGUMENT;
     const int rk = t ? std::max(0, t->region_kib) : 0;
-    const int wm = t ? std::max(0, t->wave_mib) : 0;
     const int sw = t ? std::max(-1, t->stream_wave_mib) : 0;
     const int tb = t ? std::max(0, t->scan_blocks_per_sm) : 0;
     const int eb = t ? std::max(0, t->emit_blocks_per_sm) : 0;
@@ -1390,7 +1375,6 @@ cj_status cj_context_set_tuning(cj_context* ctx, const cj_tuning* t)
     ctx->tune_emit_per_sm = eb;
     ctx->tune_pair_blocks = pb;
     ctx->tune_pair_threads = pt;
-    ctx->tune_wave_mib = wm;
     ctx->tune_stream_wave_mib = sw;
     ctx->graph_valid = false;
     if (ctx->staged && ctx->run_region_steps != region_steps(ctx)) {
@@ -1411,7 +1395,6 @@ cj_status cj_context_get_tuning(cj_context* ctx, cj_tuning* t)
     t->emit_blocks_per_sm = ctx->tune_emit_per_sm;
     t->pair_blocks = (int32_t)ctx->tune_pair_blocks;
     t->pair_threads = (int32_t)pair_threads(ctx);
-    t->wave_mib = ctx->tune_wave_mib;
     t->stream_wave_mib = ctx->tune_stream_wave_mib;
     t->ms = 0.f;
     return CJ_OK;
@@ -1437,7 +1420,6 @@ cj_status cj_autotune_staged(cj_context* ctx, int32_t reps, cj_tuning* best, cj_
                     t.emit_blocks_per_sm = tb;
                     t.pair_threads = pt;
                     t.pair_blocks = (int32_t)pb;
-                    t.wave_mib = 0;
                     t.stream_wave_mib = ctx->tune_stream_wave_mib;
                     t.ms = 0.f;
                     cand.push_back(t);

@@ -9,7 +9,7 @@
 //                 in-string mask, and the region's transfer table -- for each
 //                 of the 4 entry states (escape pending, inside a string): the
 //                 exit state, structural count, bracket count and depth delta.
-//   prefix_reduce (1024 regions per block, one per thread) composes each
+//   prefix_reduce (256 regions per block, one per thread) composes each
 //                 block's tables (only when there is more than one block).
 //   prefix_apply  (the same blocks) composes the blocks before its own, the
 //                 warps (chunks of 32 regions) before each warp and the regions
@@ -25,6 +25,10 @@
 //                 and bracket records (structural index, level, open flag,
 //                 brace or bracket) through a per-warp staging buffer in shared
 //                 memory, so that every global store is coalesced.
+//
+// A launch may cover a wave of regions [r_begin, r_end) only, starting from
+// the previous wave's end value (a streamed parse scans in waves so that each
+// wave's positions can leave for the host while later input still arrives).
 //
 // The input crosses HBM once; the masks (512 bytes per KiB, only for steps
 // with structural characters) are written once and read back only for the
@@ -53,10 +57,27 @@ constexpr uint32_t FULL = 0xFFFFFFFFu;
 constexpr int kThreads = 256;                  // 8 warps per block (tables, emit, prefix)
 constexpr int kWarpsPerBlock = kThreads / 32;
 constexpr uint32_t kInputWaitLimit = 1u << 22; // polls (>= 256 ns each) for input bytes
+// how many steps ahead of the current one the table kernel asks for a step to
+// be brought into L2 (the register load is one step ahead)
+#ifndef CJ_L2_AHEAD
+#define CJ_L2_AHEAD 2
+#endif
+constexpr int kL2Ahead = CJ_L2_AHEAD;
+// resident blocks per SM the table and emit kernels are compiled for (their
+// register budgets: 65536 / (256 x blocks))
+#ifndef CJ_TABLES_MIN_BLOCKS
+#define CJ_TABLES_MIN_BLOCKS 4
+#endif
+#ifndef CJ_EMIT_MIN_BLOCKS
+#define CJ_EMIT_MIN_BLOCKS 4
+#endif
+constexpr int kTablesMinBlocks = CJ_TABLES_MIN_BLOCKS;
+constexpr int kEmitMinBlocks = CJ_EMIT_MIN_BLOCKS;
 // emit staging, per warp: positions and bracket records of the steps since the
 // last flush (a step whose counts exceed them is written directly)
 constexpr int kPosStage = 512;
 constexpr int kBrkStage = 256;
+
 // Bits of a region table's `st` that the table algebra ignores (it reads bits
 // 0-3 only): the region's wflip, and which of its steps have stored masks.
 constexpr int kTabFlipBit = 4;
@@ -176,6 +197,14 @@ struct StrideWalk {
     __device__ __forceinline__ uint32_t region(uint32_t c) const { return c; }
 };
 
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+#ifndef CJ_EMU
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+#else
+    (void)p;
+#endif
+}
+
 __device__ __forceinline__ void stream_load(Stream& st) {
     const uint4* p = reinterpret_cast<const uint4*>(st.src + (size_t)st.j * kStepBytes);
     st.a = __ldcg(p);
@@ -198,14 +227,9 @@ __device__ __forceinline__ void stream_enter(const ScanParams& P, Stream& st, ui
     st.n = (g.len + kStepBytes - 1) / kStepBytes;
     st.src = g.base + g.off + lane * kBytesPerThread;
     stream_load(st);
-}
-
-__device__ __forceinline__ void prefetch_l2(const void* p) {
-#ifndef CJ_EMU
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-#else
-    (void)p;
-#endif
+#pragma unroll
+    for (int k = 1; k < kL2Ahead; k++)
+        if (k < st.n) prefetch_l2(st.src + (size_t)k * kStepBytes);
 }
 
 // take the next step (lo, hi), load the one after it, and ask for the one
@@ -219,7 +243,7 @@ __device__ __forceinline__ void stream_take(const ScanParams& P, Stream& st, uin
     if (st.c == kNoRegion) return;
     if (++st.j < st.n) {
         stream_load(st);
-        if (st.j + 1 < st.n) prefetch_l2(st.src + (size_t)(st.j + 1) * kStepBytes);
+        if (st.j + kL2Ahead - 1 < st.n) prefetch_l2(st.src + (size_t)(st.j + kL2Ahead - 1) * kStepBytes);
     } else {
         stream_enter<R>(P, st, walk.next(st.c), lane, walk);
     }
@@ -412,7 +436,7 @@ __device__ __forceinline__ void region_table(const ScanParams& P, const Region& 
 }
 
 template <bool LINES, int R>
-__global__ void __launch_bounds__(kThreads, 4) scan_tables(ScanParams P)
+__global__ void __launch_bounds__(kThreads, kTablesMinBlocks) scan_tables(ScanParams P)
 {
     const int lane = threadIdx.x & 31;
     const uint32_t lt = lanemask_lt();
@@ -776,7 +800,7 @@ __device__ __forceinline__ void emit_region(const ScanParams& P, const Region& g
 }
 
 template <int R>
-__global__ void __launch_bounds__(kThreads, 4) scan_emit(ScanParams P)
+__global__ void __launch_bounds__(kThreads, kEmitMinBlocks) scan_emit(ScanParams P)
 {
     __shared__ EmitStage s_stage[kWarpsPerBlock];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;

@@ -117,7 +117,13 @@ void      cj_result_free(cj_result* res);
 
 /* One-shot parse into a caller-provided host buffer (pinned for full speed)
  * of `out_cap` int32 entries, in the layout above; needs 2*(S+2) entries.
- * `lines_mode` != 0 treats the input as one JSON-Lines chunk. */
+ * `lines_mode` != 0 treats the input as one JSON-Lines chunk.  (Replaces
+ * parse_standard_json's H2D, stages and D2H, cujson/parse_standard_json.cu:
+ * 1584-1687, into memory the caller owns.)  With pinned input and output and
+ * an input of at least two streaming waves (cj_tuning.stream_wave_mib, 128 MiB
+ * by default) the parse is streamed: the input's copy, the scan in waves and
+ * the copy of each wave's positions back overlap, and the pair row follows
+ * the pairing.  On a non-OK status host_out may hold part of a result. */
 cj_status cj_parse_into(cj_context* ctx, const uint8_t* host_data, size_t size, int lines_mode,
                         int32_t* host_out, size_t out_cap, cj_parse_info* info);
 
@@ -251,8 +257,6 @@ typedef struct cj_tuning {
     int32_t emit_blocks_per_sm;  /* emit kernels (0: as many as fit) */
     int32_t pair_blocks;         /* pairing grid (0: sized to the bracket count) */
     int32_t pair_threads;        /* pairing threads per block: 64, 128 or 256 (0: 256) */
-    int32_t wave_mib;            /* staged runs scan in waves of this many MiB of input, so a
-                                    wave's mask words are still in L2 for its emit (0: one scan) */
     int32_t stream_wave_mib;     /* cj_parse_into of >= 2 waves of pinned input into pinned
                                     output: waves of this many MiB whose positions are copied
                                     back while later input arrives (0: 128; -1: not streamed) */
