@@ -130,7 +130,7 @@ struct cj_context {
     uint32_t wave_regions = 0;
     uint32_t n_waves = 0;
     DevBuf<uint4> wave_carry;
-    DevBuf<uint32_t> wave_nwork;
+    DevBuf<uint32_t> wave_nwork;        // per wave: work items, table and emit tickets
     uint4* h_wave = nullptr;
     uint4* d_h_wave = nullptr;          // h_wave as the device addresses it
     size_t h_wave_cap = 0;
@@ -393,7 +393,7 @@ cj_status enqueue(cj_context* ctx, bool graph)
     if (ctx->n_waves > 1) {
         // waves: each scans its regions from the previous wave's end value,
         // with its own work list (work items of wave w start at 2 * r_begin)
-        CJ_CUDA(cudaMemsetAsync(ctx->wave_nwork.p, 0, ctx->n_waves * sizeof(uint32_t), ctx->stream));
+        CJ_CUDA(cudaMemsetAsync(ctx->wave_nwork.p, 0, 3 * ctx->n_waves * sizeof(uint32_t), ctx->stream));
         for (uint32_t w = 0; w < ctx->n_waves; w++) {
             ScanParams wp = sp;
             wp.r_begin = w * ctx->wave_regions;
@@ -401,7 +401,8 @@ cj_status enqueue(cj_context* ctx, bool graph)
             wp.carry_in = w ? ctx->wave_carry.p + (w - 1) : nullptr;
             wp.carry_out = ctx->wave_carry.p + w;
             wp.carry_host = ctx->wave_stream ? ctx->d_h_wave + w : nullptr;
-            wp.n_work = ctx->wave_nwork.p + w;
+            wp.n_work = ctx->wave_nwork.p + 3 * w;
+            wp.tickets = ctx->wave_nwork.p + 3 * w + 1;
             wp.work = ctx->work.p + 2 * (size_t)wp.r_begin;
             launch_scan(wp, ctx->lines, shape, ctx->stream, ev ? ev + 1 : nullptr);
             ctx->launches += scan_launches(wp.r_end - wp.r_begin);
@@ -526,7 +527,7 @@ cj_status prepare_waves(cj_context* ctx, uint64_t wave_bytes)
     const uint32_t nw = (uint32_t)((ctx->n_regions + (uint64_t)ctx->wave_regions - 1) / ctx->wave_regions);
     cj_status st;
     if ((st = ensure(ctx, ctx->wave_carry, nw))) return st;
-    if ((st = ensure(ctx, ctx->wave_nwork, nw))) return st;
+    if ((st = ensure(ctx, ctx->wave_nwork, 3 * (size_t)nw))) return st;
     ctx->n_waves = nw;
     ctx->wave_stream = true;
     if (ctx->h_wave_cap < nw) {

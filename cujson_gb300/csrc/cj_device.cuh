@@ -69,8 +69,9 @@ struct Ctrl {
     uint32_t k_total;
     int32_t  neg_min_level;   // max(-level) over brackets; > 0 means a close below depth 0
     int32_t  max_depth;
-    uint32_t n_regions_done;
     uint32_t gave_up;         // the first bounded wait that expired (kGave* codes), 0 if none
+    uint32_t tables_ticket;   // regions drawn by the table kernel's warps after their first
+    uint32_t emit_ticket;     // work items drawn by the emit kernel's warps after their first
 };
 
 // where a bounded wait gave up (Ctrl::gave_up)

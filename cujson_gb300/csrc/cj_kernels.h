@@ -48,6 +48,9 @@ struct ScanParams {
     uint4* carry_out;
     uint4* carry_host;
     uint32_t* n_work;
+    // the table and emit kernels' ticket counters, zero at launch (nullptr:
+    // ctrl->tables_ticket and ctrl->emit_ticket); a wave has its own pair
+    uint32_t* tickets;
 };
 
 // Launch shape of the scan kernels (0 = as many blocks as fit).

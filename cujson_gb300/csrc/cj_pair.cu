@@ -53,6 +53,11 @@ __device__ __forceinline__ uint32_t lanemask_gt() {
 #endif
 }
 
+// pair_spine: chunks after an open's own that are checked directly, and the
+// count of far matches in a round above which each lane walks its own
+constexpr int kSpineWindow = 4;
+constexpr int kSpineWarpMax = 8;
+
 __device__ __forceinline__ unsigned long long tree_pack(uint32_t epoch, int32_t level) {
     return ((unsigned long long)epoch << 32) | (uint32_t)(0x7FFFFFFF - level);
 }
@@ -91,6 +96,36 @@ __device__ int64_t next_le(const PairParams& P, uint64_t nch, uint64_t c, int32_
         for (; i < gend; i++)
             if (tree_value(P, lvl, i) <= d) break;
         if (i >= gend) return -1;   // inconsistent tree (only on a timeout path)
+    }
+    return (int64_t)i;
+}
+
+// The same search by the whole warp (every lane gets the result): each level's
+// group of 32 entries is read at once, one lane per entry, and a ballot finds
+// the first that qualifies -- one dependent load per level instead of up to 32.
+__device__ int64_t next_le_warp(const PairParams& P, uint64_t nch, uint64_t c, int32_t d, int lane) {
+    uint64_t size[kTreeLevels + 1];
+    size[0] = nch;
+    for (int l = 1; l <= kTreeLevels; l++) size[l] = (size[l - 1] + 31) / 32;
+    uint64_t i = c + 1;
+    int lvl = 0;
+    while (true) {
+        if (i >= size[lvl]) return -1;
+        const uint64_t g0 = i & ~31ull, j = g0 + (uint64_t)lane;
+        const bool ok = j >= i && j < size[lvl] && tree_value(P, lvl, j) <= d;
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, ok);
+        if (m) { i = g0 + (uint64_t)(__ffs(m) - 1); break; }
+        if (lvl == kTreeLevels) return -1;
+        i = (g0 >> 5) + 1;
+        lvl++;
+    }
+    while (lvl > 0) {
+        lvl--;
+        const uint64_t g0 = i * 32, j = g0 + (uint64_t)lane;
+        const bool ok = j < size[lvl] && tree_value(P, lvl, j) <= d;
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, ok);
+        if (!m) return -1;          // inconsistent tree (only on a timeout path)
+        i = g0 + (uint64_t)(__ffs(m) - 1);
     }
     return (int64_t)i;
 }
@@ -276,22 +311,54 @@ __global__ void __launch_bounds__(256) pair_spine(PairParams P)
         const int4 ci = __ldcg(&P.cinfo[c]);
         const int32_t n_uo = ci.z - ci.y;          // opens still open at chunk end
         const int32_t n_uc = ci.x - ci.y;          // closes unmatched inside the chunk
+        // the matching close of the open at level d (structural ox) is the
+        // unmatched close at level d of chunk c2
+        auto resolve = [&](int64_t c2, int32_t d, uint32_t ox) {
+            if (c2 < 0 || (uint64_t)c2 >= c_end) { err |= CJ_FLAG_BRACKETS; return; }   // none, or past the document
+            const int4 cj2 = __ldcg(&P.cinfo[c2]);
+            const int32_t idx = cj2.x - 1 - d;
+            if (idx < 0 || idx >= kChunk || idx >= cj2.x - cj2.y) { err |= CJ_FLAG_BRACKETS; return; }
+            const uint32_t cx = __ldcg(P.spine + (uint64_t)c2 * kChunk + idx);
+            if ((ox ^ cx) & kCurly) err |= CJ_FLAG_BRACKETS;
+            if ((ox & ~kCurly) >= S || (cx & ~kCurly) >= S) { err |= CJ_FLAG_BRACKETS; return; }
+            pair[ox & ~kCurly] = (int32_t)((cx & ~kCurly) + 1u);
+        };
         if (n_uo < 0 || n_uc < 0 || n_uo + n_uc > kChunk) {
             err = CJ_FLAG_BRACKETS;
         } else {
-            for (int32_t i = lane; i < n_uo; i += 32) {
+            for (int32_t base = 0; base < n_uo; base += 32) {
+                // one open per lane: most match in one of the next few chunks,
+                // read together
+                const int32_t i = base + lane;
+                const bool valid = i < n_uo;
                 const int32_t d = ci.y + i;
-                const uint32_t ox = __ldcg(P.spine + c * kChunk + (kChunk - 1 - i));
-                const int64_t c2 = next_le(P, nch, c, d);
-                if (c2 < 0) { err |= CJ_FLAG_BRACKETS; continue; }
-                if ((uint64_t)c2 >= c_end) { err |= CJ_FLAG_BRACKETS; continue; }   // past the document
-                const int4 cj2 = __ldcg(&P.cinfo[c2]);
-                const int32_t idx = cj2.x - 1 - d;
-                if (idx < 0 || idx >= kChunk || idx >= cj2.x - cj2.y) { err |= CJ_FLAG_BRACKETS; continue; }
-                const uint32_t cx = __ldcg(P.spine + (uint64_t)c2 * kChunk + idx);
-                if ((ox ^ cx) & kCurly) err |= CJ_FLAG_BRACKETS;
-                if ((ox & ~kCurly) >= S || (cx & ~kCurly) >= S) { err |= CJ_FLAG_BRACKETS; continue; }
-                pair[ox & ~kCurly] = (int32_t)((cx & ~kCurly) + 1u);
+                const uint32_t ox = valid ? __ldcg(P.spine + c * kChunk + (kChunk - 1 - i)) : 0u;
+                int64_t c2 = -1;
+                if (valid) {
+                    int32_t v[kSpineWindow];
+#pragma unroll
+                    for (int k = 0; k < kSpineWindow; k++)
+                        v[k] = (c + 1 + k < nch) ? __ldcg(&P.cinfo[c + 1 + k].y) : INT_MAX;
+#pragma unroll
+                    for (int k = kSpineWindow - 1; k >= 0; k--)
+                        if (v[k] <= d) c2 = (int64_t)(c + 1 + k);
+                }
+                const bool far = valid && c2 < 0 && c + 1 + kSpineWindow < nch;
+                if (valid && !far) resolve(c2, d, ox);
+                uint32_t pend = __ballot_sync(0xFFFFFFFFu, far);
+                if (__popc(pend) >= kSpineWarpMax) {
+                    // many far matches (deep nesting): a walk per lane
+                    if (far) resolve(next_le(P, nch, c, d), d, ox);
+                } else {
+                    // a few: the warp walks the min-tree for each in turn
+                    while (pend) {
+                        const int src = __ffs(pend) - 1;
+                        pend &= pend - 1u;
+                        const int32_t ds = __shfl_sync(0xFFFFFFFFu, d, src);
+                        const int64_t c2w = next_le_warp(P, nch, c, ds, lane);
+                        if (lane == src) resolve(c2w, d, ox);
+                    }
+                }
             }
         }
         err = __reduce_or_sync(0xFFFFFFFFu, err);

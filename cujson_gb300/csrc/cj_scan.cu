@@ -10,7 +10,7 @@
 //                 of the 4 entry states (escape pending, inside a string): the
 //                 exit state, structural count, bracket count and depth delta.
 //   prefix_reduce (256 regions per block, one per thread) composes each
-//                 block's tables (only when there is more than one block).
+//                 block's tables (only when there are more than 64 blocks).
 //   prefix_apply  (the same blocks) composes the blocks before its own, the
 //                 warps (chunks of 32 regions) before each warp and the regions
 //                 before each region, and writes the segment ends, the totals,
@@ -60,7 +60,7 @@ constexpr uint32_t kInputWaitLimit = 1u << 22; // polls (>= 256 ns each) for inp
 // how many steps ahead of the current one the table kernel asks for a step to
 // be brought into L2 (the register load is one step ahead)
 #ifndef CJ_L2_AHEAD
-#define CJ_L2_AHEAD 2
+#define CJ_L2_AHEAD 4
 #endif
 constexpr int kL2Ahead = CJ_L2_AHEAD;
 // resident blocks per SM the table and emit kernels are compiled for (their
@@ -185,16 +185,27 @@ constexpr uint32_t kNoRegion = 0xFFFFFFFFu;
 
 struct Stream {
     uint4 a, b;            // the lane's 32 bytes of the next step
-    uint32_t c;            // cursor of the region of the next step (kNoRegion: none)
+    uint32_t c;            // the region of the next step (kNoRegion: none)
+    uint32_t ahead;        // lane 0: the ticket drawn for the region after it
     int j, n;              // that step's number in its region, the region's step count
     const uint8_t* src;    // the lane's bytes of step 0 of that region
 };
 
-// every nw-th region from the warp's first
-struct StrideWalk {
-    uint32_t nw, n;
-    __device__ __forceinline__ uint32_t next(uint32_t c) const { return (c + nw < n && c + nw > c) ? c + nw : kNoRegion; }
-    __device__ __forceinline__ uint32_t region(uint32_t c) const { return c; }
+// Regions after each warp's first come from a ticket counter, so a warp that
+// drew quiet regions (backslash runs) takes more of them while another works
+// through dense ones.  Each warp draws its next ticket as it enters a region
+// and reads it only when the region is done, so the atomic's latency is hidden
+// behind a whole region.
+struct TicketWalk {
+    uint32_t* ticket;      // tickets drawn so far
+    uint32_t base, n;      // ticket t is region base + t, below n
+    // lane 0's ticket (the other lanes get 0)
+    __device__ __forceinline__ uint32_t draw(int lane) const { return lane == 0 ? atomicAdd(ticket, 1u) : 0u; }
+    // the region of lane 0's ticket, in every lane
+    __device__ __forceinline__ uint32_t region(uint32_t drawn) const {
+        const uint32_t t = __shfl_sync(FULL, drawn, 0);
+        return (t < n - min(n, base)) ? base + t : kNoRegion;
+    }
 };
 
 __device__ __forceinline__ void prefetch_l2(const void* p) {
@@ -221,8 +232,9 @@ __device__ __forceinline__ void stream_enter(const ScanParams& P, Stream& st, ui
     st.j = 0;
     st.n = 0;
     if (c == kNoRegion) return;
+    st.ahead = walk.draw(lane);
     Region g;
-    region_of(P, walk.region(c), R * kStepBytes, g);
+    region_of(P, c, R * kStepBytes, g);
     if (P.ready && !__shfl_sync(FULL, lane == 0 ? wait_input(P, g) : true, 0)) { st.c = kNoRegion; return; }
     st.n = (g.len + kStepBytes - 1) / kStepBytes;
     st.src = g.base + g.off + lane * kBytesPerThread;
@@ -245,7 +257,7 @@ __device__ __forceinline__ void stream_take(const ScanParams& P, Stream& st, uin
         stream_load(st);
         if (st.j + kL2Ahead - 1 < st.n) prefetch_l2(st.src + (size_t)(st.j + kL2Ahead - 1) * kStepBytes);
     } else {
-        stream_enter<R>(P, st, walk.next(st.c), lane, walk);
+        stream_enter<R>(P, st, walk.region(st.ahead), lane, walk);
     }
 }
 
@@ -262,43 +274,6 @@ __device__ __forceinline__ void load_tab(const uint4* p, Ent t[4]) {
 __device__ __forceinline__ void store_tab(uint4* p, const Ent t[4]) {
 #pragma unroll
     for (int s = 0; s < 4; s++) p[s] = make_uint4(t[s].st, t[s].s, t[s].k, (uint32_t)t[s].d);
-}
-
-__device__ __forceinline__ void shfl_tab(const Ent t[4], Ent u[4], int src_delta, bool up) {
-#pragma unroll
-    for (int s = 0; s < 4; s++) {
-        if (up) {
-            u[s].st = __shfl_up_sync(FULL, t[s].st, src_delta);
-            u[s].s = __shfl_up_sync(FULL, t[s].s, src_delta);
-            u[s].k = __shfl_up_sync(FULL, t[s].k, src_delta);
-            u[s].d = __shfl_up_sync(FULL, t[s].d, src_delta);
-        } else {
-            u[s].st = __shfl_down_sync(FULL, t[s].st, src_delta);
-            u[s].s = __shfl_down_sync(FULL, t[s].s, src_delta);
-            u[s].k = __shfl_down_sync(FULL, t[s].k, src_delta);
-            u[s].d = __shfl_down_sync(FULL, t[s].d, src_delta);
-        }
-    }
-}
-
-// inclusive scan of tables over the lanes of a warp, in lane order
-__device__ __forceinline__ void warp_scan_tab(Ent t[4], int lane) {
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        Ent u[4];
-        shfl_tab(t, u, o, true);
-        if (lane >= o) tab_compose(u, t, t);
-    }
-}
-
-// composition of the 32 lanes' tables in lane order, in lane 0
-__device__ __forceinline__ void warp_reduce_tab(Ent t[4], int lane) {
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        Ent u[4];
-        shfl_tab(t, u, o, false);
-        if ((lane & (2 * o - 1)) == 0 && lane + o < 32) tab_compose(t, u, t);
-    }
 }
 
 // ---- scan_tables --------------------------------------------------------------
@@ -444,10 +419,11 @@ __global__ void __launch_bounds__(kThreads, kTablesMinBlocks) scan_tables(ScanPa
     const uint32_t n = P.r_end;
     const uint32_t first = P.r_begin + blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
     if (first >= n) return;
-    const StrideWalk walk{nw, n};
+    const TicketWalk walk{P.tickets ? P.tickets : &P.ctrl->tables_ticket, P.r_begin + nw, n};
     Stream st;
     stream_enter<R>(P, st, first, lane, walk);
-    for (uint32_t r = first; r < n; r += nw) {
+    // the stream holds the next region's first step when a region's table is done
+    for (uint32_t r = first; r != kNoRegion; r = st.c) {
         if (P.ready && aborted(P.ctrl)) break;     // the wait for input bytes gave up
         Region g;
         region_of(P, r, R * kStepBytes, g);
@@ -463,128 +439,282 @@ __global__ void __launch_bounds__(kThreads, kTablesMinBlocks) scan_tables(ScanPa
 // every SM.
 
 constexpr int kPrefixWarps = kPrefixPerBlock / 32;
+// scans of at most this many prefix blocks skip prefix_reduce: each block
+// composes the tables of the regions before it directly (at most 63 per thread)
+#ifndef CJ_DIRECT_PREFIX_BLOCKS
+#define CJ_DIRECT_PREFIX_BLOCKS 64
+#endif
+constexpr int kDirectPrefixBlocks = CJ_DIRECT_PREFIX_BLOCKS;
+
+// ---- state-first prefix ------------------------------------------------------------
+// Applying tables one after another, the string/escape state follows from the
+// tables' state maps alone (4 entries of 2 bits: one byte), and once each
+// table's entry state is known its counts are a plain prefix sum (restarted
+// by the reset bits).  So the prefix is two cheap scans -- of state maps, then
+// of the counts each table gives for its entry state -- instead of a scan of
+// whole 4-entry tables.
+
+constexpr uint32_t kMapIdentity = 0xE4u;     // state s -> s
+
+__device__ __forceinline__ uint32_t map_of(const Ent t[4]) {
+    return (t[0].st & 3u) | ((t[1].st & 3u) << 2) | ((t[2].st & 3u) << 4) | ((t[3].st & 3u) << 6);
+}
+__device__ __forceinline__ uint32_t map_at(uint32_t m, uint32_t s) { return (m >> (2u * s)) & 3u; }
+// map a, then map b
+__device__ __forceinline__ uint32_t map_then(uint32_t a, uint32_t b) {
+    return map_at(b, a & 3u) | (map_at(b, (a >> 2) & 3u) << 2) | (map_at(b, (a >> 4) & 3u) << 4) |
+           (map_at(b, (a >> 6) & 3u) << 6);
+}
+
+// counts added by a run of tables, and whether the run restarts them
+struct Sums {
+    uint32_t s, k;
+    int32_t d;
+    uint32_t f;            // kResetState | kResetCounts seen in the run
+};
+__device__ __forceinline__ Sums sums_zero() { Sums z; z.s = 0; z.k = 0; z.d = 0; z.f = 0; return z; }
+__device__ __forceinline__ Sums sums_of(const Ent& x) {
+    Sums r; r.s = x.s; r.k = x.k; r.d = x.d; r.f = x.st & (kResetState | kResetCounts); return r;
+}
+// run a, then run b
+__device__ __forceinline__ Sums sums_then(const Sums& a, const Sums& b) {
+    Sums r;
+    r.s = (b.f & kResetCounts) ? b.s : a.s + b.s;
+    r.k = (b.f & kResetCounts) ? b.k : a.k + b.k;
+    r.d = (b.f & kResetState) ? b.d : a.d + b.d;
+    r.f = a.f | b.f;
+    return r;
+}
+__device__ __forceinline__ Sums shfl_up_sums(const Sums& a, int o) {
+    Sums r;
+    r.s = __shfl_up_sync(FULL, a.s, o);
+    r.k = __shfl_up_sync(FULL, a.k, o);
+    r.d = __shfl_up_sync(FULL, a.d, o);
+    r.f = __shfl_up_sync(FULL, a.f, o);
+    return r;
+}
+// value v, then a run with sums p ending in state st
+__device__ __forceinline__ Ent apply_sums(const Ent& v, const Sums& p, uint32_t st) {
+    Ent r;
+    r.st = st;
+    r.s = (p.f & kResetCounts) ? p.s : v.s + p.s;
+    r.k = (p.f & kResetCounts) ? p.k : v.k + p.k;
+    r.d = (p.f & kResetState) ? p.d : v.d + p.d;
+    return r;
+}
+
+// Exclusive scans over the block's threads, in thread order: state maps
+// (identity before the first) and sums (zero before the first).  `m_ex` and
+// `p_ex` are the thread's prefixes; the block's totals go to *m_tot / *p_tot
+// when given.  Three __syncthreads; every thread of the block calls it.
+__device__ __forceinline__ void block_scan_maps(uint32_t m, uint32_t* sm, int lane, int warp, uint32_t& m_ex,
+                                                uint32_t* m_tot) {
+    uint32_t mi = m;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULL, mi, o);
+        if (lane >= o) mi = map_then(y, mi);
+    }
+    uint32_t mx = __shfl_up_sync(FULL, mi, 1);
+    if (lane == 0) mx = kMapIdentity;
+    if (lane == 31) sm[warp] = mi;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t c = lane < kPrefixWarps ? sm[lane] : kMapIdentity;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, c, o);
+            if (lane >= o) c = map_then(y, c);
+        }
+        uint32_t cx = __shfl_up_sync(FULL, c, 1);
+        if (lane == 0) cx = kMapIdentity;
+        const uint32_t tot = __shfl_sync(FULL, c, 31);
+        __syncwarp();
+        if (lane < kPrefixWarps) sm[lane] = cx;
+        if (lane == 0) sm[kPrefixWarps] = tot;
+    }
+    __syncthreads();
+    m_ex = map_then(sm[warp], mx);
+    if (m_tot) *m_tot = sm[kPrefixWarps];
+    __syncthreads();
+}
+
+__device__ __forceinline__ void block_scan_sums(const Sums& v, Sums* sm, int lane, int warp, Sums& p_ex,
+                                                Sums* p_tot) {
+    Sums si = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const Sums y = shfl_up_sums(si, o);
+        if (lane >= o) si = sums_then(y, si);
+    }
+    Sums sx = shfl_up_sums(si, 1);
+    if (lane == 0) sx = sums_zero();
+    if (lane == 31) sm[warp] = si;
+    __syncthreads();
+    if (warp == 0) {
+        Sums c = lane < kPrefixWarps ? sm[lane] : sums_zero();
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const Sums y = shfl_up_sums(c, o);
+            if (lane >= o) c = sums_then(y, c);
+        }
+        Sums cx = shfl_up_sums(c, 1);
+        if (lane == 0) cx = sums_zero();
+        Sums tot;
+        tot.s = __shfl_sync(FULL, c.s, 31);
+        tot.k = __shfl_sync(FULL, c.k, 31);
+        tot.d = __shfl_sync(FULL, c.d, 31);
+        tot.f = __shfl_sync(FULL, c.f, 31);
+        __syncwarp();
+        if (lane < kPrefixWarps) sm[lane] = cx;
+        if (lane == 0) sm[kPrefixWarps] = tot;
+    }
+    __syncthreads();
+    p_ex = sums_then(sm[warp], sx);
+    if (p_tot) *p_tot = sm[kPrefixWarps];
+    __syncthreads();
+}
 
 // Block b: the composition of its regions' tables.
 __global__ void __launch_bounds__(kPrefixPerBlock) prefix_reduce(ScanParams P)
 {
-    __shared__ Ent s_w[kPrefixWarps][4];
+    __shared__ uint32_t s_map[kPrefixWarps + 1];
+    __shared__ Sums s_w[kPrefixWarps][4];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t r = P.r_begin + blockIdx.x * (uint32_t)kPrefixPerBlock + threadIdx.x;
+    const bool in_range = r < P.r_end;
     Ent t[4];
-    if (r < P.r_end) load_tab(P.rtab + (size_t)r * 4, t);
+    if (in_range) load_tab(P.rtab + (size_t)r * 4, t);
     else tab_identity(t);
-    warp_reduce_tab(t, lane);
+    // the state each region is entered in, for each entry state of the block;
+    // then the counts summed for each
+    uint32_t m_ex, m_tot;
+    block_scan_maps(map_of(t), s_map, lane, warp, m_ex, &m_tot);
+    Sums a[4];
+#pragma unroll
+    for (uint32_t s0 = 0; s0 < 4; s0++) a[s0] = in_range ? sums_of(ent_select(t, map_at(m_ex, s0))) : sums_zero();
+    // reductions in thread order: lane L takes lane L+o's run after its own
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+        for (int s0 = 0; s0 < 4; s0++) {
+            Sums y;
+            y.s = __shfl_down_sync(FULL, a[s0].s, o);
+            y.k = __shfl_down_sync(FULL, a[s0].k, o);
+            y.d = __shfl_down_sync(FULL, a[s0].d, o);
+            y.f = __shfl_down_sync(FULL, a[s0].f, o);
+            if (lane + o < 32) a[s0] = sums_then(a[s0], y);
+        }
+    }
     if (lane == 0) {
 #pragma unroll
-        for (int k = 0; k < 4; k++) s_w[warp][k] = t[k];
+        for (int s0 = 0; s0 < 4; s0++) s_w[warp][s0] = a[s0];
     }
     __syncthreads();
     if (warp == 0) {
-        if (lane < kPrefixWarps) {
 #pragma unroll
-            for (int k = 0; k < 4; k++) t[k] = s_w[lane][k];
-        } else {
-            tab_identity(t);
+        for (int s0 = 0; s0 < 4; s0++) a[s0] = lane < kPrefixWarps ? s_w[lane][s0] : sums_zero();
+#pragma unroll
+        for (int o = 1; o < kPrefixWarps; o <<= 1) {
+#pragma unroll
+            for (int s0 = 0; s0 < 4; s0++) {
+                Sums y;
+                y.s = __shfl_down_sync(FULL, a[s0].s, o);
+                y.k = __shfl_down_sync(FULL, a[s0].k, o);
+                y.d = __shfl_down_sync(FULL, a[s0].d, o);
+                y.f = __shfl_down_sync(FULL, a[s0].f, o);
+                if (lane + o < 32) a[s0] = sums_then(a[s0], y);
+            }
         }
-        warp_reduce_tab(t, lane);
-        if (lane == 0) store_tab(P.bagg + (size_t)blockIdx.x * 4, t);
+        if (lane == 0) {
+            // the block's table: for each entry state, exit state (with the
+            // reset bits seen) and the counts
+            Ent agg[4];
+#pragma unroll
+            for (uint32_t s0 = 0; s0 < 4; s0++) {
+                agg[s0].st = map_at(m_tot, s0) | a[s0].f;
+                agg[s0].s = a[s0].s;
+                agg[s0].k = a[s0].k;
+                agg[s0].d = a[s0].d;
+            }
+            store_tab(P.bagg + (size_t)blockIdx.x * 4, agg);
+        }
     }
 }
 
 // Block b: entry values, segment ends, totals and the emit work list.
 __global__ void __launch_bounds__(kPrefixPerBlock) prefix_apply(ScanParams P)
 {
-    __shared__ Ent s_chunk[kPrefixWarps][4];   // per warp: a partial, its total, then its exclusive prefix
-    __shared__ Ent s_base;                     // the value before the block
+    __shared__ uint32_t s_map[kPrefixWarps + 1];
+    __shared__ Sums s_sum[kPrefixWarps + 1];
     __shared__ uint32_t s_cnt[kPrefixWarps];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (aborted(P.ctrl)) return;          // a timed-out run writes no outputs
     const uint32_t n = P.n_regions;
     const uint32_t b = blockIdx.x;
 
-    // the blocks before this one: every thread composes a run of them
-    {
-        const uint32_t q = (b + kPrefixPerBlock - 1) / kPrefixPerBlock;
-        Ent t[4];
-        tab_identity(t);
-        const uint32_t lo = threadIdx.x * q, hi = min(b, lo + q);
+    // the value before the scan
+    Ent v0 = ent_identity(0);
+    if (P.carry_in) {
+        const uint4 c = __ldcg(P.carry_in);
+        v0.st = c.x; v0.s = c.y; v0.k = c.z; v0.d = (int32_t)c.w;
+    }
+    // the value before this block: every thread takes a run of the units
+    // before it -- the blocks' aggregates, or, for a scan of at most
+    // kDirectPrefixBlocks blocks (no prefix_reduce launch), the regions' own
+    // tables -- first for its state map, then, once the state at the run's
+    // start is known, for its sums
+    Ent vb = v0;
+    if (b > 0) {
+        const bool direct = gridDim.x <= (uint32_t)kDirectPrefixBlocks;
+        const uint32_t units = direct ? b * (uint32_t)kPrefixPerBlock : b;
+        const uint4* src = direct ? P.rtab + (size_t)P.r_begin * 4 : P.bagg;
+        const uint32_t q = (units + kPrefixPerBlock - 1) / kPrefixPerBlock;
+        const uint32_t lo = min(units, threadIdx.x * q), hi = min(units, lo + q);
+        uint32_t m = kMapIdentity;
         for (uint32_t i = lo; i < hi; i++) {
+            const uint4* u = src + (size_t)i * 4;
+            const uint32_t um = (__ldcg(&u[0].x) & 3u) | ((__ldcg(&u[1].x) & 3u) << 2) |
+                                ((__ldcg(&u[2].x) & 3u) << 4) | ((__ldcg(&u[3].x) & 3u) << 6);
+            m = map_then(m, um);
+        }
+        uint32_t m_ex, m_tot;
+        block_scan_maps(m, s_map, lane, warp, m_ex, &m_tot);
+        uint32_t e = map_at(m_ex, v0.st & 3u);
+        Sums run = sums_zero();
+        for (uint32_t i = lo; i < hi; i++) {
+            // the whole table, so that no load waits for the previous state
             Ent u[4];
-            load_tab(P.bagg + (size_t)i * 4, u);
-            tab_compose(t, u, t);
+            load_tab(src + (size_t)i * 4, u);
+            const Ent xe = ent_select(u, e);
+            run = sums_then(run, sums_of(xe));
+            e = xe.st & 3u;
         }
-        warp_reduce_tab(t, lane);
-        if (lane == 0) {
-#pragma unroll
-            for (int k = 0; k < 4; k++) s_chunk[warp][k] = t[k];
-        }
-        __syncthreads();
-        if (warp == 0) {
-            if (lane < kPrefixWarps) {
-#pragma unroll
-                for (int k = 0; k < 4; k++) t[k] = s_chunk[lane][k];
-            } else {
-                tab_identity(t);
-            }
-            warp_reduce_tab(t, lane);
-            if (lane == 0) {
-                Ent v0 = ent_identity(0);
-                if (P.carry_in) {
-                    const uint4 c = __ldcg(P.carry_in);
-                    v0.st = c.x; v0.s = c.y; v0.k = c.z; v0.d = (int32_t)c.w;
-                }
-                s_base = ent_apply(v0, t);
-            }
-        }
-        __syncthreads();
+        Sums p_ex, p_tot;
+        block_scan_sums(run, s_sum, lane, warp, p_ex, &p_tot);
+        vb = apply_sums(v0, p_tot, map_at(m_tot, v0.st & 3u));
     }
 
-    // this warp's chunk: the regions before each region, and the chunk's total
+    // this block's regions: the state each is entered in, then the counts
+    // before each
     const uint32_t r = P.r_begin + b * (uint32_t)kPrefixPerBlock + threadIdx.x;
     const bool in_range = r < P.r_end;
     Ent t[4];
     if (in_range) load_tab(P.rtab + (size_t)r * 4, t);
     else tab_identity(t);
-    Ent incl[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) incl[k] = t[k];
-    warp_scan_tab(incl, lane);
-    if (lane == 31) {
-#pragma unroll
-        for (int k = 0; k < 4; k++) s_chunk[warp][k] = incl[k];
-    }
-    Ent ex[4];
-    shfl_tab(incl, ex, 1, true);
-    if (lane == 0) tab_identity(ex);
-    __syncthreads();
-    if (warp == 0) {
-        // the chunks before each chunk
-        Ent c[4];
-        if (lane < kPrefixWarps) {
-#pragma unroll
-            for (int k = 0; k < 4; k++) c[k] = s_chunk[lane][k];
-        } else {
-            tab_identity(c);
-        }
-        warp_scan_tab(c, lane);
-        Ent cx[4];
-        shfl_tab(c, cx, 1, true);
-        if (lane == 0) tab_identity(cx);
-        __syncwarp();
-        if (lane < kPrefixWarps) {
-#pragma unroll
-            for (int k = 0; k < 4; k++) s_chunk[lane][k] = cx[k];
-        }
-    }
-    __syncthreads();
-    const Ent v = ent_apply(ent_apply(s_base, s_chunk[warp]), ex);
+    uint32_t m_ex;
+    block_scan_maps(map_of(t), s_map, lane, warp, m_ex, nullptr);
+    const uint32_t e_state = map_at(m_ex, vb.st & 3u);
+    const Ent x = ent_select(t, e_state);
+    Sums p_ex;
+    block_scan_sums(in_range ? sums_of(x) : sums_zero(), s_sum, lane, warp, p_ex, nullptr);
+    const Ent v = apply_sums(vb, p_ex, e_state);
 
     bool work = false;
     Ent e = v, nv = v;
     uint32_t steps_flip = 0;
     if (in_range) {
         const uint32_t raw = t[0].st;           // the region's own table: wflip, stored steps
-        const Ent x = ent_select(t, v.st & 3u);
         nv = ent_apply(v, t);
         // the entry value as the region starts: a segment's first region starts
         // in state 0 at depth 0 (and at count 0 for an independent document)
@@ -807,12 +937,22 @@ __global__ void __launch_bounds__(kThreads, kEmitMinBlocks) scan_emit(ScanParams
     if (aborted(P.ctrl)) return;
     const uint32_t n = *reinterpret_cast<const volatile uint32_t*>(P.n_work ? P.n_work : &P.ctrl->n_work);
     const uint32_t nw = gridDim.x * kWarpsPerBlock;
-    for (uint32_t i = blockIdx.x * kWarpsPerBlock + warp; i < n; i += nw) {
+    uint32_t* ticket = P.tickets ? P.tickets + 1 : &P.ctrl->emit_ticket;
+    // the first item by warp number, the later ones (when there are more
+    // items than warps) from a ticket counter, drawn one item ahead, so that
+    // warps with sparse regions take more
+    const bool more = n > nw;
+    uint32_t i = blockIdx.x * kWarpsPerBlock + warp;
+    while (i < n) {
+        uint32_t t = n;
+        if (more && lane == 0) t = atomicAdd(ticket, 1u);
         const uint4 a = __ldcg(P.work + 2 * (size_t)i), b = __ldcg(P.work + 2 * (size_t)i + 1);
         Region g;
         region_of(P, a.x, R * kStepBytes, g);
         emit_region(P, g, P.masks + (size_t)a.x * R * 32 + lane, a.y & 0xFFFFu, (a.y >> 31) ? FULL : 0u, a.z, a.w,
                     (int32_t)b.x, s_stage[warp], b.y, b.z, (int32_t)b.w, lane);
+        t = __shfl_sync(FULL, t, 0);
+        i = (t < n) ? nw + t : n;
     }
 }
 
@@ -824,14 +964,14 @@ void launch_r(const ScanParams& p, bool lines, int tables_grid, int emit_grid, c
 #ifdef CJ_EMU
     (void)stream; (void)ev;
     cj_emu::launch(tables_grid, kThreads, 0, [&] { if (lines) scan_tables<true, R>(p); else scan_tables<false, R>(p); });
-    if (nb > 1) cj_emu::launch(nb, kPrefixPerBlock, 0, [&] { prefix_reduce(p); });
+    if (nb > (uint32_t)kDirectPrefixBlocks) cj_emu::launch(nb, kPrefixPerBlock, 0, [&] { prefix_reduce(p); });
     cj_emu::launch(nb, kPrefixPerBlock, 0, [&] { prefix_apply(p); });
     cj_emu::launch(emit_grid, kThreads, 0, [&] { scan_emit<R>(p); });
 #else
     if (lines) scan_tables<true, R><<<tables_grid, kThreads, 0, stream>>>(p);
     else scan_tables<false, R><<<tables_grid, kThreads, 0, stream>>>(p);
     if (ev) cudaEventRecord(ev[0], stream);
-    if (nb > 1) prefix_reduce<<<nb, kPrefixPerBlock, 0, stream>>>(p);
+    if (nb > (uint32_t)kDirectPrefixBlocks) prefix_reduce<<<nb, kPrefixPerBlock, 0, stream>>>(p);
     prefix_apply<<<nb, kPrefixPerBlock, 0, stream>>>(p);
     if (ev) cudaEventRecord(ev[1], stream);
     scan_emit<R><<<emit_grid, kThreads, 0, stream>>>(p);
@@ -882,7 +1022,7 @@ cudaError_t preload_scan_kernels()
 int scan_launches(uint32_t n_regions)
 {
     if (n_regions == 0) return 0;
-    return n_regions > (uint32_t)kPrefixPerBlock ? 4 : 3;
+    return n_regions > (uint32_t)kPrefixPerBlock * kDirectPrefixBlocks ? 4 : 3;
 }
 
 void launch_scan(const ScanParams& p0, bool lines, const ScanShape& shape, cudaStream_t stream, cudaEvent_t* ev)

@@ -20,26 +20,37 @@ FLAGS = ["-O1", "-g", "-std=c++17", "-fPIC", "-w", "-DCJ_EMU=1", f"-I{HERE / 'sh
          f"-I{ROOT / 'include'}", "-include", str(HERE / "cj_emu.h")]
 
 
-def _compile(src: Path) -> Path:
-    obj = BUILD / (src.stem + ".o")
-    cmd = ["g++", *FLAGS, "-x", "c++", "-c", str(src), "-o", str(obj)]
+# Variants of the emulation: extra defines for the kernels' sources, and the
+# library each builds.  "reduce" sends every scan of more than one prefix block
+# through prefix_reduce, which the default build uses only above 64 blocks.
+VARIANTS = {"": [], "reduce": ["-DCJ_DIRECT_PREFIX_BLOCKS=1"]}
+
+
+def _lib(variant: str) -> Path:
+    return LIB if not variant else BUILD / f"libcj_emu_{variant}.so"
+
+
+def _compile(src: Path, variant: str) -> Path:
+    obj = BUILD / (src.stem + (f"_{variant}" if variant else "") + ".o")
+    cmd = ["g++", *FLAGS, *VARIANTS[variant], "-x", "c++", "-c", str(src), "-o", str(obj)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode:
         raise RuntimeError(f"emulation build failed for {src.name}:\n{r.stderr[-4000:]}")
     return obj
 
 
-def build(force: bool = False) -> Path:
+def build(force: bool = False, variant: str = "") -> Path:
     BUILD.mkdir(exist_ok=True)
+    lib = _lib(variant)
     newest = max(p.stat().st_mtime for p in DEPS)
-    if not force and LIB.exists() and LIB.stat().st_mtime >= newest:
-        return LIB
+    if not force and lib.exists() and lib.stat().st_mtime >= newest:
+        return lib
     with ThreadPoolExecutor(3) as ex:
-        objs = list(ex.map(_compile, UNITS))
-    r = subprocess.run(["g++", "-shared", "-o", str(LIB), *map(str, objs)], capture_output=True, text=True)
+        objs = list(ex.map(lambda u: _compile(u, variant), UNITS))
+    r = subprocess.run(["g++", "-shared", "-o", str(lib), *map(str, objs)], capture_output=True, text=True)
     if r.returncode:
         raise RuntimeError(r.stderr)
-    return LIB
+    return lib
 
 
 if __name__ == "__main__":

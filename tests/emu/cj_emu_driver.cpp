@@ -149,14 +149,15 @@ int run(const uint8_t* data, const size_t* sizes, size_t n, bool lines, bool bat
     if (wave_regions) {
         const uint32_t nw = (regions + wave_regions - 1) / wave_regions;
         uint4* carry = galloc<uint4>(nw);
-        uint32_t* nwork = galloc<uint32_t>(nw);
+        uint32_t* nwork = galloc<uint32_t>(3 * (size_t)nw);
         for (uint32_t w = 0; w < nw; w++) {
             ScanParams wp = sp;
             wp.r_begin = w * wave_regions;
             wp.r_end = std::min(regions, wp.r_begin + wave_regions);
             wp.carry_in = w ? carry + (w - 1) : nullptr;
             wp.carry_out = carry + w;
-            wp.n_work = nwork + w;
+            wp.n_work = nwork + 3 * w;
+            wp.tickets = nwork + 3 * w + 1;
             wp.work = work + 2 * (size_t)wp.r_begin;
             launch_scan(wp, lines, ScanShape{0, 0}, nullptr);
             // the wave's end value holds the counts through its last region

@@ -15,9 +15,8 @@ from tests import synth
 from tests.emu import build as emu_build
 
 
-@pytest.fixture(scope="module")
-def emu():
-    L = ctypes.CDLL(str(emu_build.build()))
+def _load(variant=""):
+    L = ctypes.CDLL(str(emu_build.build(variant=variant)))
     L.cje_parse.restype = ctypes.c_int
     L.cje_parse.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int,
                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_int64),
@@ -32,6 +31,18 @@ def emu():
                                   ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                   ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_uint32)]
     return L
+
+
+@pytest.fixture(scope="module")
+def emu():
+    return _load()
+
+
+@pytest.fixture(scope="module")
+def emu_reduce():
+    """The kernels built so that every scan of more than one prefix block
+    runs prefix_reduce (the default build does so only above 64 blocks)."""
+    return _load("reduce")
 
 
 def emu_parse(emu, data, lines=False, chunks=None, region_kib=8, wave_regions=0):
@@ -143,21 +154,25 @@ def test_batch(emu, oracle):
         o += int(dS[i])
 
 
+@pytest.mark.parametrize("variant", ["", "reduce"])
 @pytest.mark.parametrize("lines", [False, True])
-def test_multi_block_prefix(emu, oracle, cj, lines):
-    """More than 1024 regions: the prefix composes several blocks."""
+def test_multi_block_prefix(emu, emu_reduce, oracle, cj, lines, variant):
+    """1280 regions, 5 prefix blocks: each block composes the blocks before
+    it, from their regions' tables (default build) or from prefix_reduce's
+    block aggregates (the "reduce" build)."""
+    L = emu_reduce if variant else emu
     if lines:
         d, _ = synth.synth_lines(synth.CONFIG_SEED_BASE + 3, 5 << 20)
-        check(emu, oracle, d, lines=True, chunks=cj.plan_lines_count(d, 3), region_kib=4)
+        check(L, oracle, d, lines=True, chunks=cj.plan_lines_count(d, 3), region_kib=4)
     else:
         d = synth.synth_document(0x601D7777, (5 << 20) + 12345, max_depth=12, huge_string_frac=0.02,
                                  huge_string_min=20000, huge_string_max=90000)
-        check(emu, oracle, d, region_kib=4)
+        check(L, oracle, d, region_kib=4)
 
 
 @pytest.mark.parametrize("wave_regions", [1, 3, 256, 300, 600])
 @pytest.mark.parametrize("lines", [False, True])
-def test_waves(emu, oracle, cj, lines, wave_regions):
+def test_waves(emu, emu_reduce, oracle, cj, lines, wave_regions):
     """The scan in waves of regions, each wave starting from the previous
     wave's end value (a streamed parse): the same result as one scan, with wave
     boundaries inside strings, escapes and JSON-Lines records, and waves of
@@ -171,5 +186,6 @@ def test_waves(emu, oracle, cj, lines, wave_regions):
         d = synth.synth_document(0x3A7E5, (2 << 20) + 4321, max_depth=12, huge_string_frac=0.05,
                                  huge_string_min=5000, huge_string_max=30000)
         check(emu, oracle, d, region_kib=4, wave_regions=wave_regions)
+        check(emu_reduce, oracle, d, region_kib=4, wave_regions=wave_regions)
         b = synth.synth_backslash_string(7, 300000)
         check(emu, oracle, b, region_kib=4, wave_regions=wave_regions)
