@@ -69,17 +69,20 @@ __device__ __forceinline__ int32_t tree_value(const PairParams& P, int lvl, uint
     return 0x7FFFFFFF - (int32_t)(uint32_t)v;
 }
 
+// entries of min-tree level lvl over nch chunks: ceil(nch / 32^lvl)
+__device__ __forceinline__ uint64_t level_size(uint64_t nch, int lvl) {
+    const int sh = 5 * lvl;
+    return (nch + (1ull << sh) - 1) >> sh;
+}
+
 // first chunk index > c whose minimum depth is <= d, or -1
 __device__ int64_t next_le(const PairParams& P, uint64_t nch, uint64_t c, int32_t d) {
-    uint64_t size[kTreeLevels + 1];
-    size[0] = nch;
-    for (int l = 1; l <= kTreeLevels; l++) size[l] = (size[l - 1] + 31) / 32;
     uint64_t i = c + 1;
     int lvl = 0;
     while (true) {
-        if (i >= size[lvl]) return -1;
+        if (i >= level_size(nch, lvl)) return -1;
         uint64_t gend = (i | 31) + 1;
-        if (gend > size[lvl]) gend = size[lvl];
+        if (gend > level_size(nch, lvl)) gend = level_size(nch, lvl);
         bool found = false;
         for (; i < gend; i++)
             if (tree_value(P, lvl, i) <= d) { found = true; break; }
@@ -92,7 +95,7 @@ __device__ int64_t next_le(const PairParams& P, uint64_t nch, uint64_t c, int32_
         lvl--;
         i *= 32;
         uint64_t gend = i + 32;
-        if (gend > size[lvl]) gend = size[lvl];
+        if (gend > level_size(nch, lvl)) gend = level_size(nch, lvl);
         for (; i < gend; i++)
             if (tree_value(P, lvl, i) <= d) break;
         if (i >= gend) return -1;   // inconsistent tree (only on a timeout path)
@@ -104,15 +107,12 @@ __device__ int64_t next_le(const PairParams& P, uint64_t nch, uint64_t c, int32_
 // group of 32 entries is read at once, one lane per entry, and a ballot finds
 // the first that qualifies -- one dependent load per level instead of up to 32.
 __device__ int64_t next_le_warp(const PairParams& P, uint64_t nch, uint64_t c, int32_t d, int lane) {
-    uint64_t size[kTreeLevels + 1];
-    size[0] = nch;
-    for (int l = 1; l <= kTreeLevels; l++) size[l] = (size[l - 1] + 31) / 32;
     uint64_t i = c + 1;
     int lvl = 0;
     while (true) {
-        if (i >= size[lvl]) return -1;
+        if (i >= level_size(nch, lvl)) return -1;
         const uint64_t g0 = i & ~31ull, j = g0 + (uint64_t)lane;
-        const bool ok = j >= i && j < size[lvl] && tree_value(P, lvl, j) <= d;
+        const bool ok = j >= i && j < level_size(nch, lvl) && tree_value(P, lvl, j) <= d;
         const uint32_t m = __ballot_sync(0xFFFFFFFFu, ok);
         if (m) { i = g0 + (uint64_t)(__ffs(m) - 1); break; }
         if (lvl == kTreeLevels) return -1;
@@ -122,7 +122,7 @@ __device__ int64_t next_le_warp(const PairParams& P, uint64_t nch, uint64_t c, i
     while (lvl > 0) {
         lvl--;
         const uint64_t g0 = i * 32, j = g0 + (uint64_t)lane;
-        const bool ok = j < size[lvl] && tree_value(P, lvl, j) <= d;
+        const bool ok = j < level_size(nch, lvl) && tree_value(P, lvl, j) <= d;
         const uint32_t m = __ballot_sync(0xFFFFFFFFu, ok);
         if (!m) return -1;          // inconsistent tree (only on a timeout path)
         i = g0 + (uint64_t)(__ffs(m) - 1);
@@ -183,16 +183,27 @@ __global__ void __launch_bounds__(256) pair_chunks(PairParams P)
         }
         const uint64_t base = c * kChunk;
         uint32_t err = 0;
-        const uint2 r0 = __ldcg(P.brk + base);
+        // the chunk's records, all loaded at once (one per lane per round)
+        uint2 recs[kChunk / 32];
+#pragma unroll
+        for (int j = 0; j < kChunk / 32; j++) {
+            const int i = j * 32 + lane;
+            recs[j] = i < cnt ? __ldcg(P.brk + base + i) : make_uint2(0u, 0u);
+        }
+        const uint32_t r0y = __shfl_sync(FULL, recs[0].y, 0);
+        const uint2 r0 = make_uint2(0u, r0y);
         const int32_t L0 = (int32_t)r0.y >> 1;
         // the head slots this chunk's records use (levels L0 - kChunk ..
         // L0 + kChunk map to slots 0 .. kHeads - 1): only those are cleared
         // here and read back at the end
         int32_t smin = kHeads - 1, smax = 0;
-        for (int i = lane; i < cnt; i += 32) {
-            const int32_t sl = ((int32_t)__ldcg(&P.brk[base + i].y) >> 1) - L0 + kChunk;
-            smin = min(smin, max(sl, 0));
-            smax = max(smax, min(sl, kHeads - 1));
+#pragma unroll
+        for (int j = 0; j < kChunk / 32; j++) {
+            if (j * 32 + lane < cnt) {
+                const int32_t sl = ((int32_t)recs[j].y >> 1) - L0 + kChunk;
+                smin = min(smin, max(sl, 0));
+                smax = max(smax, min(sl, kHeads - 1));
+            }
         }
         smin = __reduce_min_sync(FULL, smin);
         smax = __reduce_max_sync(FULL, smax);
@@ -203,10 +214,12 @@ __global__ void __launch_bounds__(256) pair_chunks(PairParams P)
         uint32_t last_open = 0;
         __syncwarp();
 
-        for (int r = 0; r < cnt; r += 32) {
+#pragma unroll
+        for (int j = 0; j < kChunk / 32; j++) {
+            const int r = j * 32;
+            if (r >= cnt) break;
             const bool valid = (r + lane) < cnt;
-            uint2 rec = make_uint2(0u, 0u);
-            if (valid) rec = __ldcg(P.brk + base + r + lane);
+            const uint2 rec = recs[j];
             const int32_t lvl = (int32_t)rec.y >> 1;
             const uint32_t is_open = rec.y & 1u;
             const uint32_t key = valid ? (uint32_t)lvl : (0xC0000000u | (uint32_t)lane);

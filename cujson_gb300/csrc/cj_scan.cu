@@ -10,7 +10,7 @@
 //                 of the 4 entry states (escape pending, inside a string): the
 //                 exit state, structural count, bracket count and depth delta.
 //   prefix_reduce (256 regions per block, one per thread) composes each
-//                 block's tables (only when there are more than 64 blocks).
+//                 block's tables (only when there is more than one block).
 //   prefix_apply  (the same blocks) composes the blocks before its own, the
 //                 warps (chunks of 32 regions) before each warp and the regions
 //                 before each region, and writes the segment ends, the totals,
@@ -276,6 +276,33 @@ __device__ __forceinline__ void store_tab(uint4* p, const Ent t[4]) {
     for (int s = 0; s < 4; s++) p[s] = make_uint4(t[s].st, t[s].s, t[s].k, (uint32_t)t[s].d);
 }
 
+__device__ __forceinline__ void shfl_tab(const Ent t[4], Ent u[4], int src_delta, bool up) {
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+        if (up) {
+            u[s].st = __shfl_up_sync(FULL, t[s].st, src_delta);
+            u[s].s = __shfl_up_sync(FULL, t[s].s, src_delta);
+            u[s].k = __shfl_up_sync(FULL, t[s].k, src_delta);
+            u[s].d = __shfl_up_sync(FULL, t[s].d, src_delta);
+        } else {
+            u[s].st = __shfl_down_sync(FULL, t[s].st, src_delta);
+            u[s].s = __shfl_down_sync(FULL, t[s].s, src_delta);
+            u[s].k = __shfl_down_sync(FULL, t[s].k, src_delta);
+            u[s].d = __shfl_down_sync(FULL, t[s].d, src_delta);
+        }
+    }
+}
+
+// composition of the 32 lanes' tables in lane order, in lane 0
+__device__ __forceinline__ void warp_reduce_tab(Ent t[4], int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        Ent u[4];
+        shfl_tab(t, u, o, false);
+        if ((lane & (2 * o - 1)) == 0 && lane + o < 32) tab_compose(t, u, t);
+    }
+}
+
 // ---- scan_tables --------------------------------------------------------------
 
 // Transfer table of one region (the whole warp; lanes 0-3 write entries 0-3).
@@ -439,12 +466,7 @@ __global__ void __launch_bounds__(kThreads, kTablesMinBlocks) scan_tables(ScanPa
 // every SM.
 
 constexpr int kPrefixWarps = kPrefixPerBlock / 32;
-// scans of at most this many prefix blocks skip prefix_reduce: each block
-// composes the tables of the regions before it directly (at most 63 per thread)
-#ifndef CJ_DIRECT_PREFIX_BLOCKS
-#define CJ_DIRECT_PREFIX_BLOCKS 64
-#endif
-constexpr int kDirectPrefixBlocks = CJ_DIRECT_PREFIX_BLOCKS;
+
 
 // ---- state-first prefix ------------------------------------------------------------
 // Applying tables one after another, the string/escape state follows from the
@@ -578,67 +600,27 @@ __device__ __forceinline__ void block_scan_sums(const Sums& v, Sums* sm, int lan
 // Block b: the composition of its regions' tables.
 __global__ void __launch_bounds__(kPrefixPerBlock) prefix_reduce(ScanParams P)
 {
-    __shared__ uint32_t s_map[kPrefixWarps + 1];
-    __shared__ Sums s_w[kPrefixWarps][4];
+    __shared__ Ent s_w[kPrefixWarps][4];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t r = P.r_begin + blockIdx.x * (uint32_t)kPrefixPerBlock + threadIdx.x;
-    const bool in_range = r < P.r_end;
     Ent t[4];
-    if (in_range) load_tab(P.rtab + (size_t)r * 4, t);
+    if (r < P.r_end) load_tab(P.rtab + (size_t)r * 4, t);
     else tab_identity(t);
-    // the state each region is entered in, for each entry state of the block;
-    // then the counts summed for each
-    uint32_t m_ex, m_tot;
-    block_scan_maps(map_of(t), s_map, lane, warp, m_ex, &m_tot);
-    Sums a[4];
-#pragma unroll
-    for (uint32_t s0 = 0; s0 < 4; s0++) a[s0] = in_range ? sums_of(ent_select(t, map_at(m_ex, s0))) : sums_zero();
-    // reductions in thread order: lane L takes lane L+o's run after its own
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-#pragma unroll
-        for (int s0 = 0; s0 < 4; s0++) {
-            Sums y;
-            y.s = __shfl_down_sync(FULL, a[s0].s, o);
-            y.k = __shfl_down_sync(FULL, a[s0].k, o);
-            y.d = __shfl_down_sync(FULL, a[s0].d, o);
-            y.f = __shfl_down_sync(FULL, a[s0].f, o);
-            if (lane + o < 32) a[s0] = sums_then(a[s0], y);
-        }
-    }
+    warp_reduce_tab(t, lane);
     if (lane == 0) {
 #pragma unroll
-        for (int s0 = 0; s0 < 4; s0++) s_w[warp][s0] = a[s0];
+        for (int k = 0; k < 4; k++) s_w[warp][k] = t[k];
     }
     __syncthreads();
     if (warp == 0) {
+        if (lane < kPrefixWarps) {
 #pragma unroll
-        for (int s0 = 0; s0 < 4; s0++) a[s0] = lane < kPrefixWarps ? s_w[lane][s0] : sums_zero();
-#pragma unroll
-        for (int o = 1; o < kPrefixWarps; o <<= 1) {
-#pragma unroll
-            for (int s0 = 0; s0 < 4; s0++) {
-                Sums y;
-                y.s = __shfl_down_sync(FULL, a[s0].s, o);
-                y.k = __shfl_down_sync(FULL, a[s0].k, o);
-                y.d = __shfl_down_sync(FULL, a[s0].d, o);
-                y.f = __shfl_down_sync(FULL, a[s0].f, o);
-                if (lane + o < 32) a[s0] = sums_then(a[s0], y);
-            }
+            for (int k = 0; k < 4; k++) t[k] = s_w[lane][k];
+        } else {
+            tab_identity(t);
         }
-        if (lane == 0) {
-            // the block's table: for each entry state, exit state (with the
-            // reset bits seen) and the counts
-            Ent agg[4];
-#pragma unroll
-            for (uint32_t s0 = 0; s0 < 4; s0++) {
-                agg[s0].st = map_at(m_tot, s0) | a[s0].f;
-                agg[s0].s = a[s0].s;
-                agg[s0].k = a[s0].k;
-                agg[s0].d = a[s0].d;
-            }
-            store_tab(P.bagg + (size_t)blockIdx.x * 4, agg);
-        }
+        warp_reduce_tab(t, lane);
+        if (lane == 0) store_tab(P.bagg + (size_t)blockIdx.x * 4, t);
     }
 }
 
@@ -659,16 +641,13 @@ __global__ void __launch_bounds__(kPrefixPerBlock) prefix_apply(ScanParams P)
         const uint4 c = __ldcg(P.carry_in);
         v0.st = c.x; v0.s = c.y; v0.k = c.z; v0.d = (int32_t)c.w;
     }
-    // the value before this block: every thread takes a run of the units
-    // before it -- the blocks' aggregates, or, for a scan of at most
-    // kDirectPrefixBlocks blocks (no prefix_reduce launch), the regions' own
-    // tables -- first for its state map, then, once the state at the run's
-    // start is known, for its sums
+    // the value before this block: every thread takes a run of the blocks'
+    // aggregate tables before it (from prefix_reduce), first for its state
+    // map, then, once the state at the run's start is known, for its sums
     Ent vb = v0;
     if (b > 0) {
-        const bool direct = gridDim.x <= (uint32_t)kDirectPrefixBlocks;
-        const uint32_t units = direct ? b * (uint32_t)kPrefixPerBlock : b;
-        const uint4* src = direct ? P.rtab + (size_t)P.r_begin * 4 : P.bagg;
+        const uint32_t units = b;
+        const uint4* src = P.bagg;
         const uint32_t q = (units + kPrefixPerBlock - 1) / kPrefixPerBlock;
         const uint32_t lo = min(units, threadIdx.x * q), hi = min(units, lo + q);
         uint32_t m = kMapIdentity;
@@ -964,14 +943,14 @@ void launch_r(const ScanParams& p, bool lines, int tables_grid, int emit_grid, c
 #ifdef CJ_EMU
     (void)stream; (void)ev;
     cj_emu::launch(tables_grid, kThreads, 0, [&] { if (lines) scan_tables<true, R>(p); else scan_tables<false, R>(p); });
-    if (nb > (uint32_t)kDirectPrefixBlocks) cj_emu::launch(nb, kPrefixPerBlock, 0, [&] { prefix_reduce(p); });
+    if (nb > 1) cj_emu::launch(nb, kPrefixPerBlock, 0, [&] { prefix_reduce(p); });
     cj_emu::launch(nb, kPrefixPerBlock, 0, [&] { prefix_apply(p); });
     cj_emu::launch(emit_grid, kThreads, 0, [&] { scan_emit<R>(p); });
 #else
     if (lines) scan_tables<true, R><<<tables_grid, kThreads, 0, stream>>>(p);
     else scan_tables<false, R><<<tables_grid, kThreads, 0, stream>>>(p);
     if (ev) cudaEventRecord(ev[0], stream);
-    if (nb > (uint32_t)kDirectPrefixBlocks) prefix_reduce<<<nb, kPrefixPerBlock, 0, stream>>>(p);
+    if (nb > 1) prefix_reduce<<<nb, kPrefixPerBlock, 0, stream>>>(p);
     prefix_apply<<<nb, kPrefixPerBlock, 0, stream>>>(p);
     if (ev) cudaEventRecord(ev[1], stream);
     scan_emit<R><<<emit_grid, kThreads, 0, stream>>>(p);
@@ -1022,7 +1001,7 @@ cudaError_t preload_scan_kernels()
 int scan_launches(uint32_t n_regions)
 {
     if (n_regions == 0) return 0;
-    return n_regions > (uint32_t)kPrefixPerBlock * kDirectPrefixBlocks ? 4 : 3;
+    return n_regions > (uint32_t)kPrefixPerBlock ? 4 : 3;
 }
 
 void launch_scan(const ScanParams& p0, bool lines, const ScanShape& shape, cudaStream_t stream, cudaEvent_t* ev)

@@ -21,9 +21,8 @@ FLAGS = ["-O1", "-g", "-std=c++17", "-fPIC", "-w", "-DCJ_EMU=1", f"-I{HERE / 'sh
 
 
 # Variants of the emulation: extra defines for the kernels' sources, and the
-# library each builds.  "reduce" sends every scan of more than one prefix block
-# through prefix_reduce, which the default build uses only above 64 blocks.
-VARIANTS = {"": [], "reduce": ["-DCJ_DIRECT_PREFIX_BLOCKS=1"]}
+# library each builds.
+VARIANTS = {"": []}
 
 
 def _lib(variant: str) -> Path:

@@ -38,13 +38,6 @@ def emu():
     return _load()
 
 
-@pytest.fixture(scope="module")
-def emu_reduce():
-    """The kernels built so that every scan of more than one prefix block
-    runs prefix_reduce (the default build does so only above 64 blocks)."""
-    return _load("reduce")
-
-
 def emu_parse(emu, data, lines=False, chunks=None, region_kib=8, wave_regions=0):
     buf = np.ascontiguousarray(np.frombuffer(bytes(data), np.uint8) if isinstance(data, bytes) else data)
     sizes = np.asarray(chunks if chunks is not None else [buf.size], np.uint64)
@@ -154,13 +147,11 @@ def test_batch(emu, oracle):
         o += int(dS[i])
 
 
-@pytest.mark.parametrize("variant", ["", "reduce"])
 @pytest.mark.parametrize("lines", [False, True])
-def test_multi_block_prefix(emu, emu_reduce, oracle, cj, lines, variant):
-    """1280 regions, 5 prefix blocks: each block composes the blocks before
-    it, from their regions' tables (default build) or from prefix_reduce's
-    block aggregates (the "reduce" build)."""
-    L = emu_reduce if variant else emu
+def test_multi_block_prefix(emu, oracle, cj, lines):
+    """1280 regions, 5 prefix blocks: prefix_reduce's block aggregates, and
+    each block's run of the aggregates before it."""
+    L = emu
     if lines:
         d, _ = synth.synth_lines(synth.CONFIG_SEED_BASE + 3, 5 << 20)
         check(L, oracle, d, lines=True, chunks=cj.plan_lines_count(d, 3), region_kib=4)
@@ -172,7 +163,7 @@ def test_multi_block_prefix(emu, emu_reduce, oracle, cj, lines, variant):
 
 @pytest.mark.parametrize("wave_regions", [1, 3, 256, 300, 600])
 @pytest.mark.parametrize("lines", [False, True])
-def test_waves(emu, emu_reduce, oracle, cj, lines, wave_regions):
+def test_waves(emu, oracle, cj, lines, wave_regions):
     """The scan in waves of regions, each wave starting from the previous
     wave's end value (a streamed parse): the same result as one scan, with wave
     boundaries inside strings, escapes and JSON-Lines records, and waves of
@@ -186,6 +177,5 @@ def test_waves(emu, emu_reduce, oracle, cj, lines, wave_regions):
         d = synth.synth_document(0x3A7E5, (2 << 20) + 4321, max_depth=12, huge_string_frac=0.05,
                                  huge_string_min=5000, huge_string_max=30000)
         check(emu, oracle, d, region_kib=4, wave_regions=wave_regions)
-        check(emu_reduce, oracle, d, region_kib=4, wave_regions=wave_regions)
         b = synth.synth_backslash_string(7, 300000)
         check(emu, oracle, b, region_kib=4, wave_regions=wave_regions)
