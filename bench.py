@@ -201,8 +201,10 @@ def cpu_baseline_sample(sample_bytes: int):
 
 def workload_config(N: int, world: int) -> dict:
     """The `config` object both arms print (identical for the same workload)."""
-    return {"workload": WORKLOAD, "bytes": N, "parallelism": f"replicas x{world}",
-            "l2": "input 1 GiB > 129 MB L2, no flush between steps"}
+    wl = WORKLOAD if N == 1 << 30 else WORKLOAD.replace("1 GiB (1073741824 B)", f"{N} B")
+    l2 = ("input larger than the 129 MB L2, no flush between steps" if N > 129 * 10 ** 6
+          else "input fits the 129 MB L2 (warm-L2 figure)")
+    return {"workload": wl, "bytes": N, "parallelism": f"replicas x{world}", "l2": l2}
 
 
 def run_reference(args, world, rank):
@@ -738,7 +740,8 @@ def run_ours(args, world, rank, local, pg):
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
         "config": workload_config(N, world),
         "workload_stats": {"structurals": S, "brackets": K, "max_depth": int(inf2.max_depth)},
-        "roofline": {"bound": "hbm", "kernel": "scan_kernel", "achieved": round(achieved, 1),
+        "roofline": {"bound": "hbm", "kernel": "scan (scan_tables + prefix_reduce + prefix_apply + scan_emit)",
+                     "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "peak_kind": peak_kind, "traffic": traffic,
                      "algorithmic_bytes": B},

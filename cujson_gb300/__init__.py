@@ -95,6 +95,8 @@ _SIGNATURES = {
                                          ctypes.POINTER(_Result)]),
     "cj_parse_lines": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                       ctypes.c_size_t, ctypes.POINTER(_Result)]),
+    "cj_parse_lines_planned": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
+                                              ctypes.c_size_t, ctypes.POINTER(_Result)]),
     "cj_result_free": (None, [ctypes.POINTER(_Result)]),
     "cj_parse_into": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
                                      ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ParseInfo)]),
@@ -160,6 +162,9 @@ _SIGNATURES = {
                                            ctypes.POINTER(ctypes.c_size_t)]),
     "cj_plan_lines_count_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                                   ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]),
+    "cj_plan_lines_bytes_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                                  ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+                                                  ctypes.POINTER(ctypes.c_size_t), ctypes.c_void_p]),
     "cj_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "cj_last_status": (ctypes.c_int, []),
     "cj_last_error": (ctypes.c_char_p, []),
@@ -297,6 +302,16 @@ class Context:
         r = _Result()
         st = lib().cj_parse_lines(self._h, ptrs, sizes, len(arrs), ctypes.byref(r))
         _check(st, "parse_json_lines")
+        return _take_result(r)
+
+    def parse_lines_planned(self, data, chunk_count: int = 0, chunk_bytes: int = 0) -> ParseResult:
+        """cj_parse_lines_planned: one JSON-Lines buffer, its chunks planned on
+        the device (chunk_count != 0: by count; else by the byte limit)."""
+        buf = _u8(data)
+        r = _Result()
+        st = lib().cj_parse_lines_planned(self._h, buf.ctypes.data if buf.size else None, buf.size, chunk_count,
+                                          chunk_bytes, ctypes.byref(r))
+        _check(st, "parse_lines_planned")
         return _take_result(r)
 
     def try_parse(self, data, lines: bool = False, chunk_sizes: Optional[Sequence[int]] = None):
@@ -485,6 +500,20 @@ class Context:
                                                 ctypes.c_void_p(stream) if stream else None),
                "plan_lines_count_device")
         return [int(x) for x in out]
+
+    def plan_lines_bytes_device(self, d_ptr: int, size: int, chunk_bytes: int, stream: int = 0) -> List[int]:
+        """cj_plan_lines_bytes_device: the byte-limit chunk plan of a JSON-Lines
+        buffer at device address `d_ptr`, computed on the device (`stream` as
+        for plan_lines_count_device)."""
+        dp = ctypes.c_void_p(d_ptr) if size else None
+        sp = ctypes.c_void_p(stream) if stream else None
+        n = ctypes.c_size_t()
+        _check(lib().cj_plan_lines_bytes_device(self._h, dp, size, chunk_bytes, None, 0, ctypes.byref(n), sp),
+               "plan_lines_bytes_device")
+        out = np.zeros(max(1, n.value), dtype=np.uint64)
+        _check(lib().cj_plan_lines_bytes_device(self._h, dp, size, chunk_bytes, out.ctypes.data, out.size,
+                                                ctypes.byref(n), sp), "plan_lines_bytes_device")
+        return [int(x) for x in out[: n.value]]
 
     def parse_into(self, data, out: np.ndarray, lines: bool = False) -> ParseInfo:
         buf = _u8(data)

@@ -145,6 +145,7 @@ struct cj_context {
     DevBuf<uint32_t> plan_counts;
     DevBuf<uint2> plan_req;
     DevBuf<unsigned long long> plan_pos;
+    DevBuf<unsigned long long> plan_bounds;   // cj_plan_lines_bytes_device: boundaries, counters
 
     // launch shapes (0 = default), set by cj_context_set_tuning / cj_autotune_staged
     int tune_region_steps = 0;
@@ -719,6 +720,106 @@ cj_status stage_run(cj_context* ctx, const uint8_t* const* chunks, const size_t*
     return st;
 }
 
+// One-shot JSON-Lines parse of a host buffer whose chunks are planned on the
+// device: the buffer goes to the staging area (`pack`) in kOverlapChunk
+// pieces on the copy stream, each piece's newlines counted per 64 KiB block as
+// soon as it lands (chunk-count plans); the plan is finished on the device,
+// every chunk moved to its 1 KiB-aligned place in `in` (batch_scatter) and the
+// chunks run as cj_parse_lines runs them.
+cj_status stage_lines_planned(cj_context* ctx, const uint8_t* data, size_t size, size_t chunk_count,
+                              size_t chunk_bytes, std::vector<size_t>& sizes)
+{
+    ctx->staged = false;
+    ctx->graph_valid = false;
+    if (!data || size == 0) return CJ_ERR_INVALID_ARGUMENT;
+    if (size > CJ_MAX_INPUT_BYTES) return CJ_ERR_TOO_LARGE;
+    CJ_CUDA(cudaSetDevice(ctx->device));
+    cj_status st;
+    const size_t nb = (size + kPlanBlockBytes - 1) / kPlanBlockBytes;
+    if ((st = ensure(ctx, ctx->pack, size + 16))) return st;
+    if (chunk_count) {
+        if ((st = ensure(ctx, ctx->plan_counts, nb))) return st;
+        if ((st = ensure(ctx, ctx->plan_req, chunk_count + 1))) return st;
+        if ((st = ensure(ctx, ctx->plan_pos, chunk_count + 1))) return st;
+    }
+    // the copy, and the newline counts of each piece behind it
+    CJ_CUDA(cudaEventRecord(ctx->ev_reset, ctx->stream));
+    CJ_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_reset, 0));
+    for (uint64_t o = 0; o < size; o += kOverlapChunk) {
+        const uint64_t c = std::min<uint64_t>(kOverlapChunk, size - o);
+        CJ_CUDA(cudaMemcpyAsync(ctx->pack.p + o, data + o, c, cudaMemcpyHostToDevice, ctx->copy_stream));
+        if (chunk_count) {
+            launch_plan_count(ctx->pack.p + o, c, ctx->plan_counts.p + o / kPlanBlockBytes, ctx->copy_stream);
+            ctx->launches += 1;
+        }
+    }
+    CJ_CUDA(cudaGetLastError());
+    CJ_CUDA(cudaEventRecord(ctx->ev_copied, ctx->copy_stream));
+    CJ_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_copied, 0));
+    if (chunk_count) {
+        std::vector<uint32_t> counts(nb);
+        CJ_CUDA(cudaMemcpyAsync(counts.data(), ctx->plan_counts.p, nb * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+        CJ_CUDA(cudaStreamSynchronize(ctx->stream));
+        sizes.assign(chunk_count, 0);
+        if (plan_lines_count_finish(ctx->pack.p, size, chunk_count, sizes.data(), counts.data(), data[size - 1],
+                                    ctx->plan_req.p, ctx->plan_pos.p, ctx->stream) != cudaSuccess)
+            return CJ_ERR_CUDA;
+        ctx->launches += 1;
+    } else {
+        size_t n = 0;
+        if ((st = cj_plan_lines_bytes_device(ctx, ctx->pack.p, size, chunk_bytes, nullptr, 0, &n, ctx->stream)))
+            return st;
+        sizes.assign(n, 0);
+        if ((st = cj_plan_lines_bytes_device(ctx, ctx->pack.p, size, chunk_bytes, sizes.data(), n, &n,
+                                             ctx->stream)))
+            return st;
+        ctx->launches += 2;
+    }
+    // chunks as cj_parse_lines takes them: an empty chunk is refused
+    const size_t n = sizes.size();
+    if (n == 0) return CJ_ERR_INVALID_ARGUMENT;
+    for (size_t k = 0; k < n; k++)
+        if (sizes[k] == 0) return CJ_ERR_INVALID_ARGUMENT;
+    if ((st = reserve(ctx, size, n))) return st;
+    if ((st = ensure(ctx, ctx->pack_off, 2 * (n + 1)))) return st;
+    ctx->h_segs.resize(n);
+    ctx->h_pack_off.assign(2 * (n + 1), 0);
+    uint64_t dev_off = 0, logical = 0, wo = 0;
+    for (size_t k = 0; k < n; k++) {
+        Segment& g = ctx->h_segs[k];
+        g.dev_off = dev_off;
+        g.len = sizes[k];
+        g.logical_off = logical;
+        g.out_base = 0;
+        g.brk_base = 0;
+        g.flags = (k > 0) ? kSegContinue : 0u;
+        g.pad = 0;
+        ctx->h_pack_off[k] = logical;
+        ctx->h_pack_off[n + 1 + k] = wo;
+        dev_off += round_up(sizes[k], kPadBytes);
+        logical += sizes[k];
+        wo += (sizes[k] + 3) / 4;
+    }
+    ctx->h_pack_off[n] = logical;
+    ctx->h_pack_off[2 * n + 1] = wo;
+    CJ_CUDA(cudaMemcpyAsync(ctx->pack_off.p, ctx->h_pack_off.data(), ctx->h_pack_off.size() * sizeof(uint64_t),
+                            cudaMemcpyHostToDevice, ctx->stream));
+    if ((st = place_regions(ctx))) return st;
+    launch_batch_scatter(ctx->pack.p, ctx->pack_off.p, ctx->pack_off.p + n + 1, ctx->segs.p, (uint32_t)n, wo,
+                         ctx->in.p, ctx->sm_count, ctx->stream);
+    ctx->launches += 1;
+    CJ_CUDA(cudaGetLastError());
+    // host vectors must outlive the copies
+    CJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->n_bytes = size;
+    ctx->n_segs = (uint32_t)n;
+    ctx->lines = true;
+    ctx->batch = false;
+    ctx->staged = true;
+    return CJ_OK;
+}
+
 cj_status read_info(cj_context* ctx, cj_parse_info* info)
 {
     if (!ctx->staged) return CJ_ERR_NOT_STAGED;
@@ -1072,7 +1173,7 @@ void cj_context_destroy(cj_context* ctx)
     release(ctx->seg_err); release(ctx->seg_depth); release(ctx->rchunk_off);
     release(ctx->layout_off); release(ctx->layout); release(ctx->pack); release(ctx->pack_off);
     release(ctx->q_count); release(ctx->q_out);
-    release(ctx->plan_counts); release(ctx->plan_req); release(ctx->plan_pos);
+    release(ctx->plan_counts); release(ctx->plan_req); release(ctx->plan_pos); release(ctx->plan_bounds);
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
     if (ctx->d_ready) cudaFree(ctx->d_ready);
@@ -1209,6 +1310,22 @@ cj_status cj_parse_lines(cj_context* ctx, const uint8_t* const* chunks, const si
     if (out) memset(out, 0, sizeof(*out));
     if (!ctx || !out) return finish(CJ_ERR_INVALID_ARGUMENT);
     cj_status st = stage_run(ctx, chunks, chunk_sizes, n_chunks, true);
+    cj_parse_info info;
+    if (!st) st = read_info(ctx, &info);
+    if (!st && info.status != CJ_OK) st = (cj_status)info.status;
+    if (!st) st = to_result(ctx, info, out);
+    out->status = st;
+    return finish(st);
+}
+
+cj_status cj_parse_lines_planned(cj_context* ctx, const uint8_t* host_data, size_t size, size_t chunk_count,
+                                 size_t chunk_bytes, cj_result* out)
+{
+    if (out) memset(out, 0, sizeof(*out));
+    if (!ctx || !out) return finish(CJ_ERR_INVALID_ARGUMENT);
+    std::vector<size_t> sizes;
+    cj_status st = stage_lines_planned(ctx, host_data, size, chunk_count, chunk_bytes, sizes);
+    if (!st) st = run(ctx);
     cj_parse_info info;
     if (!st) st = read_info(ctx, &info);
     if (!st && info.status != CJ_OK) st = (cj_status)info.status;
@@ -1556,6 +1673,25 @@ const char* cj_status_string(int status)
 int cj_last_status(void) { return g_last_status; }
 void cj_set_last_status(int status) { g_last_status = status; }
 const char* cj_last_error(void) { return cj_status_string(g_last_status); }
+
+cj_status cj_plan_lines_bytes_device(cj_context* ctx, const uint8_t* d_data, size_t size, size_t chunk_bytes,
+                                     size_t* chunk_sizes, size_t cap, size_t* n_chunks, void* stream)
+{
+    if (!ctx || !n_chunks || (!d_data && size)) return CJ_ERR_INVALID_ARGUMENT;
+    CJ_CUDA(cudaSetDevice(ctx->device));
+    *n_chunks = 0;
+    if (size == 0) return CJ_OK;
+    CJ_CUDA(cudaEventRecord(ctx->ev_plan, (cudaStream_t)stream));
+    CJ_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_plan, 0));
+    const size_t keep = chunk_sizes ? cap : 0;            // boundaries kept on the device
+    cj_status st;
+    if ((st = ensure(ctx, ctx->plan_bounds, keep + 2))) return st;
+    if (plan_lines_bytes_device(d_data, size, chunk_bytes, chunk_sizes, keep, n_chunks, ctx->plan_bounds.p + 2,
+                                ctx->plan_bounds.p, ctx->stream) != cudaSuccess)
+        return CJ_ERR_CUDA;
+    if (chunk_sizes && *n_chunks > cap) return CJ_ERR_CAPACITY;
+    return CJ_OK;
+}
 
 cj_status cj_plan_lines_count_device(cj_context* ctx, const uint8_t* d_data, size_t size, size_t chunk_count,
                                      size_t* chunk_sizes, void* stream)

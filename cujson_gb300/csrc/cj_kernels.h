@@ -118,6 +118,19 @@ cudaError_t preload_batch_kernels();
 cudaError_t plan_lines_count_device(const uint8_t* d_data, size_t size, size_t chunk_count,
                                     size_t* chunk_sizes, uint32_t* d_counts, uint2* d_req,
                                     unsigned long long* d_pos, cudaStream_t stream);
+// the same in two parts: newlines per 64 KiB block of d_data (the counts of a
+// sub-range starting on a block boundary go to its blocks' slots), then, with
+// the counts and the buffer's last byte on the host, the chunk sizes
+void launch_plan_count(const uint8_t* d_data, size_t size, uint32_t* d_counts, cudaStream_t stream);
+cudaError_t plan_lines_count_finish(const uint8_t* d_data, size_t size, size_t chunk_count, size_t* chunk_sizes,
+                                    const uint32_t* counts, uint8_t last, uint2* d_req, unsigned long long* d_pos,
+                                    cudaStream_t stream);
+constexpr uint64_t kPlanBlockBytes = 65536;
+// JSON-Lines byte-limit plan of a device buffer (cj_plan.cu); scratch: cap
+// boundaries and 2 counters.  Sizes are written only when they fit in cap.
+cudaError_t plan_lines_bytes_device(const uint8_t* d_data, size_t size, size_t chunk_bytes, size_t* chunk_sizes,
+                                    size_t cap, size_t* n_chunks, unsigned long long* d_bounds,
+                                    unsigned long long* d_count, cudaStream_t stream);
 
 cudaError_t launch_query(const uint8_t* in, const Segment* segs, uint32_t n_segs, const int32_t* pos,
                          const int32_t* pair, const uint2* brk, uint32_t S, uint32_t K, const char* key,

@@ -113,6 +113,18 @@ cj_status cj_parse_standard(cj_context* ctx, const uint8_t* host_data, size_t si
                             cj_result* out);
 cj_status cj_parse_lines(cj_context* ctx, const uint8_t* const* chunks,
                          const size_t* chunk_sizes, size_t n_chunks, cj_result* out);
+/* One-shot JSON-Lines parse of one host buffer, its chunks planned on the
+ * device (no counterpart call in the reference: it replaces the host '\n'
+ * scan of loadJSONLines_chunkCount / _chunkSizeBytes, cujson/load_file.cu:
+ * 71-78 and :141-173, followed by parse_json_lines).  chunk_count != 0: the
+ * plan of cj_plan_lines_count (newlines counted per 64 KiB block on the device
+ * as each 64 MiB piece of the copy lands); else the plan of
+ * cj_plan_lines_bytes with `chunk_bytes`.  The result, segment sizes
+ * included, is that of planning the buffer on the host and calling
+ * cj_parse_lines; a plan with an empty chunk is refused with
+ * CJ_ERR_INVALID_ARGUMENT, as parse_json_lines refuses one. */
+cj_status cj_parse_lines_planned(cj_context* ctx, const uint8_t* host_data, size_t size, size_t chunk_count,
+                                 size_t chunk_bytes, cj_result* out);
 void      cj_result_free(cj_result* res);
 
 /* One-shot parse into a caller-provided host buffer (pinned for full speed)
@@ -362,6 +374,15 @@ cj_status cj_plan_lines_bytes(const uint8_t* data, size_t size, size_t chunk_byt
  * (tests/test_plan_golden.py). */
 cj_status cj_plan_lines_count_device(cj_context* ctx, const uint8_t* d_data, size_t size,
                                      size_t chunk_count, size_t* chunk_sizes, void* stream);
+/* cj_plan_lines_bytes_device: the plan of cj_plan_lines_bytes for a buffer
+ * already in device memory, computed on the device (one warp walks the chunk
+ * boundaries, reading backwards from each chunk start + chunk_bytes to the
+ * newline that ends the chunk); arguments and results as cj_plan_lines_bytes,
+ * `stream` as for cj_plan_lines_count_device.  Replaces the host '\n' scan of
+ * loadJSONLines_chunkSizeBytes (cujson/load_file.cu:109-180) for
+ * device-resident input. */
+cj_status cj_plan_lines_bytes_device(cj_context* ctx, const uint8_t* d_data, size_t size, size_t chunk_bytes,
+                                     size_t* chunk_sizes, size_t cap, size_t* n_chunks, void* stream);
 
 const char* cj_status_string(int status);
 /* Status of the calling thread's last drop-in parse (parse_standard_json /

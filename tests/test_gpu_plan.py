@@ -1,7 +1,8 @@
-"""cj_plan_lines_count_device (JSON-Lines chunk plan computed on the device)
-against cj_plan_lines_count (the host planner; both are pinned to the
-reference's loadJSONLines_chunkCount by tests/test_plan_golden.py), and its
-ordering after the stream that fills the buffer."""
+"""cj_plan_lines_count_device and cj_plan_lines_bytes_device (JSON-Lines
+chunk plans computed on the device) against cj_plan_lines_count and
+cj_plan_lines_bytes (the host planners; all are pinned to the reference's
+loaders by tests/test_plan_golden.py), and their ordering after the stream
+that fills the buffer."""
 import numpy as np
 import pytest
 from tests import synth
@@ -47,8 +48,22 @@ def test_device_plan_matches_host_plan(cj, ctx, torch_cuda):
             assert sum(got) == data.size, (name, n)
 
 
+def test_device_bytes_plan_matches_host_plan(cj, ctx, torch_cuda):
+    torch = torch_cuda
+    for name, data in _cases(cj):
+        d = torch.from_numpy(np.array(data, copy=True)).to("cuda")
+        for limit in (0, 1, 2, 100, 1023, 1024, 4096, 65536, 1 << 20, data.size - 1, data.size, data.size + 1):
+            if limit < 0:
+                continue
+            want = cj.plan_lines_bytes(data, limit)
+            got = ctx.plan_lines_bytes_device(d.data_ptr(), int(data.size), limit)
+            assert got == want, (name, limit)
+            assert sum(got) == data.size, (name, limit)
+
+
 def test_device_plan_empty(ctx):
     assert ctx.plan_lines_count_device(0, 0, 3) == [0, 0, 0]
+    assert ctx.plan_lines_bytes_device(0, 0, 100) == []
 
 
 def test_device_plan_waits_for_the_filling_stream(cj, ctx, torch_cuda):
@@ -73,3 +88,38 @@ def test_device_plan_waits_for_the_filling_stream(cj, ctx, torch_cuda):
 
 def cj_seed():
     return synth.CONFIG_SEED_BASE + 3
+
+
+@pytest.mark.parametrize("mode,n", [("count", 1), ("count", 4), ("count", 37), ("bytes", 1 << 20),
+                                    ("bytes", 65536), ("bytes", 10 << 20)])
+def test_parse_lines_planned(cj, ctx, oracle, mode, n):
+    """One host buffer planned on the device, moved into place and parsed:
+    the same result and segment sizes as planning on the host and calling
+    cj_parse_lines, and the oracle's."""
+    data, _ = synth.synth_lines(synth.CONFIG_SEED_BASE + 23, (96 << 20) + 12345)
+    sizes = cj.plan_lines_count(data, n) if mode == "count" else cj.plan_lines_bytes(data, n)
+    if mode == "count":
+        res = ctx.parse_lines_planned(data, chunk_count=n)
+    else:
+        res = ctx.parse_lines_planned(data, chunk_bytes=n)
+    offs = np.cumsum([0] + sizes[:-1])
+    want = ctx.parse_json_lines([data[o:o + s] for o, s in zip(offs, sizes)])
+    np.testing.assert_array_equal(res.buffer, want.buffer)
+    assert list(res.segment_sizes) == list(want.segment_sizes)
+    ref = oracle.parse(data, lines=True, chunk_sizes=sizes)
+    np.testing.assert_array_equal(res.buffer, ref.reference_layout())
+
+
+def test_parse_lines_planned_refuses_empty_chunks(cj, ctx):
+    """A first line longer than the byte limit gives an empty first chunk,
+    which cj_parse_lines refuses (as parse_json_lines does): so does the
+    planned parse; and more chunks than lines."""
+    data = np.frombuffer(b"[" + b"1," * 3000 + b"1]\n" + b"{}\n" * 10, np.uint8).copy()
+    with pytest.raises(cj.CujsonError) as e:
+        ctx.parse_lines_planned(data, chunk_bytes=1000)
+    assert e.value.status == cj.ERR_INVALID_ARGUMENT
+    with pytest.raises(cj.CujsonError) as e:
+        ctx.parse_lines_planned(data, chunk_count=50)
+    assert e.value.status == cj.ERR_INVALID_ARGUMENT
+    res = ctx.parse_lines_planned(data, chunk_count=3)
+    assert res.n_structural > 0

@@ -107,8 +107,13 @@ def test_device_planner_matches_reference_loaders(ctx, c):
     data = case_bytes(c)
     d = torch.from_numpy(data.copy()).to("cuda") if data.size else None
     torch.cuda.synchronize()
+    ptr = d.data_ptr() if d is not None else 0
     for plan in c["plans"]:
-        if plan["mode"] != "count":
-            continue
-        got = ctx.plan_lines_count_device(d.data_ptr() if d is not None else 0, int(data.size), plan["n"])
-        assert_plan(got, plan, (c["name"], plan["n"]))
+        what = (c["name"], plan["mode"], plan["n"])
+        if plan["mode"] == "count":
+            got = ctx.plan_lines_count_device(ptr, int(data.size), plan["n"])
+        else:
+            limit = plan["n"] << 20 if plan["mode"] == "megabytes" else plan["n"]
+            got = ctx.plan_lines_bytes_device(ptr, int(data.size), limit)
+            assert plan["chunk_count"] == len(got), what
+        assert_plan(got, plan, what)
