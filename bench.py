@@ -321,6 +321,15 @@ def run_batch(args, local):
     ctx = cj.Context(local)
     ctx.stage_batch_packed(packed, sizes)
     best, tried = ctx.autotune(reps=2)
+    # the winner kept per GPU name and applied to a fresh context
+    import tempfile
+    with tempfile.TemporaryDirectory() as td:
+        tpath = os.path.join(td, "tuning.jsonl")
+        ctx.save_tuning(tpath)
+        tctx = cj.Context(local)
+        tctx.load_tuning(tpath)
+        persisted = tctx.get_tuning().as_dict()
+        tctx.close()
     ctx.run_graph()
     layout, status, S, depth, off = ctx.batch_layout()
     verdicts_ok = bool(((status != 0) == (kinds > 0)).all())
@@ -401,7 +410,9 @@ def run_batch(args, local):
         "speedup_device_vs_plain": round(plain_s / dev_s, 2),
         "verdicts_match_generator": verdicts_ok and plain_ok, "replay_results_identical": same,
         "gpu_launches_per_batch": int(launches), "graph": True,
-        "tuning": best.as_dict(), "tuning_candidates": len(tried),
+        "tuning": dict(best.as_dict(), pair_chunk_records=512),
+        "tuning_candidates": len(tried),
+        "tuning_persisted_and_reloaded": all(persisted[k] == v for k, v in best.as_dict().items() if k != "ms"),
         "generation_s": round(t_gen, 1),
     }
     ctx.close()

@@ -70,14 +70,14 @@ class Tuning(ctypes.Structure):
     """Launch shapes (cj_tuning): 0 = default."""
     _fields_ = [("region_kib", ctypes.c_int32), ("scan_blocks_per_sm", ctypes.c_int32),
                 ("emit_blocks_per_sm", ctypes.c_int32), ("pair_blocks", ctypes.c_int32),
-                ("pair_threads", ctypes.c_int32), ("stream_wave_mib", ctypes.c_int32),
-                ("ms", ctypes.c_float)]
+                ("pair_threads", ctypes.c_int32), ("prefetch_steps", ctypes.c_int32),
+                ("stream_wave_mib", ctypes.c_int32), ("ms", ctypes.c_float)]
 
     def as_dict(self):
         return {"region_kib": self.region_kib, "scan_blocks_per_sm": self.scan_blocks_per_sm,
                 "emit_blocks_per_sm": self.emit_blocks_per_sm, "pair_blocks": self.pair_blocks,
-                "pair_threads": self.pair_threads, "stream_wave_mib": self.stream_wave_mib,
-                "ms": round(float(self.ms), 4)}
+                "pair_threads": self.pair_threads, "prefetch_steps": self.prefetch_steps,
+                "stream_wave_mib": self.stream_wave_mib, "ms": round(float(self.ms), 4)}
 
 
 _lib: Optional[ctypes.CDLL] = None
@@ -153,6 +153,7 @@ _SIGNATURES = {
     "cj_context_span_ms": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
     "cj_host_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
     "cj_host_free": (None, [ctypes.c_void_p]),
+    "cj_host_pool_trim": (ctypes.c_size_t, []),
     "cj_load_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p),
                                     ctypes.POINTER(ctypes.c_size_t)]),
     "cj_plan_lines_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
@@ -165,6 +166,8 @@ _SIGNATURES = {
     "cj_plan_lines_bytes_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                                   ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
                                                   ctypes.POINTER(ctypes.c_size_t), ctypes.c_void_p]),
+    "cj_tuning_save": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    "cj_tuning_load": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     "cj_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "cj_last_status": (ctypes.c_int, []),
     "cj_last_error": (ctypes.c_char_p, []),
@@ -444,9 +447,10 @@ class Context:
 
     # ---- launch shapes -------------------------------------------------------------
     def set_tuning(self, region_kib: int = 0, scan_blocks_per_sm: int = 0, emit_blocks_per_sm: int = 0,
-                   pair_blocks: int = 0, pair_threads: int = 0, stream_wave_mib: int = 0) -> None:
+                   pair_blocks: int = 0, pair_threads: int = 0, prefetch_steps: int = 0,
+                   stream_wave_mib: int = 0) -> None:
         t = Tuning(region_kib, scan_blocks_per_sm, emit_blocks_per_sm, pair_blocks, pair_threads,
-                   stream_wave_mib, 0.0)
+                   prefetch_steps, stream_wave_mib, 0.0)
         _check(lib().cj_context_set_tuning(self._h, ctypes.byref(t)), "set_tuning")
 
     def get_tuning(self) -> Tuning:
@@ -454,15 +458,21 @@ class Context:
         _check(lib().cj_context_get_tuning(self._h, ctypes.byref(t)), "get_tuning")
         return t
 
+    def save_tuning(self, path: str) -> None:
+        _check(lib().cj_tuning_save(self._h, str(path).encode()), "save_tuning")
+
+    def load_tuning(self, path: str) -> None:
+        _check(lib().cj_tuning_load(self._h, str(path).encode()), "load_tuning")
+
     def autotune(self, reps: int = 3):
         """Times graph replays of the staged input for each candidate launch
         shape and keeps the fastest; returns (best, [tried])."""
         best = Tuning()
-        tried = (Tuning * 64)()
+        tried = (Tuning * 128)()
         n = ctypes.c_size_t()
-        _check(lib().cj_autotune_staged(self._h, reps, ctypes.byref(best), tried, 64, ctypes.byref(n)),
+        _check(lib().cj_autotune_staged(self._h, reps, ctypes.byref(best), tried, len(tried), ctypes.byref(n)),
                "autotune")
-        return best, [tried[i] for i in range(n.value)]
+        return best, [tried[i] for i in range(min(n.value, len(tried)))]
 
     def timing(self, enable: bool = True) -> None:
         _check(lib().cj_context_timing(self._h, int(enable)), "timing")

@@ -18,7 +18,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "cj_device.cuh"
@@ -38,6 +41,89 @@ struct DevBuf {
 };
 
 size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
+
+// Pinned host blocks handed out by the library (result buffers, cj_host_alloc)
+// are kept when freed and handed out again: pinning a large buffer costs far
+// more than copying into it, and a caller that parses file after file frees
+// and asks for buffers of about the same size each time.  A block is reused
+// for a request of at least half its size; kept blocks beyond kPinnedKeep
+// bytes are released, largest first.  Blocks the library did not hand out are
+// released with cudaFreeHost.
+constexpr size_t kPinnedKeep = 8ull << 30;
+struct PinnedPool {
+    std::mutex mu;
+    std::unordered_map<void*, size_t> live;       // handed out: size
+    std::multimap<size_t, void*> kept;            // freed, kept: size -> block
+    size_t kept_bytes = 0;
+};
+PinnedPool& pinned_pool()
+{
+    static PinnedPool* p = new PinnedPool();      // never destroyed: blocks may be freed at exit
+    return *p;
+}
+void* pinned_alloc(size_t bytes)
+{
+    PinnedPool& pp = pinned_pool();
+    bytes = std::max<size_t>(bytes, 1);
+    {
+        std::lock_guard<std::mutex> g(pp.mu);
+        auto it = pp.kept.lower_bound(bytes);
+        if (it != pp.kept.end() && it->first / 2 <= bytes) {
+            void* p = it->second;
+            pp.live[p] = it->first;
+            pp.kept_bytes -= it->first;
+            pp.kept.erase(it);
+            return p;
+        }
+    }
+    void* p = nullptr;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> g(pp.mu);
+    pp.live[p] = bytes;
+    return p;
+}
+void pinned_free(void* p)
+{
+    if (!p) return;
+    PinnedPool& pp = pinned_pool();
+    std::vector<void*> drop;
+    {
+        std::lock_guard<std::mutex> g(pp.mu);
+        auto it = pp.live.find(p);
+        if (it == pp.live.end()) {
+            drop.push_back(p);
+        } else {
+            pp.kept.emplace(it->second, p);
+            pp.kept_bytes += it->second;
+            pp.live.erase(it);
+            while (pp.kept_bytes > kPinnedKeep && !pp.kept.empty()) {
+                auto last = std::prev(pp.kept.end());
+                pp.kept_bytes -= last->first;
+                drop.push_back(last->second);
+                pp.kept.erase(last);
+            }
+        }
+    }
+    for (void* q : drop) cudaFreeHost(q);
+}
+size_t pinned_trim()
+{
+    PinnedPool& pp = pinned_pool();
+    std::vector<void*> drop;
+    size_t bytes = 0;
+    {
+        std::lock_guard<std::mutex> g(pp.mu);
+        for (auto& kv : pp.kept) drop.push_back(kv.second);
+        bytes = pp.kept_bytes;
+        pp.kept.clear();
+        pp.kept_bytes = 0;
+    }
+    for (void* q : drop) cudaFreeHost(q);
+    return bytes;
+}
 
 // recorded run: start, after the scan's tables, prefix and emit kernels, after
 // pair, after spine
@@ -153,6 +239,7 @@ struct cj_context {
     int tune_emit_per_sm = 0;
     uint32_t tune_pair_blocks = 0;
     uint32_t tune_pair_threads = 0;
+    uint32_t tune_prefetch_steps = 0;
     int tune_stream_wave_mib = 0;
     bool wave_stream = false;           // the waves of this run report to the host (streamed parse)
 };
@@ -390,6 +477,7 @@ cj_status enqueue(cj_context* ctx, bool graph)
     sp.input_wait_limit = ctx->input_wait_limit;
     sp.region_steps = ctx->run_region_steps;
     sp.sm_count = ctx->sm_count;
+    sp.prefetch_steps = ctx->tune_prefetch_steps;
     ScanShape shape{ctx->tune_tables_per_sm, ctx->tune_emit_per_sm};
     if (ctx->n_waves > 1) {
         // waves: each scans its regions from the previous wave's end value,
@@ -868,13 +956,13 @@ cj_status copy_result(cj_context* ctx, int64_t S, int32_t* out, size_t cap)
 cj_status to_result(cj_context* ctx, const cj_parse_info& info, cj_result* out)
 {
     int64_t S = info.n_structural;
-    int32_t* buf = nullptr;
-    CJ_CUDA(cudaMallocHost((void**)&buf, (size_t)(2 * S + 4) * sizeof(int32_t)));
+    int32_t* buf = static_cast<int32_t*>(pinned_alloc((size_t)(2 * S + 4) * sizeof(int32_t)));
+    if (!buf) return CJ_ERR_OUT_OF_MEMORY;
     cj_status st = copy_result(ctx, S, buf, (size_t)(2 * S + 4));
-    if (st) { cudaFreeHost(buf); return st; }
+    if (st) { pinned_free(buf); return st; }
     int64_t* seg_sizes = (int64_t*)malloc(sizeof(int64_t) * (ctx->n_segs ? ctx->n_segs : 1));
     if (!seg_sizes) {
-        cudaFreeHost(buf);
+        pinned_free(buf);
         return CJ_ERR_OUT_OF_MEMORY;
     }
     out->structural = buf;
@@ -1257,14 +1345,9 @@ cj_status cj_context_span_ms(cj_context* ctx, double* ms)
     return CJ_OK;
 }
 
-void* cj_host_alloc(size_t bytes)
-{
-    void* p = nullptr;
-    if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
-    return p;
-}
-
-void cj_host_free(void* p) { if (p) cudaFreeHost(p); }
+void* cj_host_alloc(size_t bytes) { return pinned_alloc(bytes); }
+void cj_host_free(void* p) { pinned_free(p); }
+size_t cj_host_pool_trim(void) { return pinned_trim(); }
 
 cj_status cj_context_reserve(cj_context* ctx, size_t max_bytes, size_t max_segments)
 {
@@ -1337,7 +1420,7 @@ cj_status cj_parse_lines_planned(cj_context* ctx, const uint8_t* host_data, size
 void cj_result_free(cj_result* res)
 {
     if (!res) return;
-    if (res->structural) cudaFreeHost(res->structural);
+    if (res->structural) pinned_free(res->structural);
     free(res->segment_sizes);
     memset(res, 0, sizeof(*res));
 }
@@ -1486,13 +1569,16 @@ cj_status cj_context_set_tuning(cj_context* ctx, const cj_tuning* t)
     const int eb = t ? std::max(0, t->emit_blocks_per_sm) : 0;
     const uint32_t pb = t ? (uint32_t)std::max(0, t->pair_blocks) : 0u;
     const uint32_t pt = t ? (uint32_t)std::max(0, t->pair_threads) : 0u;
+    const uint32_t pf = t ? (uint32_t)std::max(0, t->prefetch_steps) : 0u;
     if (pt && pt != 64 && pt != 128 && pt != 256) return CJ_ERR_INVALID_ARGUMENT;
+    if (pf && (pf < 2 || pf > 8)) return CJ_ERR_INVALID_ARGUMENT;
     if (rk && !region_steps_valid(rk)) return CJ_ERR_INVALID_ARGUMENT;
     ctx->tune_region_steps = rk;
     ctx->tune_tables_per_sm = tb;
     ctx->tune_emit_per_sm = eb;
     ctx->tune_pair_blocks = pb;
     ctx->tune_pair_threads = pt;
+    ctx->tune_prefetch_steps = pf;
     ctx->tune_stream_wave_mib = sw;
     ctx->graph_valid = false;
     if (ctx->staged && ctx->run_region_steps != region_steps(ctx)) {
@@ -1513,6 +1599,7 @@ cj_status cj_context_get_tuning(cj_context* ctx, cj_tuning* t)
     t->emit_blocks_per_sm = ctx->tune_emit_per_sm;
     t->pair_blocks = (int32_t)ctx->tune_pair_blocks;
     t->pair_threads = (int32_t)pair_threads(ctx);
+    t->prefetch_steps = ctx->tune_prefetch_steps ? (int32_t)ctx->tune_prefetch_steps : 4;
     t->stream_wave_mib = ctx->tune_stream_wave_mib;
     t->ms = 0.f;
     return CJ_OK;
@@ -1525,23 +1612,26 @@ cj_status cj_autotune_staged(cj_context* ctx, int32_t reps, cj_tuning* best, cj_
     if (!ctx->staged) return finish(CJ_ERR_NOT_STAGED);
     CJ_CUDA(cudaSetDevice(ctx->device));
     const uint32_t sm = (uint32_t)ctx->sm_count;
-    // region size (4, 8, 16 KiB) x resident scan blocks per SM (as many as
-    // fit, or 2) x pairing threads per block x pairing blocks
+    // region size (4, 8, 16 KiB) x L2 prefetch distance (2, 4, 8 steps) x
+    // resident scan blocks per SM (as many as fit, or 2) x pairing threads
+    // per block x pairing blocks
     std::vector<cj_tuning> cand;
     for (int rk : {4, 8, 16})
-        for (int tb : {0, 2})
-            for (int pt : {128, 256})
-                for (uint32_t pb : {0u, sm * 4}) {
-                    cj_tuning t;
-                    t.region_kib = rk;
-                    t.scan_blocks_per_sm = tb;
-                    t.emit_blocks_per_sm = tb;
-                    t.pair_threads = pt;
-                    t.pair_blocks = (int32_t)pb;
-                    t.stream_wave_mib = ctx->tune_stream_wave_mib;
-                    t.ms = 0.f;
-                    cand.push_back(t);
-                }
+        for (int pf : {2, 4, 8})
+            for (int tb : {0, 2})
+                for (int pt : {128, 256})
+                    for (uint32_t pb : {0u, sm * 4}) {
+                        cj_tuning t;
+                        t.region_kib = rk;
+                        t.prefetch_steps = pf;
+                        t.scan_blocks_per_sm = tb;
+                        t.emit_blocks_per_sm = tb;
+                        t.pair_threads = pt;
+                        t.pair_blocks = (int32_t)pb;
+                        t.stream_wave_mib = ctx->tune_stream_wave_mib;
+                        t.ms = 0.f;
+                        cand.push_back(t);
+                    }
     cudaEvent_t e0, e1;
     CJ_CUDA(cudaEventCreate(&e0));
     CJ_CUDA(cudaEventCreate(&e1));
@@ -1571,6 +1661,89 @@ cj_status cj_autotune_staged(cj_context* ctx, int32_t reps, cj_tuning* best, cj_
     if (st) return finish(st);
     if (best) *best = win;
     return finish(CJ_OK);
+}
+
+namespace {
+
+const char* kTuningKeys[] = {"region_kib", "scan_blocks_per_sm", "emit_blocks_per_sm", "pair_blocks",
+                             "pair_threads", "prefetch_steps", "stream_wave_mib"};
+
+int32_t* tuning_field(cj_tuning& t, int i)
+{
+    int32_t* f[] = {&t.region_kib, &t.scan_blocks_per_sm, &t.emit_blocks_per_sm, &t.pair_blocks,
+                    &t.pair_threads, &t.prefetch_steps, &t.stream_wave_mib};
+    return f[i];
+}
+
+std::string gpu_name(int device)
+{
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) {
+        cudaGetLastError();
+        return "unknown";
+    }
+    std::string n = prop.name;
+    for (char& c : n)
+        if (c == '"' || c == '\\' || c == '\n') c = ' ';
+    return n;
+}
+
+// the lines of a tuning file, without the one for `gpu`
+std::vector<std::string> tuning_lines_except(const char* path, const std::string& gpu, std::string* mine)
+{
+    std::vector<std::string> keep;
+    FILE* f = fopen(path, "r");
+    if (!f) return keep;
+    const std::string key = "{\"gpu\": \"" + gpu + "\"";
+    char buf[1024];
+    while (fgets(buf, sizeof buf, f)) {
+        std::string line(buf);
+        while (!line.empty() && (line.back() == '\n' || line.back() == '\r')) line.pop_back();
+        if (line.empty()) continue;
+        if (line.compare(0, key.size(), key) == 0) {
+            if (mine) *mine = line;
+        } else {
+            keep.push_back(line);
+        }
+    }
+    fclose(f);
+    return keep;
+}
+
+}  // namespace
+
+cj_status cj_tuning_save(cj_context* ctx, const char* path)
+{
+    if (!ctx || !path) return CJ_ERR_INVALID_ARGUMENT;
+    cj_tuning t;
+    cj_context_get_tuning(ctx, &t);
+    const std::string gpu = gpu_name(ctx->device);
+    std::vector<std::string> lines = tuning_lines_except(path, gpu, nullptr);
+    std::string mine = "{\"gpu\": \"" + gpu + "\"";
+    for (int i = 0; i < 7; i++) mine += std::string(", \"") + kTuningKeys[i] + "\": " + std::to_string(*tuning_field(t, i));
+    mine += "}";
+    lines.push_back(mine);
+    FILE* f = fopen(path, "w");
+    if (!f) return CJ_ERR_INVALID_ARGUMENT;
+    for (const std::string& l : lines) fprintf(f, "%s\n", l.c_str());
+    return fclose(f) == 0 ? CJ_OK : CJ_ERR_INVALID_ARGUMENT;
+}
+
+cj_status cj_tuning_load(cj_context* ctx, const char* path)
+{
+    if (!ctx || !path) return CJ_ERR_INVALID_ARGUMENT;
+    std::string mine;
+    tuning_lines_except(path, gpu_name(ctx->device), &mine);
+    if (mine.empty()) return CJ_ERR_INVALID_ARGUMENT;      // no entry for this GPU
+    cj_tuning t;
+    memset(&t, 0, sizeof t);
+    for (int i = 0; i < 7; i++) {
+        const std::string k = std::string("\"") + kTuningKeys[i] + "\": ";
+        const size_t at = mine.find(k);
+        if (at == std::string::npos) return CJ_ERR_INVALID_ARGUMENT;
+        *tuning_field(t, i) = (int32_t)strtol(mine.c_str() + at + k.size(), nullptr, 10);
+    }
+    return cj_context_set_tuning(ctx, &t);
 }
 
 cj_status cj_run_staged_starved(cj_context* ctx, uint32_t polls, cj_parse_info* info)

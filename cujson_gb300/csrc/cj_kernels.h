@@ -36,6 +36,7 @@ struct ScanParams {
     uint32_t input_wait_limit;  // polls before a wait for input gives up (0: default)
     int region_steps;           // 1 KiB steps per region: 4, 8 or 16
     int sm_count;
+    uint32_t prefetch_steps;    // the table kernel's L2 prefetch distance in steps (0: 4)
     // A wave: the launch scans regions [r_begin, r_end) only (r_end 0: all),
     // starting from the value in carry_in (nullptr: the document start) and
     // leaving the value after r_end - 1 in carry_out (nullptr: not kept);

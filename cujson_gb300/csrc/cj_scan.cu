@@ -58,15 +58,16 @@ constexpr int kThreads = 256;                  // 8 warps per block (tables, emi
 constexpr int kWarpsPerBlock = kThreads / 32;
 constexpr uint32_t kInputWaitLimit = 1u << 22; // polls (>= 256 ns each) for input bytes
 // how many steps ahead of the current one the table kernel asks for a step to
-// be brought into L2 (the register load is one step ahead)
+// be brought into L2 when ScanParams::prefetch_steps is 0 (the register load
+// is one step ahead)
 #ifndef CJ_L2_AHEAD
 #define CJ_L2_AHEAD 4
 #endif
 constexpr int kL2Ahead = CJ_L2_AHEAD;
-// steps held in registers ahead of the current one (1 or 2)
-#ifndef CJ_REG_AHEAD
-#define CJ_REG_AHEAD 1
-#endif
+__device__ __forceinline__ int l2_ahead(const ScanParams& P) {
+    return P.prefetch_steps ? (int)P.prefetch_steps : kL2Ahead;
+}
+
 // resident blocks per SM the table and emit kernels are compiled for (their
 // register budgets: 65536 / (256 x blocks))
 #ifndef CJ_TABLES_MIN_BLOCKS
@@ -189,9 +190,6 @@ constexpr uint32_t kNoRegion = 0xFFFFFFFFu;
 
 struct Stream {
     uint4 a, b;            // the lane's 32 bytes of the next step
-#if CJ_REG_AHEAD > 1
-    uint4 a2, b2;          // and of the step after it, when in the same region
-#endif
     uint32_t c;            // the region of the next step (kNoRegion: none)
     uint32_t ahead;        // lane 0: the ticket drawn for the region after it
     int j, n;              // that step's number in its region, the region's step count
@@ -228,13 +226,7 @@ __device__ __forceinline__ void stream_load(Stream& st) {
     st.a = __ldcg(p);
     st.b = __ldcg(p + 1);
 }
-#if CJ_REG_AHEAD > 1
-__device__ __forceinline__ void stream_load2(Stream& st) {
-    const uint4* p = reinterpret_cast<const uint4*>(st.src + (size_t)(st.j + 1) * kStepBytes);
-    st.a2 = __ldcg(p);
-    st.b2 = __ldcg(p + 1);
-}
-#endif
+
 
 // point the stream at step 0 of cursor c's region and load it (after the wait
 // for its input bytes of an overlapped parse; a wait that gives up ends the
@@ -253,11 +245,8 @@ __device__ __forceinline__ void stream_enter(const ScanParams& P, Stream& st, ui
     st.n = (g.len + kStepBytes - 1) / kStepBytes;
     st.src = g.base + g.off + lane * kBytesPerThread;
     stream_load(st);
-#if CJ_REG_AHEAD > 1
-    if (st.n > 1) stream_load2(st);
-#endif
-#pragma unroll
-    for (int k = CJ_REG_AHEAD; k < kL2Ahead; k++)
+    const int ahead = l2_ahead(P);
+    for (int k = 1; k < ahead; k++)
         if (k < st.n) prefetch_l2(st.src + (size_t)k * kStepBytes);
 }
 
@@ -271,14 +260,9 @@ __device__ __forceinline__ void stream_take(const ScanParams& P, Stream& st, uin
     hi = st.b;
     if (st.c == kNoRegion) return;
     if (++st.j < st.n) {
-#if CJ_REG_AHEAD > 1
-        st.a = st.a2;
-        st.b = st.b2;
-        if (st.j + 1 < st.n) stream_load2(st);
-#else
         stream_load(st);
-#endif
-        if (st.j + kL2Ahead - 1 < st.n) prefetch_l2(st.src + (size_t)(st.j + kL2Ahead - 1) * kStepBytes);
+        const int ahead = l2_ahead(P);
+        if (st.j + ahead - 1 < st.n) prefetch_l2(st.src + (size_t)(st.j + ahead - 1) * kStepBytes);
     } else {
         stream_enter<R>(P, st, walk.region(st.ahead), lane, walk);
     }

@@ -269,6 +269,8 @@ typedef struct cj_tuning {
     int32_t emit_blocks_per_sm;  /* emit kernels (0: as many as fit) */
     int32_t pair_blocks;         /* pairing grid (0: sized to the bracket count) */
     int32_t pair_threads;        /* pairing threads per block: 64, 128 or 256 (0: 256) */
+    int32_t prefetch_steps;      /* how many 1 KiB steps ahead the scan asks for input to be
+                                    brought into L2: 2..8 (0: 4); the staging depth */
     int32_t stream_wave_mib;     /* cj_parse_into of >= 2 waves of pinned input into pinned
                                     output: waves of this many MiB whose positions are copied
                                     back while later input arrives (0: 128; -1: not streamed) */
@@ -278,6 +280,12 @@ cj_status cj_context_set_tuning(cj_context* ctx, const cj_tuning* tuning);   /* 
 cj_status cj_context_get_tuning(cj_context* ctx, cj_tuning* tuning);
 cj_status cj_autotune_staged(cj_context* ctx, int32_t reps, cj_tuning* best, cj_tuning* tried,
                              size_t tried_cap, size_t* n_tried);
+/* The context's tuning kept in a file of one JSON line per GPU name
+ * ({"gpu": "<name>", "region_kib": .., ...}): cj_tuning_save writes (or
+ * replaces) this GPU's line, cj_tuning_load applies it (CJ_ERR_INVALID_ARGUMENT
+ * when the file has no line for this GPU; the tuning is then unchanged). */
+cj_status cj_tuning_save(cj_context* ctx, const char* path);
+cj_status cj_tuning_load(cj_context* ctx, const char* path);
 
 /* ---- serving: a request loop with continuous batching -------------------------
  * No counterpart in the reference.  A server owns `slots` contexts on one
@@ -340,10 +348,16 @@ cj_status cj_context_scan_phase_ms(cj_context* ctx, double* tables_ms, double* p
                                    double* emit_ms, int64_t* runs);
 /* Milliseconds from the first recorded run's start to the last one's end. */
 cj_status cj_context_span_ms(cj_context* ctx, double* ms);
-/* Pinned host memory (cudaMallocHost / cudaFreeHost) for callers without the
- * CUDA runtime headers. */
+/* Pinned host memory for callers without the CUDA runtime headers.  Blocks
+ * the library hands out (these, and the result buffers of cj_parse_standard /
+ * cj_parse_lines) are kept when freed with cj_host_free / cj_result_free and
+ * handed out again for a request of at least half their size, since pinning a
+ * large buffer costs far more than filling it; up to 8 GiB is kept.
+ * cj_host_pool_trim releases every kept block and returns their bytes.  A
+ * block may also be released with cudaFreeHost. */
 void* cj_host_alloc(size_t bytes);
 void  cj_host_free(void* p);
+size_t cj_host_pool_trim(void);
 
 /* ---- loaders and JSON-Lines chunk planning ----------------------------------
  * cj_load_file reads a whole file into pinned host memory (free it with

@@ -93,6 +93,27 @@ def test_autotune_keeps_results(cj, oracle, ctx):
     assert min(t.ms for t in tried) == pytest.approx(best.ms)
     ctx.run_graph()
     np.testing.assert_array_equal(ctx.batch_layout()[0], want)
+    assert {t.prefetch_steps for t in tried} == {2, 4, 8} and {t.region_kib for t in tried} == {4, 8, 16}
+    # the winner kept in a file keyed by GPU name, and applied again
+    import tempfile, os
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "tuning.jsonl")
+        with open(path, "w") as f:
+            f.write('{"gpu": "another GPU", "region_kib": 4}\n')
+        ctx.save_tuning(path)
+        ctx.set_tuning()
+        ctx.load_tuning(path)
+        got = ctx.get_tuning()
+        for k in ("region_kib", "scan_blocks_per_sm", "pair_blocks", "pair_threads", "prefetch_steps"):
+            assert getattr(got, k) == getattr(best, k), k
+        lines = open(path).read().splitlines()
+        assert len(lines) == 2 and lines[0].startswith('{"gpu": "another GPU"')
+        with open(path, "w") as f:
+            f.write('{"gpu": "another GPU", "region_kib": 4}\n')
+        with pytest.raises(cj.CujsonError):
+            ctx.load_tuning(path)
+    ctx.run_graph()
+    np.testing.assert_array_equal(ctx.batch_layout()[0], want)
     ctx.set_tuning()   # back to defaults for the other tests
 
 

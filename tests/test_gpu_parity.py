@@ -201,3 +201,16 @@ def test_input_wait_timeout_reported(cj, ctx, oracle):
     st2, res = ctx.try_parse(d)
     assert st2 == cj.OK
     np.testing.assert_array_equal(res.buffer, oracle.parse(d).reference_layout())
+
+
+def test_result_buffers_kept_and_reused(cj, ctx, oracle):
+    """A freed result buffer is kept pinned and handed out again (pinning a
+    large buffer costs more than filling it); the results stay exact."""
+    d = synth.synth_document(0x9001, 8 << 20)
+    ref = oracle.parse(d)
+    cj.lib().cj_host_pool_trim()
+    for _ in range(3):
+        assert_same(ctx.parse_standard_json(d), ref)
+    kept = cj.lib().cj_host_pool_trim()
+    assert kept >= 4 * (2 * ref.n_structural + 4)
+    assert cj.lib().cj_host_pool_trim() == 0
