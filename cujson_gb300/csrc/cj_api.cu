@@ -140,7 +140,6 @@ struct cj_context {
     DevBuf<int32_t> pos, pair;
     DevBuf<uint2> brk;
     DevBuf<uint4> rtab, bagg;           // region and prefix-block transfer tables
-    DevBuf<uint4> mid;                  // per region: its first half's counts
     DevBuf<uint4> work;                 // the emit kernel's work items (2 per region)
     DevBuf<uint4> masks;                // per region step: mask words for the emit kernel
     DevBuf<Segment> segs;
@@ -287,7 +286,6 @@ cj_status reserve_regions(cj_context* ctx, size_t regions)
 {
     cj_status st;
     if ((st = ensure(ctx, ctx->rtab, regions * 4))) return st;
-    if ((st = ensure(ctx, ctx->mid, regions))) return st;
     if ((st = ensure(ctx, ctx->work, regions * 2))) return st;
     if ((st = ensure(ctx, ctx->region_seg, regions))) return st;
     if ((st = ensure(ctx, ctx->bagg, prefix_blocks(regions) * 4))) return st;
@@ -470,7 +468,6 @@ cj_status enqueue(cj_context* ctx, bool graph)
     sp.brk_cap = ctx->brk.cap;
     sp.rtab = ctx->rtab.p;
     sp.bagg = ctx->bagg.p;
-    sp.mid = ctx->mid.p;
     sp.masks = ctx->masks.p;
     sp.work = ctx->work.p;
     sp.ctrl = ctx->d_ctrl;
@@ -1258,7 +1255,7 @@ void cj_context_destroy(cj_context* ctx)
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     release(ctx->in); release(ctx->pos); release(ctx->pair); release(ctx->brk);
-    release(ctx->rtab); release(ctx->bagg); release(ctx->mid); release(ctx->work); release(ctx->masks);
+    release(ctx->rtab); release(ctx->bagg); release(ctx->work); release(ctx->masks);
     release(ctx->segs); release(ctx->seg_out); release(ctx->region_seg);
     release(ctx->spine); release(ctx->cinfo); release(ctx->tree);
     release(ctx->seg_err); release(ctx->seg_depth); release(ctx->rchunk_off);

@@ -21,8 +21,6 @@ struct ScanParams {
     uint64_t brk_cap;           // entries of brk
     uint4* rtab;                // 4 entries per region: transfer tables
     uint4* bagg;                // 4 per block of kPrefixPerBlock regions: block tables
-    uint4* mid;                 // per region: its first half's counts (structurals, brackets,
-                                // opens; low 16 bits outside strings, high 16 all)
     uint4* masks;               // per region and step, 32 lanes: the 4 mask words of the steps
                                 // that hold structural characters (masks_cap(...) entries)
     uint4* work;                // 2 per region with structurals to emit (ctrl->n_work of them):

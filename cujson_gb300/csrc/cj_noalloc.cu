@@ -49,7 +49,6 @@ struct alignas(256) Scratch {
     alignas(256) int32_t pair[kScap];
     alignas(256) uint2 brk[kScap];
     alignas(256) uint4 rtab[kRegions * 4];
-    alignas(256) uint4 mid[kRegions];
     alignas(256) uint4 bagg[kPrefixBlocks * 4];
     alignas(256) uint4 work[kRegions * 2];
     alignas(256) uint4 masks[kRegions * kRegionSteps * 32];
@@ -205,7 +204,6 @@ cj_status parse_noalloc(const uint8_t* d_data, size_t size, int32_t* d_out, size
     sp.brk_cap = kScap;
     sp.rtab = s->rtab;
     sp.bagg = s->bagg;
-    sp.mid = s->mid;
     sp.masks = s->masks;
     sp.work = s->work;
     sp.ctrl = &s->ctrl;

@@ -322,7 +322,7 @@ __device__ __forceinline__ void warp_reduce_tab(Ent t[4], int lane) {
 // inside strings.  The steps come from the warp's stream `st`.
 template <bool LINES, int R, typename Walk>
 __device__ __forceinline__ void region_table(const ScanParams& P, const Region& g, uint4* out, uint4* mout,
-                                             uint4* mid_out, int lane, uint32_t lt, Stream& st, const Walk& walk)
+                                             int lane, uint32_t lt, Stream& st, const Walk& walk)
 {
     const int nsteps = (g.len + kStepBytes - 1) / kStepBytes;
     // the 4 bytes before the region (their UTF-8 leads carry in): loaded now,
@@ -336,9 +336,7 @@ __device__ __forceinline__ void region_table(const ScanParams& P, const Region& 
     // per lane, two counts per register (low half: outside strings for an entry
     // outside one; high half: all): structurals, brackets, opens (<= 512 each)
     uint32_t n_c = 0, n_k = 0, n_o = 0;
-    uint32_t h_c = 0, h_k = 0, h_o = 0;    // the same for the region's first half
     for (int j = 0; j < nsteps; j++) {
-        if (j == R / 2) { h_c = n_c; h_k = n_k; h_o = n_o; }
         uint4 lo, hi;
         stream_take<R>(P, st, lo, hi, lane, walk);
         const int step_len = min(kStepBytes, g.len - j * kStepBytes);
@@ -432,13 +430,6 @@ __device__ __forceinline__ void region_table(const ScanParams& P, const Region& 
     const int32_t K0 = (int32_t)__reduce_add_sync(FULL, n_k & 0xFFFFu), Kt = (int32_t)__reduce_add_sync(FULL, n_k >> 16);
     const int32_t O0 = (int32_t)__reduce_add_sync(FULL, n_o & 0xFFFFu), Ot = (int32_t)__reduce_add_sync(FULL, n_o >> 16);
     const int32_t D0 = 2 * O0 - K0, Dt = 2 * Ot - Kt;
-    // the first half's counts (both halves' of a region of at most half the
-    // steps), for an emit that cuts the region in two
-    if (nsteps <= R / 2) { h_c = n_c; h_k = n_k; h_o = n_o; }
-    const uint32_t H_c = __reduce_add_sync(FULL, h_c & 0xFFFFu) | (__reduce_add_sync(FULL, h_c >> 16) << 16);
-    const uint32_t H_k = __reduce_add_sync(FULL, h_k & 0xFFFFu) | (__reduce_add_sync(FULL, h_k >> 16) << 16);
-    const uint32_t H_o = __reduce_add_sync(FULL, h_o & 0xFFFFu) | (__reduce_add_sync(FULL, h_o >> 16) << 16);
-    if (lane == 4) *mid_out = make_uint4(H_c, H_k, H_o, 0u);
     if (lane < 4) {
         // a segment's first region is entered outside strings at depth 0 whatever
         // came before: every entry state reads as state 0, with the reset bits
@@ -471,8 +462,8 @@ __global__ void __launch_bounds__(kThreads, kTablesMinBlocks) scan_tables(ScanPa
         if (P.ready && aborted(P.ctrl)) break;     // the wait for input bytes gave up
         Region g;
         region_of(P, r, R * kStepBytes, g);
-        region_table<LINES, R>(P, g, P.rtab + (size_t)r * 4, P.masks + (size_t)r * R * 32 + lane, P.mid + r, lane,
-                               lt, st, walk);
+        region_table<LINES, R>(P, g, P.rtab + (size_t)r * 4, P.masks + (size_t)r * R * 32 + lane, lane, lt, st,
+                               walk);
     }
 }
 
@@ -937,44 +928,18 @@ __global__ void __launch_bounds__(kThreads, kEmitMinBlocks) scan_emit(ScanParams
     // the first item by warp number, the later ones (when there are more
     // items than warps) from a ticket counter, drawn one item ahead, so that
     // warps with sparse regions take more
-    // few items for the grid (a sparse document): each region in two halves,
-    // one warp each, the second half's entry value from the first half's
-    // counts that the table kernel kept
-    const bool halves = n <= 2u * nw;
-    const uint32_t items = halves ? 2u * n : n;
-    const bool more = items > nw;
+    const bool more = n > nw;
     uint32_t i = blockIdx.x * kWarpsPerBlock + warp;
-    while (i < items) {
-        uint32_t t = items;
+    while (i < n) {
+        uint32_t t = n;
         if (more && lane == 0) t = atomicAdd(ticket, 1u);
-        const uint32_t wi = halves ? i >> 1 : i;
-        const uint4 a = __ldcg(P.work + 2 * (size_t)wi), b = __ldcg(P.work + 2 * (size_t)wi + 1);
-        const uint32_t steps = a.y & 0xFFFFu, flip = (a.y >> 31) ? FULL : 0u;
-        const uint4* mk = P.masks + (size_t)a.x * R * 32 + lane;
+        const uint4 a = __ldcg(P.work + 2 * (size_t)i), b = __ldcg(P.work + 2 * (size_t)i + 1);
         Region g;
         region_of(P, a.x, R * kStepBytes, g);
-        if (!halves) {
-            emit_region(P, g, mk, steps, flip, a.z, a.w, (int32_t)b.x, s_stage[warp], b.y, b.z, (int32_t)b.w,
-                        lane);
-        } else {
-            const uint32_t low = (1u << (R / 2)) - 1u;
-            const uint32_t mine = (i & 1u) ? steps & ~low : steps & low;
-            if (mine) {
-                // the first half's counts outside strings for this entry state
-                const uint4 h = __ldcg(P.mid + a.x);
-                const uint32_t hc = flip ? (h.x >> 16) - (h.x & 0xFFFFu) : (h.x & 0xFFFFu);
-                const uint32_t hk = flip ? (h.y >> 16) - (h.y & 0xFFFFu) : (h.y & 0xFFFFu);
-                const uint32_t ho = flip ? (h.z >> 16) - (h.z & 0xFFFFu) : (h.z & 0xFFFFu);
-                const uint32_t ms = a.z + hc, mk_ = a.w + hk;
-                const int32_t md = (int32_t)b.x + 2 * (int32_t)ho - (int32_t)hk;
-                if (i & 1u)
-                    emit_region(P, g, mk, mine, flip, ms, mk_, md, s_stage[warp], b.y, b.z, (int32_t)b.w, lane);
-                else
-                    emit_region(P, g, mk, mine, flip, a.z, a.w, (int32_t)b.x, s_stage[warp], ms, mk_, md, lane);
-            }
-        }
+        emit_region(P, g, P.masks + (size_t)a.x * R * 32 + lane, a.y & 0xFFFFu, (a.y >> 31) ? FULL : 0u, a.z, a.w,
+                    (int32_t)b.x, s_stage[warp], b.y, b.z, (int32_t)b.w, lane);
         t = __shfl_sync(FULL, t, 0);
-        i = (t < items) ? nw + t : items;
+        i = (t < n) ? nw + t : n;
     }
 }
 

@@ -108,7 +108,6 @@ int run(const uint8_t* data, const size_t* sizes, size_t n, bool lines, bool bat
     std::copy(region_seg.begin(), region_seg.end(), d_region_seg);
     uint4* rtab = galloc<uint4>((size_t)regions * 4);
     uint4* bagg = galloc<uint4>(prefix_blocks(regions) * 4);
-    uint4* mid = galloc<uint4>(std::max<size_t>(regions, 1));
     uint4* work = galloc<uint4>((size_t)regions * 2);
     uint4* masks = galloc<uint4>((size_t)regions * region_steps * 32);
     Ctrl* ctrl = galloc<Ctrl>(1);
@@ -140,7 +139,6 @@ int run(const uint8_t* data, const size_t* sizes, size_t n, bool lines, bool bat
     sp.brk_cap = b_cap;
     sp.rtab = rtab;
     sp.bagg = bagg;
-    sp.mid = mid;
     sp.masks = masks;
     sp.work = work;
     sp.ctrl = ctrl;
