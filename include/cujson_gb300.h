@@ -118,7 +118,7 @@ cj_status cj_parse_lines(cj_context* ctx, const uint8_t* const* chunks,
  * scan of loadJSONLines_chunkCount / _chunkSizeBytes, cujson/load_file.cu:
  * 71-78 and :141-173, followed by parse_json_lines).  chunk_count != 0: the
  * plan of cj_plan_lines_count (newlines counted per 64 KiB block on the device
- * as each 64 MiB piece of the copy lands); else the plan of
+ * as each 128 MiB piece of the copy lands); else the plan of
  * cj_plan_lines_bytes with `chunk_bytes`.  The result, segment sizes
  * included, is that of planning the buffer on the host and calling
  * cj_parse_lines; a plan with an empty chunk is refused with
