@@ -66,6 +66,14 @@ class _Result(ctypes.Structure):
                 ("segment_sizes", ctypes.POINTER(ctypes.c_int64))]
 
 
+class ValueCounts(ctypes.Structure):
+    """cj_value_counts: slots, and slots of each CJ_VAL_* type."""
+    _fields_ = [("n_slots", ctypes.c_int64), ("by_type", ctypes.c_int64 * 8)]
+
+
+VAL_NONE, VAL_STRING, VAL_INT, VAL_DOUBLE, VAL_TRUE, VAL_FALSE, VAL_NULL, VAL_INVALID = range(8)
+
+
 class Tuning(ctypes.Structure):
     """Launch shapes (cj_tuning): 0 = default."""
     _fields_ = [("region_kib", ctypes.c_int32), ("scan_blocks_per_sm", ctypes.c_int32),
@@ -166,6 +174,12 @@ _SIGNATURES = {
     "cj_plan_lines_bytes_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                                   ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
                                                   ctypes.POINTER(ctypes.c_size_t), ctypes.c_void_p]),
+    "cj_decode_values": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "cj_context_staged_bytes": (ctypes.c_size_t, [ctypes.c_void_p]),
+    "cj_values_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p]),
+    "cj_copy_values": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t]),
     "cj_tuning_save": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     "cj_tuning_load": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     "cj_status_string": (ctypes.c_char_p, [ctypes.c_int]),
@@ -457,6 +471,23 @@ class Context:
         t = Tuning()
         _check(lib().cj_context_get_tuning(self._h, ctypes.byref(t)), "get_tuning")
         return t
+
+    def decode_values(self):
+        """cj_decode_values on the staged result, copied out: (types uint8[S+1],
+        nums uint64[S+1], lens uint32[S+1], strings uint8[n_bytes], counts
+        by type).  Slot 0 is the text before the first structural, slot i the
+        text after structural i."""
+        counts = ValueCounts()
+        _check(lib().cj_decode_values(self._h, ctypes.byref(counts)), "decode_values")
+        n = int(counts.n_slots)
+        types = np.zeros(n, np.uint8)
+        nums = np.zeros(n, np.uint64)
+        lens = np.zeros(n, np.uint32)
+        nbytes = int(lib().cj_context_staged_bytes(self._h))
+        strings = np.zeros(max(1, nbytes), np.uint8)
+        _check(lib().cj_copy_values(self._h, types.ctypes.data, nums.ctypes.data, lens.ctypes.data, n,
+                                    strings.ctypes.data, strings.size), "copy_values")
+        return types, nums, lens, strings, [int(x) for x in counts.by_type]
 
     def save_tuning(self, path: str) -> None:
         _check(lib().cj_tuning_save(self._h, str(path).encode()), "save_tuning")

@@ -57,7 +57,7 @@ def _stale(obj: Path, src: Path, newest_header: float) -> bool:
 
 def _compile(src: Path) -> tuple[Path, str]:
     obj = BUILD / (src.stem + ".o")
-    cmd = [_nvcc(), *ARCH, *NVCC_FLAGS, f"-I{INCLUDE}", f"-I{CSRC}", "-c", str(src), "-o", str(obj)]
+    cmd = [_nvcc(), *ARCH, *NVCC_FLAGS, f"-I{INCLUDE}", f"-I{CSRC}", f"-I{BUILD}", "-c", str(src), "-o", str(obj)]
     if src.suffix == ".cpp":
         cmd[1:1] = ["-x", "c++"]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -69,6 +69,14 @@ def _compile(src: Path) -> tuple[Path, str]:
 def build(force: bool = False, verbose: bool = False) -> Path:
     """Compile and link the library; returns its path."""
     BUILD.mkdir(parents=True, exist_ok=True)
+    # the value decoder's table of powers of five (generated, not committed)
+    pow5 = BUILD / "cj_pow5.inc"
+    if force or not pow5.exists():
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("cj_pow5_table", PKG / "pow5_table.py")
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.write(pow5)
     newest_header = max((h.stat().st_mtime for h in _headers()), default=0.0)
     srcs = _sources()
     todo = [s for s in srcs if force or _stale(BUILD / (s.stem + ".o"), s, newest_header)]

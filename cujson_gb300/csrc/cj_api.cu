@@ -223,6 +223,14 @@ struct cj_context {
     std::vector<cudaEvent_t> wave_ev;
     cudaEvent_t ev_d2h = nullptr;
 
+    // value decoding over the staged result (cj_decode_values)
+    DevBuf<uint8_t> val_type, val_str;
+    DevBuf<uint64_t> val_num;
+    DevBuf<uint32_t> val_len, val_long;
+    DevBuf<unsigned long long> val_counts;
+    DevBuf<uint64_t> pow5;
+    uint64_t val_slots = 0;             // slots of the last decode (0: none)
+
     // queries over a staged JSON-Lines result
     DevBuf<unsigned long long> q_count;
     DevBuf<long long> q_out;
@@ -1233,7 +1241,7 @@ cj_status cj_context_create(int device, cj_context** out)
         // every kernel an overlapped run launches behind a waiting scan
         cudaFuncAttributes a;
         if (preload_scan_kernels() != cudaSuccess || preload_pair_kernels() != cudaSuccess ||
-            preload_batch_kernels() != cudaSuccess ||
+            preload_batch_kernels() != cudaSuccess || preload_value_kernels() != cudaSuccess ||
             cudaFuncGetAttributes(&a, (const void*)mark_ready) != cudaSuccess) {
             cj_context_destroy(ctx);
             return CJ_ERR_CUDA;
@@ -1268,6 +1276,8 @@ void cj_context_destroy(cj_context* ctx)
     release(ctx->seg_err); release(ctx->seg_depth); release(ctx->rchunk_off);
     release(ctx->layout_off); release(ctx->layout); release(ctx->pack); release(ctx->pack_off);
     release(ctx->q_count); release(ctx->q_out);
+    release(ctx->val_type); release(ctx->val_str); release(ctx->val_num); release(ctx->val_len);
+    release(ctx->val_long); release(ctx->val_counts); release(ctx->pow5);
     release(ctx->plan_counts); release(ctx->plan_req); release(ctx->plan_pos); release(ctx->plan_bounds);
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
@@ -1367,6 +1377,7 @@ cj_status cj_context_reserve(cj_context* ctx, size_t max_bytes, size_t max_segme
 void* cj_context_stream(cj_context* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 int64_t cj_context_launch_count(cj_context* ctx) { return ctx ? ctx->launches : 0; }
 size_t cj_context_device_bytes(cj_context* ctx) { return ctx ? ctx->dev_bytes : 0; }
+size_t cj_context_staged_bytes(cj_context* ctx) { return (ctx && ctx->staged) ? ctx->n_bytes : 0; }
 
 cj_context* cj_default_context(void)
 {
@@ -1751,6 +1762,94 @@ cj_status cj_tuning_load(cj_context* ctx, const char* path)
         *tuning_field(t, i) = (int32_t)strtol(mine.c_str() + at + k.size(), nullptr, 10);
     }
     return cj_context_set_tuning(ctx, &t);
+}
+
+static_assert(CJ_VAL_NONE == kValNone && CJ_VAL_STRING == kValString && CJ_VAL_INT == kValInt &&
+                  CJ_VAL_DOUBLE == kValDouble && CJ_VAL_TRUE == kValTrue && CJ_VAL_FALSE == kValFalse &&
+                  CJ_VAL_NULL == kValNull && CJ_VAL_INVALID == kValInvalid &&
+                  CJ_VAL_TYPES == kValTypes,
+              "value types of the C ABI and the kernels");
+
+cj_status cj_decode_values(cj_context* ctx, cj_value_counts* counts)
+{
+    if (!ctx) return CJ_ERR_INVALID_ARGUMENT;
+    if (!ctx->staged || ctx->batch) return CJ_ERR_NOT_STAGED;
+    cj_parse_info info;
+    cj_status st = read_info(ctx, &info);
+    if (st) return st;
+    if (info.status != CJ_OK) return (cj_status)info.status;
+    CJ_CUDA(cudaSetDevice(ctx->device));
+    const uint64_t S = (uint64_t)info.n_structural, slots = S + 1;
+    if ((st = ensure(ctx, ctx->val_type, slots))) return st;
+    if ((st = ensure(ctx, ctx->val_num, slots))) return st;
+    if ((st = ensure(ctx, ctx->val_len, slots))) return st;
+    if ((st = ensure(ctx, ctx->val_str, ctx->n_bytes + 1))) return st;
+    const uint64_t long_cap = ctx->n_bytes / 256 + 1;
+    if ((st = ensure(ctx, ctx->val_long, long_cap + 1))) return st;    // the list, then its counter
+    if ((st = ensure(ctx, ctx->val_counts, kValTypes))) return st;
+    if (!ctx->pow5.p) {
+        if ((st = ensure(ctx, ctx->pow5, 2 * 651))) return st;
+        CJ_CUDA(cudaMemcpy(ctx->pow5.p, kPow5Table, sizeof(kPow5Table), cudaMemcpyHostToDevice));
+    }
+    ValueParams vp{};
+    vp.in = ctx->in.p;
+    vp.segs = ctx->segs.p;
+    vp.n_segs = ctx->n_segs;
+    vp.pos = ctx->pos.p;
+    vp.S = (uint32_t)S;
+    vp.n_bytes = ctx->n_bytes;
+    vp.type = ctx->val_type.p;
+    vp.num = ctx->val_num.p;
+    vp.len = ctx->val_len.p;
+    vp.str_out = ctx->val_str.p;
+    vp.long_list = ctx->val_long.p;
+    vp.long_cap = (uint32_t)std::min<uint64_t>(long_cap, 0xFFFFFFFFull);
+    vp.n_long = ctx->val_long.p + long_cap;
+    vp.counts = ctx->val_counts.p;
+    vp.pow5 = ctx->pow5.p;
+    CJ_CUDA(cudaMemsetAsync(vp.n_long, 0, sizeof(uint32_t), ctx->stream));
+    CJ_CUDA(cudaMemsetAsync(ctx->val_counts.p, 0, kValTypes * sizeof(unsigned long long), ctx->stream));
+    if (launch_decode_values(vp, ctx->sm_count, ctx->stream) != cudaSuccess) return CJ_ERR_CUDA;
+    ctx->launches += 4;
+    ctx->val_slots = slots;
+    if (counts) {
+        unsigned long long c[kValTypes];
+        CJ_CUDA(cudaMemcpyAsync(c, ctx->val_counts.p, sizeof c, cudaMemcpyDeviceToHost, ctx->stream));
+        CJ_CUDA(cudaStreamSynchronize(ctx->stream));
+        counts->n_slots = (int64_t)slots;
+        for (int k = 0; k < kValTypes; k++) counts->by_type[k] = (int64_t)c[k];
+    }
+    return CJ_OK;
+}
+
+cj_status cj_values_device(cj_context* ctx, const uint8_t** type, const uint64_t** num, const uint32_t** len,
+                           const uint8_t** strings)
+{
+    if (!ctx) return CJ_ERR_INVALID_ARGUMENT;
+    if (!ctx->val_slots) return CJ_ERR_NOT_STAGED;
+    if (type) *type = ctx->val_type.p;
+    if (num) *num = ctx->val_num.p;
+    if (len) *len = ctx->val_len.p;
+    if (strings) *strings = ctx->val_str.p;
+    return CJ_OK;
+}
+
+cj_status cj_copy_values(cj_context* ctx, uint8_t* type, uint64_t* num, uint32_t* len, size_t slot_cap,
+                         uint8_t* strings, size_t string_cap)
+{
+    if (!ctx) return CJ_ERR_INVALID_ARGUMENT;
+    if (!ctx->val_slots) return CJ_ERR_NOT_STAGED;
+    if ((type || num || len) && slot_cap < ctx->val_slots) return CJ_ERR_CAPACITY;
+    if (strings && string_cap < ctx->n_bytes) return CJ_ERR_CAPACITY;
+    CJ_CUDA(cudaSetDevice(ctx->device));
+    const size_t n = ctx->val_slots;
+    if (type) CJ_CUDA(cudaMemcpyAsync(type, ctx->val_type.p, n, cudaMemcpyDeviceToHost, ctx->stream));
+    if (num) CJ_CUDA(cudaMemcpyAsync(num, ctx->val_num.p, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    if (len) CJ_CUDA(cudaMemcpyAsync(len, ctx->val_len.p, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    if (strings && ctx->n_bytes)
+        CJ_CUDA(cudaMemcpyAsync(strings, ctx->val_str.p, ctx->n_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    CJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    return CJ_OK;
 }
 
 cj_status cj_run_staged_starved(cj_context* ctx, uint32_t polls, cj_parse_info* info)

@@ -113,6 +113,36 @@ cudaError_t preload_scan_kernels();
 cudaError_t preload_pair_kernels();
 cudaError_t preload_batch_kernels();
 
+// value decoding over a staged result (cj_values.cu): per slot (the text
+// before the first structural, and after each), a type, an int64 / double /
+// decoded-string offset, and a decoded string length
+enum : uint8_t {
+    kValNone = 0, kValString = 1, kValInt = 2, kValDouble = 3, kValTrue = 4, kValFalse = 5, kValNull = 6,
+    kValInvalid = 7,
+    kValDeferred = 8               // internal: a number for the exact decimal conversion
+};
+constexpr int kValTypes = 8;
+struct ValueParams {
+    const uint8_t* in;
+    const Segment* segs;
+    uint32_t n_segs;
+    const int32_t* pos;            // the staged result's positions (1-based, logical)
+    uint32_t S;
+    uint64_t n_bytes;              // logical input bytes
+    uint8_t* type;                 // S + 1 slots
+    uint64_t* num;                 // int64 / double bits / decoded string's offset in str_out
+    uint32_t* len;                 // decoded string length
+    uint8_t* str_out;              // n_bytes: decoded strings at their content offsets
+    uint32_t* long_list;           // slots for the second kernel: long strings, deferred numbers
+    uint32_t long_cap;
+    uint32_t* n_long;              // entries wanted (more than long_cap: the rest are swept)
+    unsigned long long* counts;    // kValTypes
+    const uint64_t* pow5;          // kPow5Table on the device
+};
+cudaError_t launch_decode_values(const ValueParams& p, int sm_count, cudaStream_t stream);
+cudaError_t preload_value_kernels();
+extern const uint64_t kPow5Table[2 * 651];
+
 // key/value queries over a staged JSON-Lines result (cj_query.cu)
 // JSON-Lines chunk plan of a device buffer (cj_plan.cu); scratch: nb =
 // ceil(size / 64 KiB) counts, chunk_count + 1 requests and positions

@@ -1,0 +1,615 @@
+// cj_values.cu -- value decoding over a parsed result: the scalar between
+// every two structurals decoded -- strings unescaped to UTF-8, numbers to
+// int64 or double, true / false / null.  The reference stops at the index:
+// its iterator hands out the raw bytes of a value (getValue,
+// cujson/query/query_iterator.cpp:512); this is the "value decoding" step that
+// would follow it.
+//
+// Slots: slot 0 is the text before the first structural, slot i (1 <= i <= S)
+// the text after structural i up to the next one (or the end of the input).
+// Each slot's text, less JSON whitespace at both ends, is one of: nothing,
+// a string, a number, a literal -- anything else is marked invalid.
+//
+//   decode_slots   one thread per slot; a string longer than kShortBytes goes
+//                  to a list instead, so one long string does not hold up a
+//                  warp of short ones;
+//   decode_deferred, decode_swept: below.
+//
+// A string's decoded bytes are written at its own content offset in the
+// output buffer (decoding never lengthens a string), so no prefix sum is
+// needed; its decoded length goes to len[].  Numbers: an integer without a
+// fraction or exponent that fits int64 is exact; otherwise the correctly
+// rounded double, by Clinger's fast path (exact powers of ten, at most 2^53
+// and 10^22) or the Eisel-Lemire algorithm (a 128-bit product with a
+// truncated power of five, D. Lemire 2021); inputs of more than 19
+// significant digits are tried at both neighbours of their truncation.  The
+// rare inputs that neither decides (a product too close to a halfway point,
+// subnormal results) join the second kernel's list and are converted exactly
+// there: the decimal-shift method (the "simple decimal conversion" of
+// Go's strconv and of Nigel Tao's Wuffs) -- the digits held as a big decimal,
+// shifted by powers of two into [1/2, 1), then 53 bits more, then rounded half
+// to even; 800 digits are held, more only set a sticky flag, and the
+// exact halfway points of doubles need at most 767.
+//
+//   decode_deferred  the list (long strings and deferred numbers), with a
+//                    digit buffer per thread in shared memory;
+//   decode_swept     only when the list overflowed: the deferred numbers it
+//                    did not hold, found by a pass over the types.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "cj_device.cuh"
+#include "cj_kernels.h"
+
+namespace cj {
+
+namespace {
+
+constexpr uint32_t kShortBytes = 256;     // longer strings go to the second kernel
+constexpr int kValThreads = 256;
+
+__device__ __forceinline__ bool is_ws(uint8_t c) { return c == ' ' || c == '\t' || c == '\n' || c == '\r'; }
+
+// the byte at logical offset x: segments are searched once per slot and then
+// followed forward
+struct Reader {
+    const ValueParams* P;
+    uint32_t seg;
+    uint64_t lo, hi;          // logical range of the current segment
+    const uint8_t* base;      // its first byte on the device
+    __device__ void seek(uint64_t x) {
+        uint32_t a = 0, b = P->n_segs;
+        while (b - a > 1) {
+            const uint32_t m = (a + b) >> 1;
+            if (__ldg(&P->segs[m].logical_off) <= x) a = m;
+            else b = m;
+        }
+        set(a);
+    }
+    __device__ void set(uint32_t s) {
+        seg = s;
+        lo = __ldg(&P->segs[s].logical_off);
+        hi = lo + __ldg(&P->segs[s].len);
+        base = P->in + __ldg(&P->segs[s].dev_off);
+    }
+    __device__ uint8_t at(uint64_t x) {
+        while (x >= hi && seg + 1 < P->n_segs) set(seg + 1);
+        return x < hi ? __ldg(base + (x - lo)) : (uint8_t)' ';
+    }
+};
+
+__device__ __forceinline__ int hexval(uint8_t c) {
+    if (c >= '0' && c <= '9') return c - '0';
+    if (c >= 'a' && c <= 'f') return c - 'a' + 10;
+    if (c >= 'A' && c <= 'F') return c - 'A' + 10;
+    return -1;
+}
+
+// the string whose quotes are at logical offsets a and b (b > a): its
+// decoded bytes from out[a + 1] on; returns the decoded length, or -1 when
+// the content is not a valid JSON string
+__device__ int64_t decode_string(Reader& rd, uint64_t a, uint64_t b, uint8_t* out)
+{
+    uint64_t o = a + 1;
+    for (uint64_t x = a + 1; x < b;) {
+        const uint8_t c = rd.at(x);
+        if (c < 0x20u) return -1;                         // control characters must be escaped
+        if (c == '"') return -1;                          // an inner quote ends the string early
+        if (c != '\\') { out[o++] = c; x++; continue; }
+        if (x + 1 >= b) return -1;
+        const uint8_t e = rd.at(x + 1);
+        uint8_t r;
+        switch (e) {
+            case '"': r = '"'; break;
+            case '\\': r = '\\'; break;
+            case '/': r = '/'; break;
+            case 'b': r = '\b'; break;
+            case 'f': r = '\f'; break;
+            case 'n': r = '\n'; break;
+            case 'r': r = '\r'; break;
+            case 't': r = '\t'; break;
+            case 'u': {
+                if (x + 6 > b) return -1;
+                uint32_t cp = 0;
+                for (int k = 0; k < 4; k++) {
+                    const int h = hexval(rd.at(x + 2 + k));
+                    if (h < 0) return -1;
+                    cp = (cp << 4) | (uint32_t)h;
+                }
+                x += 6;
+                if (cp >= 0xD800u && cp <= 0xDBFFu) {
+                    // a high surrogate must be followed by an escaped low one
+                    if (x + 6 > b || rd.at(x) != '\\' || rd.at(x + 1) != 'u') return -1;
+                    uint32_t lo = 0;
+                    for (int k = 0; k < 4; k++) {
+                        const int h = hexval(rd.at(x + 2 + k));
+                        if (h < 0) return -1;
+                        lo = (lo << 4) | (uint32_t)h;
+                    }
+                    if (lo < 0xDC00u || lo > 0xDFFFu) return -1;
+                    x += 6;
+                    cp = 0x10000u + ((cp - 0xD800u) << 10) + (lo - 0xDC00u);
+                } else if (cp >= 0xDC00u && cp <= 0xDFFFu) {
+                    return -1;                            // a lone low surrogate
+                }
+                if (cp < 0x80u) {
+                    out[o++] = (uint8_t)cp;
+                } else if (cp < 0x800u) {
+                    out[o++] = (uint8_t)(0xC0u | (cp >> 6));
+                    out[o++] = (uint8_t)(0x80u | (cp & 0x3Fu));
+                } else if (cp < 0x10000u) {
+                    out[o++] = (uint8_t)(0xE0u | (cp >> 12));
+                    out[o++] = (uint8_t)(0x80u | ((cp >> 6) & 0x3Fu));
+                    out[o++] = (uint8_t)(0x80u | (cp & 0x3Fu));
+                } else {
+                    out[o++] = (uint8_t)(0xF0u | (cp >> 18));
+                    out[o++] = (uint8_t)(0x80u | ((cp >> 12) & 0x3Fu));
+                    out[o++] = (uint8_t)(0x80u | ((cp >> 6) & 0x3Fu));
+                    out[o++] = (uint8_t)(0x80u | (cp & 0x3Fu));
+                }
+                continue;
+            }
+            default: return -1;
+        }
+        out[o++] = r;
+        x += 2;
+    }
+    return (int64_t)(o - (a + 1));
+}
+
+// ---- numbers -------------------------------------------------------------------
+
+constexpr int kQMin = -342, kQMax = 308;
+constexpr uint64_t kInfBits = 0x7FF0000000000000ull;
+
+// Eisel-Lemire: the correctly rounded double of w * 10^q (w != 0, at most 19
+// digits), as bits, or -1 when the 128-bit product cannot decide it
+__device__ int64_t eisel_lemire(uint64_t w, int32_t q, const uint64_t* __restrict__ pow5)
+{
+    if (q < kQMin) return 0;                                   // rounds to +0
+    if (q > kQMax) return (int64_t)kInfBits;
+    const int lz = __clzll((long long)w);
+    w <<= lz;
+    const int idx = 2 * (q - kQMin);
+    uint64_t hi = __umul64hi(w, __ldg(pow5 + idx)), lo = w * __ldg(pow5 + idx);
+    if ((hi & 0x1FFull) == 0x1FFull) {
+        // the truncated table entry may matter: add the next 64 bits
+        const uint64_t hi2 = __umul64hi(w, __ldg(pow5 + idx + 1));
+        lo += hi2;
+        if (hi2 > lo) hi++;
+    }
+    if (lo == ~0ull && (q < -27 || q > 55)) return -1;
+    const int upperbit = (int)(hi >> 63);
+    uint64_t m = hi >> (upperbit + 9);
+    int32_t p2 = (int32_t)((((152170 + 65536) * q) >> 16) + 63) + upperbit - lz + 1023;
+    if (p2 <= 0) return -1;                                    // subnormal or zero: not decided here
+    // exactly halfway between two doubles (only possible for small |q|):
+    // round to even
+    if (lo <= 1 && q >= -4 && q <= 23 && (m & 3u) == 1u && (m << (upperbit + 9)) == hi) m &= ~1ull;
+    m += m & 1u;
+    m >>= 1;
+    if (m >= (2ull << 52)) {
+        m = 1ull << 52;
+        p2++;
+    }
+    m &= ~(1ull << 52);
+    if (p2 >= 0x7FF) return (int64_t)kInfBits;
+    return (int64_t)(((uint64_t)p2 << 52) | m);
+}
+
+__device__ const double kExact10[23] = {1e0,  1e1,  1e2,  1e3,  1e4,  1e5,  1e6,  1e7,  1e8,  1e9,  1e10, 1e11,
+                                        1e12, 1e13, 1e14, 1e15, 1e16, 1e17, 1e18, 1e19, 1e20, 1e21, 1e22};
+
+// a number token [a, b): type and value bits
+__device__ uint8_t decode_number(Reader& rd, uint64_t a, uint64_t b, const uint64_t* pow5, uint64_t& bits)
+{
+    uint64_t x = a;
+    bool neg = false;
+    if (rd.at(x) == '-') { neg = true; x++; }
+    if (x >= b) return kValInvalid;
+    uint64_t w = 0;
+    int digits = 0;               // significant digits kept in w (at most 19)
+    int32_t drop = 0;             // integer-part digits beyond the 19 kept
+    bool truncated = false;       // a nonzero digit was dropped
+    bool nonzero = false;
+    const uint64_t int_start = x;
+    uint8_t c = rd.at(x);
+    if (c == '0') {
+        x++;
+    } else if (c >= '1' && c <= '9') {
+        while (x < b && (c = rd.at(x)) >= '0' && c <= '9') {
+            if (digits < 19) { w = w * 10 + (c - '0'); digits++; nonzero = true; }
+            else { drop++; if (c != '0') truncated = true; }
+            x++;
+        }
+    } else {
+        return kValInvalid;
+    }
+    const uint64_t int_digits = x - int_start;
+    bool frac = false, expo = false;
+    int32_t frac_kept = 0;
+    if (x < b && rd.at(x) == '.') {
+        frac = true;
+        x++;
+        const uint64_t f0 = x;
+        while (x < b && (c = rd.at(x)) >= '0' && c <= '9') {
+            if (!nonzero && c == '0') {
+                frac_kept++;      // leading zeros of a value below 1: not significant
+            } else if (digits < 19) {
+                w = w * 10 + (c - '0');
+                digits++;
+                frac_kept++;
+                nonzero = true;
+            } else if (c != '0') {
+                truncated = true;
+            }
+            x++;
+        }
+        if (x == f0) return kValInvalid;
+    }
+    int64_t e10 = 0;
+    if (x < b && ((c = rd.at(x)) == 'e' || c == 'E')) {
+        expo = true;
+        x++;
+        bool eneg = false;
+        if (x < b && ((c = rd.at(x)) == '+' || c == '-')) { eneg = c == '-'; x++; }
+        const uint64_t e0 = x;
+        while (x < b && (c = rd.at(x)) >= '0' && c <= '9') {
+            if (e10 < 100000) e10 = e10 * 10 + (c - '0');
+            x++;
+        }
+        if (x == e0) return kValInvalid;
+        if (eneg) e10 = -e10;
+    }
+    if (x != b) return kValInvalid;
+    if (!frac && !expo) {
+        // an integer: exact in int64 when it fits
+        if (int_digits <= 19 && drop == 0) {
+            if (!neg && w <= 0x7FFFFFFFFFFFFFFFull) { bits = w; return kValInt; }
+            if (neg && w <= 0x8000000000000000ull) { bits = (uint64_t)(-(int64_t)(w - 1) - 1); return kValInt; }
+        }
+    }
+    const int64_t q64 = e10 + drop - frac_kept;
+    if (w == 0) {
+        bits = neg ? 0x8000000000000000ull : 0ull;
+        return kValDouble;
+    }
+    if (q64 < -100000 || q64 > 100000) {
+        bits = (q64 > 0 ? kInfBits : 0ull) | (neg ? 0x8000000000000000ull : 0ull);
+        return kValDouble;
+    }
+    const int32_t q = (int32_t)q64;
+    int64_t r;
+    if (!truncated && w <= (1ull << 53) && q >= -22 && q <= 22) {
+        // Clinger's fast path: both operands exact, one correctly rounded operation
+        double d = (double)w;
+        d = q < 0 ? d / kExact10[-q] : d * kExact10[q];
+        r = (int64_t)__double_as_longlong(d);
+    } else {
+        r = eisel_lemire(w, q, pow5);
+        // more than 19 significant digits: the value lies between w and w + 1
+        // at this exponent; decided only when both round alike
+        if (r >= 0 && truncated && eisel_lemire(w + 1, q, pow5) != r) r = -1;
+    }
+    if (r < 0) return kValDeferred;
+    bits = (uint64_t)r | (neg ? 0x8000000000000000ull : 0ull);
+    return kValDouble;
+}
+
+// ---- the exact conversion ----------------------------------------------------------
+
+constexpr int kDecHold = 800;                 // digits held between shifts
+constexpr int kDecBuf = kDecHold + 20;        // room for the digits one left shift adds
+constexpr int kDeferredThreads = 32;
+
+// value = 0.d[0] d[1] ... d[nd-1] * 10^dp; `trunc`: nonzero digits beyond
+// d[nd-1] were dropped (the value is a little above what is held)
+struct Decimal {
+    uint8_t* d;
+    int nd;
+    int dp;
+    bool trunc;
+};
+
+__device__ void dec_trim(Decimal& x)
+{
+    while (x.nd > 0 && x.d[x.nd - 1] == 0) x.nd--;
+    if (x.nd == 0) x.dp = 0;
+}
+
+// x /= 2^k, 1 <= k <= 60
+__device__ void dec_shr(Decimal& x, int k)
+{
+    const uint64_t mask = (1ull << k) - 1;
+    uint64_t n = 0;
+    int r = 0, w = 0;
+    while ((n >> k) == 0) {               // digits until the quotient's first one is nonzero
+        if (r < x.nd) {
+            n = n * 10 + x.d[r];
+        } else {
+            if (n == 0) { x.nd = 0; x.dp = 0; return; }
+            n *= 10;
+        }
+        r++;
+    }
+    x.dp -= r - 1;
+    while (r < x.nd) {                    // one digit out per digit in: w < r throughout
+        const uint8_t c = (uint8_t)(n >> k);
+        n = (n & mask) * 10 + x.d[r++];
+        x.d[w++] = c;
+    }
+    while (n > 0) {                       // the remainder's digits
+        const uint8_t c = (uint8_t)(n >> k);
+        n = (n & mask) * 10;
+        if (w < kDecHold) x.d[w++] = c;
+        else if (c) x.trunc = true;
+    }
+    x.nd = w;
+    dec_trim(x);
+}
+
+// x *= 2^k, 1 <= k <= 60: digits from the last, each written 19 places
+// further on (2^60 * 9 carries into at most 19 new digits), then moved down
+__device__ void dec_shl(Decimal& x, int k)
+{
+    if (x.nd == 0) return;
+    constexpr int kOff = 19;
+    const int end = x.nd + kOff;
+    int w = end;
+    uint64_t n = 0;
+    for (int r = x.nd - 1; r >= 0; r--) {
+        n += (uint64_t)x.d[r] << k;
+        const uint64_t q = n / 10;
+        x.d[--w] = (uint8_t)(n - 10 * q);
+        n = q;
+    }
+    while (n > 0) {
+        const uint64_t q = n / 10;
+        x.d[--w] = (uint8_t)(n - 10 * q);
+        n = q;
+    }
+    int len = end - w;
+    x.dp += len - x.nd;
+    if (len > kDecHold) {
+        for (int j = w + kDecHold; j < end; j++)
+            if (x.d[j]) x.trunc = true;
+        len = kDecHold;
+    }
+    for (int j = 0; j < len; j++) x.d[j] = x.d[w + j];
+    x.nd = len;
+    dec_trim(x);
+}
+
+// floor(k * log2(10)) for 1 <= k <= 18: the shift that keeps a value below
+// 10^-k below 1
+__device__ __forceinline__ int dec_shift_for(int k) { return k >= 18 ? 59 : (k * 217706) >> 16; }
+
+// the integer nearest x (x < 2^53 + 1), ties to even
+__device__ uint64_t dec_round(const Decimal& x)
+{
+    if (x.nd == 0 || x.dp < 0) return 0;
+    uint64_t n = 0;
+    int i = 0;
+    for (; i < x.dp && i < x.nd; i++) n = n * 10 + x.d[i];
+    for (; i < x.dp; i++) n *= 10;
+    bool up = false;
+    if (x.dp < x.nd) {
+        const uint8_t c = x.d[x.dp];
+        // trailing zeros are trimmed: a digit after the 5 means above half
+        up = c > 5 || (c == 5 && (x.trunc || x.dp + 1 < x.nd || (n & 1)));
+    }
+    return n + up;
+}
+
+// the number token [a, b) (its syntax already checked) as the correctly
+// rounded double's bits, sign included
+__device__ uint64_t decode_number_exact(Reader& rd, uint64_t a, uint64_t b, uint8_t* digits)
+{
+    Decimal x{digits, 0, 0, false};
+    uint64_t p = a;
+    const bool neg = rd.at(p) == '-';
+    if (neg) p++;
+    uint8_t c;
+    for (; p < b && (c = rd.at(p)) >= '0' && c <= '9'; p++) {
+        if (x.nd == 0 && c == '0') continue;                     // a leading zero
+        if (x.nd < kDecHold) x.d[x.nd++] = (uint8_t)(c - '0');
+        else if (c != '0') x.trunc = true;
+        x.dp++;
+    }
+    if (p < b && rd.at(p) == '.') {
+        for (p++; p < b && (c = rd.at(p)) >= '0' && c <= '9'; p++) {
+            if (x.nd == 0 && c == '0') { x.dp--; continue; }     // zeros before the first digit
+            if (x.nd < kDecHold) x.d[x.nd++] = (uint8_t)(c - '0');
+            else if (c != '0') x.trunc = true;
+        }
+    }
+    if (p < b) {                                                 // the exponent
+        p++;
+        bool eneg = false;
+        if ((c = rd.at(p)) == '+' || c == '-') { eneg = c == '-'; p++; }
+        int e = 0;
+        for (; p < b; p++)
+            if (e < 100000) e = e * 10 + (rd.at(p) - '0');
+        x.dp += eneg ? -e : e;
+    }
+    dec_trim(x);
+    const uint64_t sign = neg ? 0x8000000000000000ull : 0ull;
+    if (x.nd == 0 || x.dp < -330) return sign;                   // below half the least subnormal
+    if (x.dp > 310) return sign | kInfBits;
+    int e2 = 0;
+    while (x.dp > 0) {
+        const int k = x.dp >= 18 ? 60 : dec_shift_for(x.dp);
+        dec_shr(x, k);
+        e2 += k;
+    }
+    while (x.dp < 0 || (x.dp == 0 && x.d[0] < 5)) {
+        const int k = x.dp == 0 ? 1 : dec_shift_for(-x.dp);
+        dec_shl(x, k);
+        e2 -= k;
+    }
+    // the value is v * 2^e2 with v in [1/2, 1): 1.f * 2^(e2 - 1)
+    int e = e2 - 1;
+    if (e > 1023) return sign | kInfBits;
+    if (e < -1022) {                                             // subnormal: down to 2^-1022
+        for (int s = -1022 - e; s > 0; s -= 60) dec_shr(x, s < 60 ? s : 60);
+        e = -1022;
+    }
+    dec_shl(x, 53);
+    uint64_t m = dec_round(x);
+    if (m == (1ull << 53)) {
+        m >>= 1;
+        if (++e > 1023) return sign | kInfBits;
+    }
+    if (m < (1ull << 52)) return sign | m;                      // subnormal (or zero)
+    return sign | ((uint64_t)(e + 1023) << 52) | (m & ((1ull << 52) - 1));
+}
+
+// the trimmed text of slot i: [a, b) (a == b: nothing)
+__device__ void slot_range(const ValueParams& P, Reader& rd, uint64_t i, uint64_t& a, uint64_t& b)
+{
+    a = i == 0 ? 0 : (uint64_t)(uint32_t)__ldg(P.pos + i - 1);          // positions are 1-based
+    b = i == P.S ? P.n_bytes : (uint64_t)(uint32_t)__ldg(P.pos + i) - 1;
+    if (b < a) b = a;
+    rd.seek(a);
+    while (a < b && is_ws(rd.at(a))) a++;
+    while (b > a && is_ws(rd.at(b - 1))) b--;
+}
+
+__device__ uint8_t decode_slot(const ValueParams& P, Reader& rd, uint64_t i, uint64_t a, uint64_t b)
+{
+    if (a == b) return kValNone;
+    const uint8_t c = rd.at(a);
+    if (c == '"') {
+        if (b - a < 2 || rd.at(b - 1) != '"') return kValInvalid;
+        const int64_t n = decode_string(rd, a, b - 1, P.str_out);
+        if (n < 0) return kValInvalid;
+        P.num[i] = a + 1;                 // where the decoded bytes start
+        P.len[i] = (uint32_t)n;
+        return kValString;
+    }
+    if (c == 't' || c == 'f' || c == 'n') {
+        const char* lit = c == 't' ? "true" : c == 'f' ? "false" : "null";
+        const uint64_t n = c == 'f' ? 5 : 4;
+        if (b - a != n) return kValInvalid;
+        for (uint64_t k = 0; k < n; k++)
+            if (rd.at(a + k) != (uint8_t)lit[k]) return kValInvalid;
+        return c == 't' ? kValTrue : c == 'f' ? kValFalse : kValNull;
+    }
+    if (c == '-' || (c >= '0' && c <= '9')) {
+        uint64_t bits = 0;
+        const uint8_t t = decode_number(rd, a, b, P.pow5, bits);
+        if (t == kValInt || t == kValDouble) P.num[i] = bits;
+        return t;
+    }
+    return kValInvalid;
+}
+
+__global__ void __launch_bounds__(kValThreads) decode_slots(ValueParams P)
+{
+    const uint64_t n = (uint64_t)P.S + 1;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        Reader rd{&P, 0, 0, 0, nullptr};
+        uint64_t a, b;
+        slot_range(P, rd, i, a, b);
+        P.num[i] = 0;
+        P.len[i] = 0;
+        const bool long_string = b - a > kShortBytes && rd.at(a) == '"';
+        uint8_t t = kValString;
+        if (!long_string) t = decode_slot(P, rd, i, a, b);
+        if (long_string || t == kValDeferred) {
+            const uint32_t k = atomicAdd(P.n_long, 1u);
+            if (k < P.long_cap) P.long_list[k] = (uint32_t)i;            // decided by decode_deferred
+            else if (long_string) t = decode_slot(P, rd, i, a, b);       // the list is full
+            else t = kValDeferred;                                       // left for decode_swept
+        }
+        P.type[i] = t;
+    }
+}
+
+__device__ void decode_deferred_slot(const ValueParams& P, uint64_t i, uint8_t* digits)
+{
+    Reader rd{&P, 0, 0, 0, nullptr};
+    uint64_t a, b;
+    slot_range(P, rd, i, a, b);
+    if (rd.at(a) == '"') {
+        P.type[i] = decode_slot(P, rd, i, a, b);
+    } else {
+        P.num[i] = decode_number_exact(rd, a, b, digits);
+        P.type[i] = kValDouble;
+    }
+}
+
+__global__ void __launch_bounds__(kDeferredThreads) decode_deferred(ValueParams P)
+{
+    __shared__ uint8_t digits[kDeferredThreads][kDecBuf];
+    const uint32_t n = min(*P.n_long, P.long_cap);
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        decode_deferred_slot(P, P.long_list[k], digits[threadIdx.x]);
+}
+
+__global__ void __launch_bounds__(kDeferredThreads) decode_swept(ValueParams P)
+{
+    __shared__ uint8_t digits[kDeferredThreads][kDecBuf];
+    if (*P.n_long <= P.long_cap) return;                      // the list held every entry
+    const uint64_t n = (uint64_t)P.S + 1;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        if (P.type[i] == kValDeferred) decode_deferred_slot(P, i, digits[threadIdx.x]);
+}
+
+// type counts
+__global__ void __launch_bounds__(kValThreads) count_types(ValueParams P)
+{
+    __shared__ unsigned long long c[kValTypes];
+    if (threadIdx.x < kValTypes) c[threadIdx.x] = 0;
+    __syncthreads();
+    const uint64_t n = (uint64_t)P.S + 1;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        atomicAdd(&c[min((uint32_t)P.type[i], (uint32_t)kValTypes - 1u)], 1ull);
+    __syncthreads();
+    if (threadIdx.x < kValTypes && c[threadIdx.x]) atomicAdd(P.counts + threadIdx.x, c[threadIdx.x]);
+}
+
+}  // namespace
+
+cudaError_t launch_decode_values(const ValueParams& p, int sm_count, cudaStream_t stream)
+{
+    const uint64_t n = (uint64_t)p.S + 1;
+    const int grid = (int)std::min<uint64_t>((n + kValThreads - 1) / kValThreads, (uint64_t)sm_count * 8);
+#ifdef CJ_EMU
+    (void)stream;
+    cj_emu::launch(grid, kValThreads, 0, [&] { decode_slots(p); });
+    cj_emu::launch(sm_count * 2, kDeferredThreads, 0, [&] { decode_deferred(p); });
+    cj_emu::launch(sm_count * 2, kDeferredThreads, 0, [&] { decode_swept(p); });
+    cj_emu::launch(grid, kValThreads, 0, [&] { count_types(p); });
+    return cudaSuccess;
+#else
+    decode_slots<<<grid, kValThreads, 0, stream>>>(p);
+    decode_deferred<<<sm_count * 8, kDeferredThreads, 0, stream>>>(p);
+    decode_swept<<<sm_count * 8, kDeferredThreads, 0, stream>>>(p);
+    count_types<<<grid, kValThreads, 0, stream>>>(p);
+    return cudaGetLastError();
+#endif
+}
+
+cudaError_t preload_value_kernels()
+{
+#ifdef CJ_EMU
+    return cudaSuccess;
+#else
+    cudaFuncAttributes a;
+    cudaError_t e = cudaFuncGetAttributes(&a, (const void*)decode_slots);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, (const void*)decode_deferred);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, (const void*)decode_swept);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, (const void*)count_types);
+    return e;
+#endif
+}
+
+// the 128-bit powers of five (pow5_table.py), copied to the device once
+extern const uint64_t kPow5Table[2 * 651];
+const uint64_t kPow5Table[2 * 651] = {
+#include "cj_pow5.inc"
+};
+
+}  // namespace cj

@@ -103,6 +103,7 @@ cj_status cj_context_reserve(cj_context* ctx, size_t max_bytes, size_t max_segme
 void*     cj_context_stream(cj_context* ctx);           /* cudaStream_t */
 int64_t   cj_context_launch_count(cj_context* ctx);     /* kernels launched so far */
 size_t    cj_context_device_bytes(cj_context* ctx);     /* arena size */
+size_t    cj_context_staged_bytes(cj_context* ctx);     /* input bytes of the staged input (0: none) */
 
 /* Process-wide default context on the current device (used by the drop-in
  * C++ headers); created on first use. */
@@ -358,6 +359,35 @@ cj_status cj_context_span_ms(cj_context* ctx, double* ms);
 void* cj_host_alloc(size_t bytes);
 void  cj_host_free(void* p);
 size_t cj_host_pool_trim(void);
+
+/* ---- value decoding ------------------------------------------------------------
+ * No counterpart call in the reference, whose iterator hands out a value's raw
+ * bytes (getValue, cujson/query/query_iterator.cpp:512).  cj_decode_values
+ * decodes every scalar of the staged (not batch) result on the device: slot 0
+ * is the text before the first structural, slot i (1..S) the text after
+ * structural i up to the next one; each, less JSON whitespace at both ends, is
+ * nothing, a string (unescaped to UTF-8), an integer that fits int64 (exact),
+ * another number (the correctly rounded double, round-half-even, subnormals
+ * and overflow to infinity included), true, false, null, or invalid.  Per slot:
+ * type[i]; num[i] = the int64, the double's bits, or for a string the offset
+ * of its decoded bytes in `strings`; len[i] = a string's decoded length.
+ * `strings` has one byte per input byte (a string's decoded bytes start at its
+ * content's logical offset).  The arrays stay on the device
+ * (cj_values_device) until the next decode; cj_copy_values copies them out
+ * (S + 1 slots; n_bytes string bytes). */
+enum {
+    CJ_VAL_NONE = 0, CJ_VAL_STRING = 1, CJ_VAL_INT = 2, CJ_VAL_DOUBLE = 3, CJ_VAL_TRUE = 4, CJ_VAL_FALSE = 5,
+    CJ_VAL_NULL = 6, CJ_VAL_INVALID = 7, CJ_VAL_TYPES = 8
+};
+typedef struct cj_value_counts {
+    int64_t n_slots;
+    int64_t by_type[8];          /* slots of each CJ_VAL_* type */
+} cj_value_counts;
+cj_status cj_decode_values(cj_context* ctx, cj_value_counts* counts);
+cj_status cj_values_device(cj_context* ctx, const uint8_t** type, const uint64_t** num, const uint32_t** len,
+                           const uint8_t** strings);
+cj_status cj_copy_values(cj_context* ctx, uint8_t* type, uint64_t* num, uint32_t* len, size_t slot_cap,
+                         uint8_t* strings, size_t string_cap);
 
 /* ---- loaders and JSON-Lines chunk planning ----------------------------------
  * cj_load_file reads a whole file into pinned host memory (free it with

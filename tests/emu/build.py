@@ -13,10 +13,10 @@ ROOT = HERE.parent.parent
 CSRC = ROOT / "cujson_gb300" / "csrc"
 BUILD = HERE / "_build"
 LIB = BUILD / "libcj_emu.so"
-UNITS = [CSRC / "cj_scan.cu", CSRC / "cj_pair.cu", HERE / "cj_emu_driver.cpp"]
+UNITS = [CSRC / "cj_scan.cu", CSRC / "cj_pair.cu", CSRC / "cj_values.cu", HERE / "cj_emu_driver.cpp"]
 DEPS = UNITS + [HERE / "cj_emu.h", HERE / "shim" / "cuda_runtime.h", CSRC / "cj_device.cuh",
                 CSRC / "cj_kernels.h", ROOT / "include" / "cujson_gb300.h"]
-FLAGS = ["-O1", "-g", "-std=c++17", "-fPIC", "-w", "-DCJ_EMU=1", f"-I{HERE / 'shim'}", f"-I{CSRC}",
+FLAGS = ["-O1", "-g", "-std=c++17", "-fPIC", "-w", "-DCJ_EMU=1", f"-I{HERE / 'shim'}", f"-I{CSRC}", f"-I{BUILD}",
          f"-I{ROOT / 'include'}", "-include", str(HERE / "cj_emu.h")]
 
 
@@ -40,6 +40,13 @@ def _compile(src: Path, variant: str) -> Path:
 
 def build(force: bool = False, variant: str = "") -> Path:
     BUILD.mkdir(exist_ok=True)
+    pow5 = BUILD / "cj_pow5.inc"          # the value decoder's table of powers of five
+    if not pow5.exists():
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("cj_pow5_table", ROOT / "cujson_gb300" / "pow5_table.py")
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.write(pow5)
     lib = _lib(variant)
     newest = max(p.stat().st_mtime for p in DEPS)
     if not force and lib.exists() and lib.stat().st_mtime >= newest:

@@ -243,6 +243,11 @@ inline unsigned __reduce_max_sync(unsigned, unsigned v) { return (unsigned)cj_em
 inline int __popc(uint32_t x) { return __builtin_popcount(x); }
 inline int __clz(int x) { return x == 0 ? 32 : __builtin_clz((uint32_t)x); }
 inline int __ffs(int x) { return x == 0 ? 0 : __builtin_ctz((uint32_t)x) + 1; }
+inline int __clzll(long long x) { return x == 0 ? 64 : __builtin_clzll((unsigned long long)x); }
+inline unsigned long long __umul64hi(unsigned long long a, unsigned long long b) {
+    return (unsigned long long)(((unsigned __int128)a * b) >> 64);
+}
+inline long long __double_as_longlong(double d) { long long r; std::memcpy(&r, &d, sizeof r); return r; }
 inline void __nanosleep(unsigned) {}
 inline void __threadfence() {}
 inline void __threadfence_system() {}

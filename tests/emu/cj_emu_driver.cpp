@@ -64,9 +64,18 @@ constexpr size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
 // verdicts); otherwise one document or JSON-Lines chunks continuing counts.
 // `wave_regions` > 0: the scan runs in waves of that many regions, each from
 // the previous wave's end value, as a streamed parse runs it.
+// `vals` (optional): after a valid parse, the value decoder's outputs too
+struct ValOut {
+    uint8_t* type;
+    uint64_t* num;
+    uint32_t* len;
+    uint8_t* strings;
+    int64_t* counts;
+};
+
 int run(const uint8_t* data, const size_t* sizes, size_t n, bool lines, bool batch, int region_steps,
         int32_t* out_pos, int32_t* out_pair, size_t cap, int64_t* out_S, uint32_t* out_flags,
-        uint32_t* doc_flags, int64_t* doc_S, uint32_t wave_regions = 0)
+        uint32_t* doc_flags, int64_t* doc_S, uint32_t wave_regions = 0, const ValOut* vals = nullptr)
 {
     size_t total = 0, padded = 0;
     for (size_t i = 0; i < n; i++) { total += sizes[i]; padded += round_up(sizes[i], kPadBytes); }
@@ -201,6 +210,34 @@ int run(const uint8_t* data, const size_t* sizes, size_t n, bool lines, bool bat
     uint32_t flags = ctrl->error_flags;
     if (ctrl->neg_min_level > 0) flags |= CJ_FLAG_BRACKETS;
     *out_flags = flags;
+    if (vals && !batch && flags == 0) {
+        const uint64_t S = ctrl->s_total, slots = S + 1;
+        ValueParams vp{};
+        vp.in = in;
+        vp.segs = d_segs;
+        vp.n_segs = (uint32_t)n;
+        vp.pos = pos;
+        vp.S = (uint32_t)S;
+        vp.n_bytes = total;
+        vp.type = galloc<uint8_t>(slots);
+        vp.num = galloc<uint64_t>(slots);
+        vp.len = galloc<uint32_t>(slots);
+        vp.str_out = galloc<uint8_t>(total + 1);
+        const uint64_t long_cap = total / 256 + 1;
+        vp.long_list = galloc<uint32_t>(long_cap + 1);
+        vp.long_cap = (uint32_t)long_cap;
+        vp.n_long = vp.long_list + long_cap;
+        vp.counts = galloc<unsigned long long>(kValTypes);
+        uint64_t* pow5 = galloc<uint64_t>(2 * 651);
+        std::copy(kPow5Table, kPow5Table + 2 * 651, pow5);
+        vp.pow5 = pow5;
+        launch_decode_values(vp, 3, nullptr);
+        std::copy(vp.type, vp.type + slots, vals->type);
+        std::copy(vp.num, vp.num + slots, vals->num);
+        std::copy(vp.len, vp.len + slots, vals->len);
+        std::copy(vp.str_out, vp.str_out + total, vals->strings);
+        for (int k = 0; k < kValTypes; k++) vals->counts[k] = (int64_t)vp.counts[k];
+    }
     if (batch) {
         // documents back to back in the output arrays
         size_t o = 0;
@@ -234,6 +271,15 @@ extern "C" int cje_parse(const uint8_t* data, const size_t* sizes, size_t n, int
 {
     return run(data, sizes, n, lines != 0, false, region_steps, out_pos, out_pair, cap, out_S, out_flags,
                nullptr, seg_S);
+}
+
+extern "C" int cje_parse_values(const uint8_t* data, const size_t* sizes, size_t n, int lines, int64_t* out_S,
+                                uint32_t* out_flags, uint8_t* type, uint64_t* num, uint32_t* len, uint8_t* strings,
+                                int64_t* counts, int32_t* scratch_pos, int32_t* scratch_pair, size_t cap)
+{
+    ValOut v{type, num, len, strings, counts};
+    return run(data, sizes, n, lines != 0, false, 4, scratch_pos, scratch_pair, cap, out_S, out_flags, nullptr,
+               nullptr, 0, &v);
 }
 
 extern "C" int cje_parse_waves(const uint8_t* data, const size_t* sizes, size_t n, int lines, int region_steps,
