@@ -59,6 +59,7 @@ def parse_args():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-documents measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-query", action="store_true", help="skip the device query measurement")
+    ap.add_argument("--no-values", action="store_true", help="skip the value decoding measurement")
     ap.add_argument("--no-configs", action="store_true", help="skip configs 1 and 3")
     ap.add_argument("--query-bytes", type=int, default=0,
                     help="event-log bytes of the query measurement (default: the 2 GB JSON-Lines limit)")
@@ -655,6 +656,26 @@ def run_query(args, local):
     return out
 
 
+def run_values(args, ctx, data, S):
+    """Value decoding over the staged benchmark document: every scalar slot
+    decoded on the device (strings unescaped, numbers to int64 / double,
+    literals), the arrays left on the device; wall time per call, which
+    includes the copy-back of the type counts."""
+    ctx.stage_standard(data)
+    ctx.run()
+    for _ in range(max(3, args.warmup)):
+        counts = ctx.decode_values_counts()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        counts = ctx.decode_values_counts()
+    dt = (time.perf_counter() - t0) / args.steps
+    names = ["none", "string", "int", "double", "true", "false", "null", "invalid"]
+    return {"workload": f"the {data.size} B benchmark document's {S + 1} slots",
+            "ms": round(dt * 1e3, 4), "input_GBps": round(data.size / dt / 1e9, 1),
+            "slots_per_s": round((S + 1) / dt, 1), "by_type": dict(zip(names, counts)),
+            "correct": sum(counts) == S + 1 and counts[7] == 0}
+
+
 def run_ours(args, world, rank, local, pg):
     import cujson_gb300 as cj
     peak, peak_kind = measured_peaks()
@@ -725,6 +746,7 @@ def run_ours(args, world, rank, local, pg):
 
     if rank != 0:
         return
+    values = None if args.no_values else run_values(args, ctx, data, S)
     batch = None if args.no_batch else run_batch(args, local)
     serve = None if args.no_serve else run_serve(args, local)
     query = None if args.no_query else run_query(args, local)
@@ -761,7 +783,7 @@ def run_ours(args, world, rank, local, pg):
                                "pair": round(pair_ms / runs, 4), "spine": round(spine_ms / runs, 4)},
         "parse_roofline_frac": round(B / (span_max / args.steps / 1e3) / 1e9 / peak, 4),
         "e2e": e2e, "cpu_baseline": cpu, "cpu_baseline_port": cpu_port, "gpu_launches": int(launches), "clocks": ck,
-        "batch": batch, "serving": serve, "query": query, "other_configs": others,
+        "batch": batch, "serving": serve, "query": query, "values": values, "other_configs": others,
     }
     print(json.dumps(line), flush=True)
 

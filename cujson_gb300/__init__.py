@@ -489,6 +489,13 @@ class Context:
                                     strings.ctypes.data, strings.size), "copy_values")
         return types, nums, lens, strings, [int(x) for x in counts.by_type]
 
+    def decode_values_counts(self) -> List[int]:
+        """cj_decode_values on the staged result, leaving the arrays on the
+        device: the slot counts by type."""
+        counts = ValueCounts()
+        _check(lib().cj_decode_values(self._h, ctypes.byref(counts)), "decode_values")
+        return [int(x) for x in counts.by_type]
+
     def save_tuning(self, path: str) -> None:
         _check(lib().cj_tuning_save(self._h, str(path).encode()), "save_tuning")
 

@@ -74,6 +74,7 @@ struct Reader {
         base = P->in + __ldg(&P->segs[s].dev_off);
     }
     __device__ uint8_t at(uint64_t x) {
+        if (x < lo) seek(x);                                   // back into an earlier segment
         while (x >= hi && seg + 1 < P->n_segs) set(seg + 1);
         return x < hi ? __ldg(base + (x - lo)) : (uint8_t)' ';
     }
@@ -156,6 +157,162 @@ __device__ int64_t decode_string(Reader& rd, uint64_t a, uint64_t b, uint8_t* ou
         x += 2;
     }
     return (int64_t)(o - (a + 1));
+}
+
+// ---- long strings: a warp per string ------------------------------------------------
+//
+// The string's content is taken 512 bytes a step, 16 bytes a lane, staged in
+// shared memory with 8 bytes before and 12 after.  Whether a byte is escaped
+// (its predecessor a backslash that is not itself escaped) is a two-state
+// recurrence: each lane's 16 bytes map the state at their start to the state
+// at their end, and a warp scan of those maps gives every lane its starting
+// state.  A lane then classifies its bytes within a window of 8 bytes before
+// and 12 after its own (an escape reaches 11 bytes ahead, the low half of a
+// surrogate pair looks 6 back), counts what each emits, and writes at its
+// offset from a warp prefix sum.
+
+constexpr int kLaneBytes = 16;
+constexpr int kWinBefore = 8, kWinAfter = 12;
+constexpr int kWarpStep = 32 * kLaneBytes;
+constexpr int kStage = kWinBefore + kWarpStep + kWinAfter;
+
+__device__ __forceinline__ int hex4(const uint8_t* p)
+{
+    const int x = hexval(p[0]), y = hexval(p[1]), z = hexval(p[2]), w = hexval(p[3]);
+    return (x | y | z | w) < 0 ? -1 : (x << 12) | (y << 8) | (z << 4) | w;
+}
+
+__device__ __forceinline__ int utf8_put(uint32_t cp, uint8_t* o)
+{
+    const int n = cp < 0x80u ? 1 : cp < 0x800u ? 2 : cp < 0x10000u ? 3 : 4;
+    if (o) {
+        if (n == 1) {
+            o[0] = (uint8_t)cp;
+        } else {
+            o[0] = (uint8_t)((0xFF00u >> n) | (cp >> (6 * (n - 1))));     // 110x, 1110, 11110 leads
+            for (int k = 1; k < n; k++) o[k] = (uint8_t)(0x80u | ((cp >> (6 * (n - 1 - k))) & 0x3Fu));
+        }
+    }
+    return n;
+}
+
+// what window byte j (kWinBefore <= j < kWinBefore + kLaneBytes, at content
+// offset q < len) emits: its byte count (written to o when o is set), or -1
+// when the string is invalid there.  st: bit k set when window byte k is a
+// backslash that starts an escape.
+__device__ int emit_byte(const uint8_t* w, uint64_t st, int j, uint64_t q, uint64_t len, uint8_t* o)
+{
+    const uint8_t c = w[j];
+    if ((st >> j) & 1) {
+        if (q + 1 >= len) return -1;                 // the backslash would escape the closing quote
+        uint8_t r;
+        switch (w[j + 1]) {
+            case '"': r = '"'; break;
+            case '\\': r = '\\'; break;
+            case '/': r = '/'; break;
+            case 'b': r = '\b'; break;
+            case 'f': r = '\f'; break;
+            case 'n': r = '\n'; break;
+            case 'r': r = '\r'; break;
+            case 't': r = '\t'; break;
+            case 'u': {
+                if (q + 5 >= len) return -1;
+                const int cu = hex4(w + j + 2);
+                if (cu < 0) return -1;
+                if (cu >= 0xD800 && cu <= 0xDBFF) {
+                    if (q + 11 >= len || w[j + 6] != '\\' || w[j + 7] != 'u') return -1;
+                    const int lo = hex4(w + j + 8);
+                    if (lo < 0xDC00 || lo > 0xDFFF) return -1;
+                    return utf8_put(0x10000u + ((uint32_t)(cu - 0xD800) << 10) + (uint32_t)(lo - 0xDC00), o);
+                }
+                if (cu >= 0xDC00 && cu <= 0xDFFF) {
+                    // only as the second half of a pair, which the first half emitted
+                    const int hi = hex4(w + j - 4);
+                    return (((st >> (j - 6)) & 1) && w[j - 5] == 'u' && hi >= 0xD800 && hi <= 0xDBFF) ? 0 : -1;
+                }
+                return utf8_put((uint32_t)cu, o);
+            }
+            default: return -1;
+        }
+        if (o) o[0] = r;
+        return 1;
+    }
+    if ((st >> (j - 1)) & 1) return 0;                          // the escaped character
+    for (int t = 2; t <= 5; t++)                                // a hex digit of an escaped u
+        if (((st >> (j - t)) & 1) && w[j - t + 1] == 'u') return 0;
+    if (c < 0x20u || c == '"') return -1;
+    if (o) o[0] = c;
+    return 1;
+}
+
+// a warp decodes the content src[0, len) of one string into out, staging
+// through `stage` (kStage bytes of shared memory, this warp's); every lane
+// returns the decoded length, or -1 when it is not a valid JSON string
+__device__ int64_t decode_string_warp(const uint8_t* __restrict__ src, uint64_t len, uint8_t* __restrict__ out,
+                                      uint8_t* stage)
+{
+    const int lane = (int)(threadIdx.x & 31);
+    const uint8_t* w = stage + kLaneBytes * lane;               // this lane's window
+    uint32_t carry = 0;           // escaped-state at the step's first byte
+    uint32_t prev8 = 0;           // that state 8 bytes before lane 0's first byte
+    uint64_t done = 0;            // bytes written
+    for (uint64_t c0 = 0; c0 < len; c0 += kWarpStep) {
+        __syncwarp();
+        for (int k = lane; k < kStage; k += 32) {
+            const int64_t q = (int64_t)c0 - kWinBefore + k;
+            stage[k] = (q >= 0 && (uint64_t)q < len) ? __ldg(src + q) : (uint8_t)0;
+        }
+        __syncwarp();
+        // this lane's state map, then the warp's scan of maps
+        uint32_t e0 = 0, e1 = 1;
+        for (int j = kWinBefore; j < kWinBefore + kLaneBytes; j++) {
+            const uint32_t bs = w[j] == '\\';
+            e0 = !e0 & bs;
+            e1 = !e1 & bs;
+        }
+        uint32_t m = e0 | (e1 << 1);
+        #pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t up = __shfl_up_sync(~0u, m, d);
+            if (lane >= d) m = ((m >> (up & 1u)) & 1u) | (((m >> ((up >> 1) & 1u)) & 1u) << 1);
+        }
+        const uint32_t excl = __shfl_up_sync(~0u, m, 1);
+        const uint32_t cin = lane ? (excl >> carry) & 1u : carry;
+        carry = (__shfl_sync(~0u, m, 31) >> carry) & 1u;
+        // the state 8 bytes in, handed to the next lane as its window's start
+        uint32_t e = cin;
+        for (int j = kWinBefore; j < kWinBefore + 8; j++) e = !e & (uint32_t)(w[j] == '\\');
+        uint32_t start = __shfl_up_sync(~0u, e, 1);
+        if (lane == 0) start = prev8;
+        prev8 = __shfl_sync(~0u, e, 31);
+        uint64_t st = 0;
+        e = start;
+        for (int j = 0; j < kWinBefore + kLaneBytes + kWinAfter; j++) {
+            e = !e & (uint32_t)(w[j] == '\\');
+            st |= (uint64_t)e << j;
+        }
+        // count, place, write
+        const uint64_t q0 = c0 + (uint64_t)kLaneBytes * lane;
+        const int own = q0 >= len ? 0 : len - q0 < (uint64_t)kLaneBytes ? (int)(len - q0) : kLaneBytes;
+        int n = 0;
+        bool bad = false;
+        for (int j = 0; j < own; j++) {
+            const int k = emit_byte(w, st, kWinBefore + j, q0 + j, len, nullptr);
+            bad |= k < 0;
+            n += k;
+        }
+        if (__any_sync(~0u, bad)) return -1;
+        int pre = n;
+        #pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int up = __shfl_up_sync(~0u, pre, d);
+            if (lane >= d) pre += up;
+        }
+        uint8_t* o = out + done + (pre - n);
+        for (int j = 0; j < own; j++) o += emit_byte(w, st, kWinBefore + j, q0 + j, len, o);
+        done += (uint64_t)__shfl_sync(~0u, pre, 31);
+    }
+    return (int64_t)done;
 }
 
 // ---- numbers -------------------------------------------------------------------
@@ -301,7 +458,8 @@ __device__ uint8_t decode_number(Reader& rd, uint64_t a, uint64_t b, const uint6
 
 constexpr int kDecHold = 800;                 // digits held between shifts
 constexpr int kDecBuf = kDecHold + 20;        // room for the digits one left shift adds
-constexpr int kDeferredThreads = 32;
+constexpr int kDeferredThreads = 128;       // four warps, a digit buffer each
+constexpr int kSweptThreads = 32;           // a digit buffer per thread
 
 // value = 0.d[0] d[1] ... d[nd-1] * 10^dp; `trunc`: nonzero digits beyond
 // d[nd-1] were dropped (the value is a little above what is held)
@@ -466,14 +624,58 @@ __device__ uint64_t decode_number_exact(Reader& rd, uint64_t a, uint64_t b, uint
 }
 
 // the trimmed text of slot i: [a, b) (a == b: nothing)
-__device__ void slot_range(const ValueParams& P, Reader& rd, uint64_t i, uint64_t& a, uint64_t& b)
+// the text of slot i, untrimmed: [a, b)
+__device__ __forceinline__ void slot_bounds(const ValueParams& P, uint64_t i, uint64_t& a, uint64_t& b)
 {
     a = i == 0 ? 0 : (uint64_t)(uint32_t)__ldg(P.pos + i - 1);          // positions are 1-based
     b = i == P.S ? P.n_bytes : (uint64_t)(uint32_t)__ldg(P.pos + i) - 1;
     if (b < a) b = a;
+}
+
+// [a, b) less JSON whitespace at both ends, by one thread
+__device__ void trim(Reader& rd, uint64_t& a, uint64_t& b)
+{
     rd.seek(a);
     while (a < b && is_ws(rd.at(a))) a++;
     while (b > a && is_ws(rd.at(b - 1))) b--;
+}
+
+// the same by a warp, 512 bytes a step from each end; every lane gets the
+// result (a slot may hold a long run of whitespace)
+__device__ void trim_warp(Reader& rd, uint64_t& a, uint64_t& b)
+{
+    const int lane = (int)(threadIdx.x & 31);
+    rd.seek(a);
+    uint64_t base = a;
+    for (; base < b; base += 32 * kLaneBytes) {
+        uint32_t m = 0;                                   // this lane's non-whitespace bytes
+        for (int k = 0; k < kLaneBytes; k++) {
+            const uint64_t x = base + (uint64_t)(kLaneBytes * lane + k);
+            m |= (uint32_t)(x < b && !is_ws(rd.at(x))) << k;
+        }
+        const uint32_t any = __ballot_sync(~0u, m != 0);
+        if (any) {
+            const int src = __ffs(any) - 1;
+            base += (uint64_t)(kLaneBytes * src + __ffs(__shfl_sync(~0u, m, src)) - 1);
+            break;
+        }
+    }
+    a = base < b ? base : b;
+    uint64_t top = b;                                     // one past the last byte looked at
+    for (; top > a; top -= top - a < 32 * kLaneBytes ? top - a : 32 * kLaneBytes) {
+        uint32_t m = 0;
+        for (int k = 0; k < kLaneBytes; k++) {
+            const uint64_t d = (uint64_t)(kLaneBytes * lane + k) + 1;
+            m |= (uint32_t)(d <= top - a && !is_ws(rd.at(top - d))) << k;
+        }
+        const uint32_t any = __ballot_sync(~0u, m != 0);
+        if (any) {
+            const int src = __ffs(any) - 1;
+            top -= (uint64_t)(kLaneBytes * src + __ffs(__shfl_sync(~0u, m, src)) - 1);
+            break;
+        }
+    }
+    b = top;
 }
 
 __device__ uint8_t decode_slot(const ValueParams& P, Reader& rd, uint64_t i, uint64_t a, uint64_t b)
@@ -511,50 +713,83 @@ __global__ void __launch_bounds__(kValThreads) decode_slots(ValueParams P)
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         Reader rd{&P, 0, 0, 0, nullptr};
         uint64_t a, b;
-        slot_range(P, rd, i, a, b);
+        slot_bounds(P, i, a, b);
         P.num[i] = 0;
         P.len[i] = 0;
-        const bool long_string = b - a > kShortBytes && rd.at(a) == '"';
-        uint8_t t = kValString;
-        if (!long_string) t = decode_slot(P, rd, i, a, b);
-        if (long_string || t == kValDeferred) {
+        const bool long_slot = b - a > kShortBytes;
+        uint8_t t = kValNone;
+        if (!long_slot) {
+            trim(rd, a, b);
+            t = decode_slot(P, rd, i, a, b);
+        }
+        if (long_slot || t == kValDeferred) {
             const uint32_t k = atomicAdd(P.n_long, 1u);
-            if (k < P.long_cap) P.long_list[k] = (uint32_t)i;            // decided by decode_deferred
-            else if (long_string) t = decode_slot(P, rd, i, a, b);       // the list is full
-            else t = kValDeferred;                                       // left for decode_swept
+            if (k < P.long_cap) {
+                P.long_list[k] = (uint32_t)i;                        // decided by decode_deferred
+            } else if (long_slot) {                                  // the list is full
+                trim(rd, a, b);
+                t = decode_slot(P, rd, i, a, b);                     // kValDeferred: left for decode_swept
+            }
         }
         P.type[i] = t;
     }
 }
 
-__device__ void decode_deferred_slot(const ValueParams& P, uint64_t i, uint8_t* digits)
+__device__ void decode_deferred_number(const ValueParams& P, Reader& rd, uint64_t i, uint64_t a, uint64_t b,
+                                       uint8_t* digits)
 {
-    Reader rd{&P, 0, 0, 0, nullptr};
-    uint64_t a, b;
-    slot_range(P, rd, i, a, b);
-    if (rd.at(a) == '"') {
-        P.type[i] = decode_slot(P, rd, i, a, b);
-    } else {
-        P.num[i] = decode_number_exact(rd, a, b, digits);
-        P.type[i] = kValDouble;
+    P.num[i] = decode_number_exact(rd, a, b, digits);
+    P.type[i] = kValDouble;
+}
+
+// a warp per listed slot (a long one, or a number that needs the exact
+// conversion): trimmed by the warp, then a string decoded by the whole warp,
+// anything else by its first lane
+__global__ void __launch_bounds__(kDeferredThreads) decode_deferred(ValueParams P)
+{
+    constexpr int kWarps = kDeferredThreads / 32;
+    __shared__ uint8_t digits[kWarps][kDecBuf];
+    __shared__ uint8_t stage[kWarps][kStage];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t n = min(*P.n_long, P.long_cap);
+    for (uint32_t k = blockIdx.x * kWarps + warp; k < n; k += gridDim.x * kWarps) {
+        const uint64_t i = P.long_list[k];
+        Reader rd{&P, 0, 0, 0, nullptr};
+        uint64_t a, b;
+        slot_bounds(P, i, a, b);
+        trim_warp(rd, a, b);
+        if (a < b && rd.at(a) == '"' && b - a >= 2 && rd.at(b - 1) == '"' && a >= rd.lo) {
+            // the whole string lies in the segment of its closing quote
+            const int64_t m = decode_string_warp(rd.base + (a + 1 - rd.lo), b - a - 2, P.str_out + a + 1,
+                                                 stage[warp]);
+            if (lane == 0) {
+                P.num[i] = m < 0 ? 0 : a + 1;
+                P.len[i] = m < 0 ? 0u : (uint32_t)m;
+                P.type[i] = m < 0 ? kValInvalid : kValString;
+            }
+        } else if (lane == 0) {
+            const uint8_t t = decode_slot(P, rd, i, a, b);
+            if (t == kValDeferred) decode_deferred_number(P, rd, i, a, b, digits[warp]);
+            else P.type[i] = t;
+        }
     }
 }
 
-__global__ void __launch_bounds__(kDeferredThreads) decode_deferred(ValueParams P)
+// only when the list overflowed: a thread per slot, the deferred numbers the
+// list did not hold
+__global__ void __launch_bounds__(kSweptThreads) decode_swept(ValueParams P)
 {
-    __shared__ uint8_t digits[kDeferredThreads][kDecBuf];
-    const uint32_t n = min(*P.n_long, P.long_cap);
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
-        decode_deferred_slot(P, P.long_list[k], digits[threadIdx.x]);
-}
-
-__global__ void __launch_bounds__(kDeferredThreads) decode_swept(ValueParams P)
-{
-    __shared__ uint8_t digits[kDeferredThreads][kDecBuf];
+    __shared__ uint8_t digits[kSweptThreads][kDecBuf];
     if (*P.n_long <= P.long_cap) return;                      // the list held every entry
     const uint64_t n = (uint64_t)P.S + 1;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-        if (P.type[i] == kValDeferred) decode_deferred_slot(P, i, digits[threadIdx.x]);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        if (P.type[i] != kValDeferred) continue;
+        Reader rd{&P, 0, 0, 0, nullptr};
+        uint64_t a, b;
+        slot_bounds(P, i, a, b);
+        trim(rd, a, b);
+        decode_deferred_number(P, rd, i, a, b, digits[threadIdx.x]);
+    }
 }
 
 // type counts
@@ -580,13 +815,13 @@ cudaError_t launch_decode_values(const ValueParams& p, int sm_count, cudaStream_
     (void)stream;
     cj_emu::launch(grid, kValThreads, 0, [&] { decode_slots(p); });
     cj_emu::launch(sm_count * 2, kDeferredThreads, 0, [&] { decode_deferred(p); });
-    cj_emu::launch(sm_count * 2, kDeferredThreads, 0, [&] { decode_swept(p); });
+    cj_emu::launch(sm_count * 2, kSweptThreads, 0, [&] { decode_swept(p); });
     cj_emu::launch(grid, kValThreads, 0, [&] { count_types(p); });
     return cudaSuccess;
 #else
     decode_slots<<<grid, kValThreads, 0, stream>>>(p);
-    decode_deferred<<<sm_count * 8, kDeferredThreads, 0, stream>>>(p);
-    decode_swept<<<sm_count * 8, kDeferredThreads, 0, stream>>>(p);
+    decode_deferred<<<sm_count * 16, kDeferredThreads, 0, stream>>>(p);
+    decode_swept<<<sm_count * 8, kSweptThreads, 0, stream>>>(p);
     count_types<<<grid, kValThreads, 0, stream>>>(p);
     return cudaGetLastError();
 #endif

@@ -7,6 +7,7 @@ check.  The kernels run through the CPU emulation here (tests/emu) and on the
 GPU in the tests marked gpu."""
 import ctypes
 import json
+import math
 import random
 import struct
 
@@ -55,7 +56,10 @@ def expected(text: bytes):
     if isinstance(v, int):
         if -(1 << 63) <= v < (1 << 63):
             return INT, v
-        return DOUBLE, float(v)
+        try:
+            return DOUBLE, float(v)
+        except OverflowError:                      # past the largest double: infinity
+            return DOUBLE, math.inf if v > 0 else -math.inf
     if isinstance(v, float):
         return DOUBLE, v
     return INVALID, None
@@ -168,6 +172,51 @@ def test_numbers(emu):
     assert counts[DOUBLE] > 2000 and counts[INT] > 300
 
 
+def long_strings_doc(seed: int, n: int) -> bytes:
+    """Strings of 300-3000 bytes built from every kind of piece (plain text,
+    multi-byte UTF-8, each escape, \\u escapes of 1-3 UTF-8 bytes, surrogate
+    pairs, backslash runs), so escapes straddle every lane and step boundary;
+    a fifth carry one fault (a lone or reversed surrogate, a bad escape or
+    hex digit, a raw control character)."""
+    rng = random.Random(seed)
+    pieces = ["a", "xyz", "caf\u00e9", "\\\"", "\\\\", "\\/", "\\b", "\\f", "\\n", "\\r", "\\t",
+              "\\u0041", "\\u00e9", "\\u20AC", "\\uffff", "\\ud83d\\ude00", "\\uD800\\uDFFF",
+              "\u00e9", "\u20ac", "\U0001f600", "\\\\\\\\", "\\\\u0041", " "]
+    faults = ["\\ud800", "\\udc00", "\\ude00\\ud83d", "\\x", "\\u12G4", "\\u12", "\x01",
+              "\\ud83d\\u0041", "\\ud83dx"]
+    out = []
+    for k in range(n):
+        parts, size = [], rng.randint(300, 3000)
+        while sum(map(len, parts)) < size:
+            p = rng.choice(pieces)
+            parts.append(p * rng.randint(1, 40) if p in ("a", "\\\\") else p)
+        if k % 5 == 4:
+            parts.insert(rng.randrange(len(parts) + 1), rng.choice(faults))
+        out.append('"' + "".join(parts) + '"')
+    return ("[" + ", ".join(out) + "]").encode("utf-8")
+
+
+LONG_SLOTS_DOC = (b"[" + b" " * 5000 + b"1, \"a\"" + b"\n" * 700 + b", " + b"1" * 400 + b", tru" + b" " * 3000
+                  + b"e, 0." + b"0" * 500 + b"1,\t" + b" \r\n" * 300 + b"\"" + b"x" * 900 + b"\"" + b" " * 999
+                  + b", -" + b"9" * 330 + b"e-700, 1e" + b"0" * 300 + b"1]" + b" " * 70000)
+
+
+def test_long_slots(emu):
+    """Slots longer than a thread takes: long whitespace runs (the slot after
+    the last structural among them), long numbers, a literal split by
+    spaces."""
+    pos, t, nums, lens, strs, counts = emu_values(emu, LONG_SLOTS_DOC)
+    check_values(LONG_SLOTS_DOC, pos, t, nums, lens, strs)
+    assert counts[INVALID] == 1 and counts[STRING] == 2 and counts[DOUBLE] == 4
+
+
+def test_long_strings(emu):
+    d = long_strings_doc(3, 120)
+    pos, t, nums, lens, strs, counts = emu_values(emu, d)
+    check_values(d, pos, t, nums, lens, strs)
+    assert counts[STRING] >= 80 and counts[INVALID] >= 20
+
+
 def halfway_doc(seed: int, n: int) -> bytes:
     """Exact halfway points between neighbouring doubles (normal and
     subnormal), each also nudged by one unit in its last written digit:
@@ -241,6 +290,8 @@ def _gpu_values(cj, ctx, data: bytes, lines=False):
 @pytest.mark.gpu
 def test_gpu_values(cj, ctx):
     _gpu_values(cj, ctx, STRING_DOC)
+    _gpu_values(cj, ctx, LONG_SLOTS_DOC)
+    _gpu_values(cj, ctx, long_strings_doc(17, 3000))
     _gpu_values(cj, ctx, number_doc(11, 20000))
     _gpu_values(cj, ctx, halfway_doc(13, 2000))
     _gpu_values(cj, ctx, ("[" + ",".join(f"{k % 97 + 1}e-{310 + k % 13}" for k in range(60000)) + "]").encode())
