@@ -512,7 +512,10 @@ class Context:
                "autotune")
         return best, [tried[i] for i in range(min(n.value, len(tried)))]
 
-    def timing(self, enable: bool = True) -> None:
+    def timing(self, enable: int = 1) -> None:
+        """cj_context_timing: 0 off; 1 (True) an event at every kernel
+        boundary; 2 events at the run's start, the scan's end and the run's
+        end only, so the kernels overlap their launches as untimed runs do."""
         _check(lib().cj_context_timing(self._h, int(enable)), "timing")
 
     def phase_ms(self):

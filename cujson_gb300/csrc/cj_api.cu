@@ -30,6 +30,15 @@
 
 using namespace cj;
 
+bool cj::dependent_launch_enabled()
+{
+    static const bool on = [] {
+        const char* e = getenv("CJ_PDL");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
 namespace {
 
 thread_local int g_last_status = CJ_OK;
@@ -168,7 +177,7 @@ struct cj_context {
     int64_t launches = 0;
     size_t dev_bytes = 0;
 
-    bool timing = false;
+    int timing = 0;                     // 0 off, 1 an event at every kernel boundary, 2 scan and run ends
     std::vector<cudaEvent_t> events;   // kEventsPerRun per recorded run
     size_t events_used = 0;
 
@@ -462,6 +471,7 @@ cj_status enqueue(cj_context* ctx, bool graph)
         ctx->events_used += kEventsPerRun;
         CJ_CUDA(cudaEventRecord(ev[0], ctx->stream));
     }
+    const bool fine = ev && ctx->timing == 1;
 
     ScanParams sp{};
     sp.in = ctx->in.p;
@@ -501,15 +511,20 @@ cj_status enqueue(cj_context* ctx, bool graph)
             wp.n_work = ctx->wave_nwork.p + 3 * w;
             wp.tickets = ctx->wave_nwork.p + 3 * w + 1;
             wp.work = ctx->work.p + 2 * (size_t)wp.r_begin;
-            launch_scan(wp, ctx->lines, shape, ctx->stream, ev ? ev + 1 : nullptr);
+            launch_scan(wp, ctx->lines, shape, ctx->stream, fine ? ev + 1 : nullptr);
             ctx->launches += scan_launches(wp.r_end - wp.r_begin);
             // no copy on the stream between waves: a copy queued behind a
             // scan that waits for input bytes could hold up the input's copies
             if (ctx->wave_stream) CJ_CUDA(cudaEventRecord(ctx->wave_ev[w], ctx->stream));
         }
     } else {
-        launch_scan(sp, ctx->lines, shape, ctx->stream, ev ? ev + 1 : nullptr);
+        launch_scan(sp, ctx->lines, shape, ctx->stream, fine ? ev + 1 : nullptr);
         ctx->launches += scan_launches(ctx->n_regions);
+    }
+    if (ev && !fine) {
+        // coarse timing: no events between the scan's kernels, which would
+        // keep each from being scheduled while the one before it finishes
+        for (int k = 1; k <= 3; k++) CJ_CUDA(cudaEventRecord(ev[k], ctx->stream));
     }
     if (ctx->batch) {
         launch_batch_prefix(ctx->segs.p, ctx->seg_out.p, ctx->n_segs, ctx->layout_off.p, ctx->rchunk_off.p,
@@ -543,8 +558,9 @@ cj_status enqueue(cj_context* ctx, bool graph)
                                      (size_t)ctx->sm_count * 8 * 256 / pthreads);
     if (ctx->tune_pair_blocks) grid = (int)std::min<size_t>((size_t)grid, ctx->tune_pair_blocks);
     launch_pair(pp, grid, ctx->stream, (int)pthreads);
-    if (ev) CJ_CUDA(cudaEventRecord(ev[4], ctx->stream));
+    if (fine) CJ_CUDA(cudaEventRecord(ev[4], ctx->stream));
     launch_spine(pp, grid, ctx->stream, (int)pthreads);
+    if (ev && !fine) CJ_CUDA(cudaEventRecord(ev[4], ctx->stream));
     if (ev) CJ_CUDA(cudaEventRecord(ev[5], ctx->stream));
     ctx->launches += 2;
     if (ctx->batch) {
@@ -1305,7 +1321,7 @@ void cj_context_destroy(cj_context* ctx)
 cj_status cj_context_timing(cj_context* ctx, int enable)
 {
     if (!ctx) return CJ_ERR_INVALID_ARGUMENT;
-    ctx->timing = enable != 0;
+    ctx->timing = enable < 0 ? 0 : (enable > 2 ? 1 : enable);
     ctx->events_used = 0;
     return CJ_OK;
 }

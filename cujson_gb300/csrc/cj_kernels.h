@@ -8,6 +8,47 @@
 
 namespace cj {
 
+// Programmatic dependent launch.  A kernel launched by launch_dependent may
+// be scheduled while the kernel before it on the stream is still running; it
+// calls wait_previous_grid() before touching anything that kernel wrote (the
+// wait returns once that grid has completed and its writes are visible; for
+// a plain launch it returns at once).  allow_next_grid() lets the next
+// kernel's blocks be scheduled as soon as every block of this grid has
+// started; without it they are scheduled as this grid's blocks exit.
+__device__ __forceinline__ void wait_previous_grid()
+{
+#ifdef __CUDA_ARCH__
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+#endif
+}
+__device__ __forceinline__ void allow_next_grid()
+{
+#ifdef __CUDA_ARCH__
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
+}
+// whether launch_dependent sets the attribute (CJ_PDL=0 in the environment
+// turns it off, for comparison)
+bool dependent_launch_enabled();
+#ifndef CJ_EMU
+template <typename... Params, typename... Args>
+inline cudaError_t launch_dependent(void (*kernel)(Params...), int grid, int block, size_t smem,
+                                    cudaStream_t stream, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = dependent_launch_enabled() ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+#endif
+
 struct ScanParams {
     const uint8_t* in;
     const Segment* segs;

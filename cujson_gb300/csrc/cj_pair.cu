@@ -146,6 +146,8 @@ __device__ __forceinline__ uint32_t doc_of_item(const PairParams& P, uint64_t w)
 
 __global__ void __launch_bounds__(256) pair_chunks(PairParams P)
 {
+    allow_next_grid();
+    wait_previous_grid();
 #ifdef CJ_EMU
     uint32_t* s_heads_all = reinterpret_cast<uint32_t*>(cj_emu::g_dyn_smem.data());
 #else
@@ -300,6 +302,7 @@ __global__ void __launch_bounds__(256) pair_spine(PairParams P)
 {
     const int lane = threadIdx.x & 31;
     const bool batch = P.rchunk_off != nullptr;
+    wait_previous_grid();
     if (__ldcg(&P.ctrl->error_flags) & CJ_FLAG_OVERFLOW) return;
     const uint32_t K = batch ? 0u : P.ctrl->k_total;
     const uint64_t nch = batch ? P.n_chunks : ((uint64_t)K + kChunk - 1) / kChunk;
@@ -400,7 +403,7 @@ void launch_pair(const PairParams& p, int grid, cudaStream_t stream, int threads
     (void)stream;
     cj_emu::launch(grid, threads, smem, [&] { pair_chunks(p); });
 #else
-    pair_chunks<<<grid, threads, smem, stream>>>(p);
+    launch_dependent(pair_chunks, grid, threads, smem, stream, p);
 #endif
 }
 
@@ -410,7 +413,7 @@ void launch_spine(const PairParams& p, int grid, cudaStream_t stream, int thread
     (void)stream;
     cj_emu::launch(grid, threads, 0, [&] { pair_spine(p); });
 #else
-    pair_spine<<<grid, threads, 0, stream>>>(p);
+    launch_dependent(pair_spine, grid, threads, 0, stream, p);
 #endif
 }
 

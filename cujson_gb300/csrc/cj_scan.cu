@@ -448,6 +448,7 @@ __device__ __forceinline__ void region_table(const ScanParams& P, const Region& 
 template <bool LINES, int R>
 __global__ void __launch_bounds__(kThreads, kTablesMinBlocks) scan_tables(ScanParams P)
 {
+    allow_next_grid();
     const int lane = threadIdx.x & 31;
     const uint32_t lt = lanemask_lt();
     const uint32_t nw = gridDim.x * kWarpsPerBlock;
@@ -609,6 +610,8 @@ __device__ __forceinline__ void block_scan_sums(const Sums& v, Sums* sm, int lan
 __global__ void __launch_bounds__(kPrefixPerBlock) prefix_reduce(ScanParams P)
 {
     __shared__ Ent s_w[kPrefixWarps][4];
+    allow_next_grid();
+    wait_previous_grid();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t r = P.r_begin + blockIdx.x * (uint32_t)kPrefixPerBlock + threadIdx.x;
     Ent t[4];
@@ -639,6 +642,8 @@ __global__ void __launch_bounds__(kPrefixPerBlock) prefix_apply(ScanParams P)
     __shared__ Sums s_sum[kPrefixWarps + 1];
     __shared__ uint32_t s_cnt[kPrefixWarps];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    allow_next_grid();
+    wait_previous_grid();
     if (aborted(P.ctrl)) return;          // a timed-out run writes no outputs
     const uint32_t n = P.n_regions;
     const uint32_t b = blockIdx.x;
@@ -921,6 +926,8 @@ __global__ void __launch_bounds__(kThreads, kEmitMinBlocks) scan_emit(ScanParams
 {
     __shared__ EmitStage s_stage[kWarpsPerBlock];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    allow_next_grid();
+    wait_previous_grid();
     if (aborted(P.ctrl)) return;
     const uint32_t n = *reinterpret_cast<const volatile uint32_t*>(P.n_work ? P.n_work : &P.ctrl->n_work);
     const uint32_t nw = gridDim.x * kWarpsPerBlock;
@@ -958,10 +965,10 @@ void launch_r(const ScanParams& p, bool lines, int tables_grid, int emit_grid, c
     if (lines) scan_tables<true, R><<<tables_grid, kThreads, 0, stream>>>(p);
     else scan_tables<false, R><<<tables_grid, kThreads, 0, stream>>>(p);
     if (ev) cudaEventRecord(ev[0], stream);
-    if (nb > 1) prefix_reduce<<<nb, kPrefixPerBlock, 0, stream>>>(p);
-    prefix_apply<<<nb, kPrefixPerBlock, 0, stream>>>(p);
+    if (nb > 1) launch_dependent(prefix_reduce, (int)nb, kPrefixPerBlock, 0, stream, p);
+    launch_dependent(prefix_apply, (int)nb, kPrefixPerBlock, 0, stream, p);
     if (ev) cudaEventRecord(ev[1], stream);
-    scan_emit<R><<<emit_grid, kThreads, 0, stream>>>(p);
+    launch_dependent(scan_emit<R>, emit_grid, kThreads, 0, stream, p);
     if (ev) cudaEventRecord(ev[2], stream);
 #endif
 }
