@@ -88,6 +88,8 @@ __global__ void __launch_bounds__(1024) batch_prefix(const Segment* __restrict__
     __shared__ uint64_t warp_tot[2][32];
     __shared__ uint64_t carry_s[2];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+    allow_next_grid();
+    wait_previous_grid();
     if (tid == 0) carry_s[0] = carry_s[1] = 0;
     __syncthreads();
     for (uint32_t base = 0; base < n; base += blockDim.x) {
@@ -155,6 +157,7 @@ __global__ void __launch_bounds__(256) batch_layout(const Segment* __restrict__ 
                                                     int32_t* __restrict__ layout)
 {
     const int lane = threadIdx.x & 31;
+    wait_previous_grid();
     const uint64_t total = __ldcg(off + n);
     const uint64_t per_run = 32ull * kLayoutRun;
     const uint64_t runs = (total + per_run - 1) / per_run;
@@ -219,14 +222,14 @@ void launch_batch_scatter(const uint8_t* packed, const uint64_t* src_off, const 
 void launch_batch_prefix(const Segment* segs, const SegmentOut* seg_out, uint32_t n, uint64_t* layout_off,
                          uint64_t* rchunk_off, cudaStream_t stream)
 {
-    batch_prefix<<<1, 1024, 0, stream>>>(segs, seg_out, n, layout_off, rchunk_off);
+    launch_dependent(batch_prefix, 1, 1024, 0, stream, segs, seg_out, n, layout_off, rchunk_off);
 }
 
 void launch_batch_layout(const Segment* segs, const SegmentOut* seg_out, uint32_t n, const int32_t* pos,
                          const int32_t* pair, const uint64_t* off, int32_t* layout, int sm_count,
                          cudaStream_t stream)
 {
-    batch_layout<<<sm_count * 8, 256, 0, stream>>>(segs, seg_out, n, pos, pair, off, layout);
+    launch_dependent(batch_layout, sm_count * 8, 256, 0, stream, segs, seg_out, n, pos, pair, off, layout);
 }
 
 }  // namespace cj

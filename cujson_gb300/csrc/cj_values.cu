@@ -709,6 +709,7 @@ __device__ uint8_t decode_slot(const ValueParams& P, Reader& rd, uint64_t i, uin
 
 __global__ void __launch_bounds__(kValThreads) decode_slots(ValueParams P)
 {
+    allow_next_grid();
     const uint64_t n = (uint64_t)P.S + 1;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         Reader rd{&P, 0, 0, 0, nullptr};
@@ -751,6 +752,8 @@ __global__ void __launch_bounds__(kDeferredThreads) decode_deferred(ValueParams 
     __shared__ uint8_t digits[kWarps][kDecBuf];
     __shared__ uint8_t stage[kWarps][kStage];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    allow_next_grid();
+    wait_previous_grid();
     const uint32_t n = min(*P.n_long, P.long_cap);
     for (uint32_t k = blockIdx.x * kWarps + warp; k < n; k += gridDim.x * kWarps) {
         const uint64_t i = P.long_list[k];
@@ -780,6 +783,8 @@ __global__ void __launch_bounds__(kDeferredThreads) decode_deferred(ValueParams 
 __global__ void __launch_bounds__(kSweptThreads) decode_swept(ValueParams P)
 {
     __shared__ uint8_t digits[kSweptThreads][kDecBuf];
+    allow_next_grid();
+    wait_previous_grid();
     if (*P.n_long <= P.long_cap) return;                      // the list held every entry
     const uint64_t n = (uint64_t)P.S + 1;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -797,6 +802,7 @@ __global__ void __launch_bounds__(kValThreads) count_types(ValueParams P)
 {
     __shared__ unsigned long long c[kValTypes];
     if (threadIdx.x < kValTypes) c[threadIdx.x] = 0;
+    wait_previous_grid();
     __syncthreads();
     const uint64_t n = (uint64_t)P.S + 1;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
@@ -820,9 +826,9 @@ cudaError_t launch_decode_values(const ValueParams& p, int sm_count, cudaStream_
     return cudaSuccess;
 #else
     decode_slots<<<grid, kValThreads, 0, stream>>>(p);
-    decode_deferred<<<sm_count * 16, kDeferredThreads, 0, stream>>>(p);
-    decode_swept<<<sm_count * 8, kSweptThreads, 0, stream>>>(p);
-    count_types<<<grid, kValThreads, 0, stream>>>(p);
+    launch_dependent(decode_deferred, sm_count * 16, kDeferredThreads, 0, stream, p);
+    launch_dependent(decode_swept, sm_count * 8, kSweptThreads, 0, stream, p);
+    launch_dependent(count_types, grid, kValThreads, 0, stream, p);
     return cudaGetLastError();
 #endif
 }
