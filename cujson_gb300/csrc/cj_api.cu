@@ -1796,12 +1796,16 @@ cj_status cj_decode_values(cj_context* ctx, cj_value_counts* counts)
     if (info.status != CJ_OK) return (cj_status)info.status;
     CJ_CUDA(cudaSetDevice(ctx->device));
     const uint64_t S = (uint64_t)info.n_structural, slots = S + 1;
-    if ((st = ensure(ctx, ctx->val_type, slots))) return st;
+    if ((st = ensure(ctx, ctx->val_type, slots + 4))) return st;     // read a word at a time
     if ((st = ensure(ctx, ctx->val_num, slots))) return st;
     if ((st = ensure(ctx, ctx->val_len, slots))) return st;
     if ((st = ensure(ctx, ctx->val_str, ctx->n_bytes + 1))) return st;
-    const uint64_t long_cap = ctx->n_bytes / 256 + 1;
-    if ((st = ensure(ctx, ctx->val_long, long_cap + 1))) return st;    // the list, then its counter
+    // the lists of the second kernel, then their counters: slots longer than
+    // 256 bytes (at most n / 257 of them), and escaped strings and numbers
+    // for the exact conversion (those past n / 64 are decoded in place)
+    const uint64_t long_cap = std::min<uint64_t>(ctx->n_bytes / 256 + 1, 0xFFFFFFFFull);
+    const uint64_t short_cap = std::min<uint64_t>(ctx->n_bytes / 64 + 1, 0xFFFFFFFFull);
+    if ((st = ensure(ctx, ctx->val_long, long_cap + short_cap + 3))) return st;
     if ((st = ensure(ctx, ctx->val_counts, kValTypes))) return st;
     if (!ctx->pow5.p) {
         if ((st = ensure(ctx, ctx->pow5, 2 * 651))) return st;
@@ -1819,11 +1823,13 @@ cj_status cj_decode_values(cj_context* ctx, cj_value_counts* counts)
     vp.len = ctx->val_len.p;
     vp.str_out = ctx->val_str.p;
     vp.long_list = ctx->val_long.p;
-    vp.long_cap = (uint32_t)std::min<uint64_t>(long_cap, 0xFFFFFFFFull);
-    vp.n_long = ctx->val_long.p + long_cap;
+    vp.long_cap = (uint32_t)long_cap;
+    vp.short_list = ctx->val_long.p + long_cap;
+    vp.short_cap = (uint32_t)short_cap;
+    vp.counters = ctx->val_long.p + long_cap + short_cap;
     vp.counts = ctx->val_counts.p;
     vp.pow5 = ctx->pow5.p;
-    CJ_CUDA(cudaMemsetAsync(vp.n_long, 0, sizeof(uint32_t), ctx->stream));
+    CJ_CUDA(cudaMemsetAsync(vp.counters, 0, 3 * sizeof(uint32_t), ctx->stream));
     CJ_CUDA(cudaMemsetAsync(ctx->val_counts.p, 0, kValTypes * sizeof(unsigned long long), ctx->stream));
     if (launch_decode_values(vp, ctx->sm_count, ctx->stream) != cudaSuccess) return CJ_ERR_CUDA;
     ctx->launches += 4;

@@ -174,9 +174,11 @@ struct ValueParams {
     uint64_t* num;                 // int64 / double bits / decoded string's offset in str_out
     uint32_t* len;                 // decoded string length
     uint8_t* str_out;              // n_bytes: decoded strings at their content offsets
-    uint32_t* long_list;           // slots for the second kernel: long strings, deferred numbers
+    uint32_t* long_list;           // slots longer than the first kernel takes, for the second
     uint32_t long_cap;
-    uint32_t* n_long;              // entries wanted (more than long_cap: the rest are swept)
+    uint32_t* short_list;          // escaped strings and numbers for the exact conversion, likewise
+    uint32_t short_cap;
+    uint32_t* counters;            // entries wanted in each list, then the short list's ticket
     unsigned long long* counts;    // kValTypes
     const uint64_t* pow5;          // kPow5Table on the device
 };

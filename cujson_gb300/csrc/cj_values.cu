@@ -10,9 +10,11 @@
 // Each slot's text, less JSON whitespace at both ends, is one of: nothing,
 // a string, a number, a literal -- anything else is marked invalid.
 //
-//   decode_slots   one thread per slot; a string longer than kShortBytes goes
-//                  to a list instead, so one long string does not hold up a
-//                  warp of short ones;
+//   decode_slots   one thread per slot; a string without escapes copied four
+//                  bytes a store; a slot longer than kShortBytes, or a string
+//                  that holds an escape, goes to a list instead, so that one
+//                  long or escaped string does not hold up a warp of short
+//                  plain ones;
 //   decode_deferred, decode_swept: below.
 //
 // A string's decoded bytes are written at its own content offset in the
@@ -47,6 +49,7 @@ namespace cj {
 namespace {
 
 constexpr uint32_t kShortBytes = 256;     // longer strings go to the second kernel
+constexpr uint32_t FULL_MASK = 0xFFFFFFFFu;
 constexpr int kValThreads = 256;
 
 __device__ __forceinline__ bool is_ws(uint8_t c) { return c == ' ' || c == '\t' || c == '\n' || c == '\r'; }
@@ -159,6 +162,43 @@ __device__ int64_t decode_string(Reader& rd, uint64_t a, uint64_t b, uint8_t* ou
     return (int64_t)(o - (a + 1));
 }
 
+// the 4 bytes at p, whatever its alignment (two aligned loads; the input
+// buffer has slack after every segment)
+__device__ __forceinline__ uint32_t load4(const uint8_t* p)
+{
+    const uintptr_t u = reinterpret_cast<uintptr_t>(p);
+    const uint32_t* q = reinterpret_cast<const uint32_t*>(u & ~(uintptr_t)3);
+    const uint32_t sh = (uint32_t)(u & 3u) * 8u;
+    const uint32_t lo = __ldg(q);
+    return sh ? __funnelshift_r(lo, __ldg(q + 1), sh) : lo;
+}
+
+// a string without escapes, quotes or control bytes (most strings), copied
+// to out at its own offsets, four bytes a store in the middle: content
+// [s0, e), all in the reader's current segment (the closing quote's).
+// Returns its length, or -1 when it holds a byte that needs decode_string.
+__device__ int64_t copy_plain(Reader& rd, uint64_t s0, uint64_t e, uint8_t* out)
+{
+    const uint8_t* src = rd.base - rd.lo;                       // logical offset x at src + x
+    uint64_t x = s0;
+    for (; x < e && (x & 3u); x++) {
+        const uint8_t c = __ldg(src + x);
+        if (c == '\\' || c == '"' || c < 0x20u) return -1;
+        out[x] = c;
+    }
+    for (; x + 4 <= e; x += 4) {
+        const uint32_t v = load4(src + x);
+        if (__vcmpeq4(v, 0x5C5C5C5Cu) | __vcmpeq4(v, 0x22222222u) | __vcmpltu4(v, 0x20202020u)) return -1;
+        *reinterpret_cast<uint32_t*>(out + x) = v;
+    }
+    for (; x < e; x++) {
+        const uint8_t c = __ldg(src + x);
+        if (c == '\\' || c == '"' || c < 0x20u) return -1;
+        out[x] = c;
+    }
+    return (int64_t)(e - s0);
+}
+
 // ---- long strings: a warp per string ------------------------------------------------
 //
 // The string's content is taken 512 bytes a step, 16 bytes a lane, staged in
@@ -174,6 +214,7 @@ __device__ int64_t decode_string(Reader& rd, uint64_t a, uint64_t b, uint8_t* ou
 constexpr int kLaneBytes = 16;
 constexpr int kWinBefore = 8, kWinAfter = 12;
 constexpr int kWarpStep = 32 * kLaneBytes;
+constexpr int kWin = kWinBefore + kLaneBytes + kWinAfter;
 constexpr int kStage = kWinBefore + kWarpStep + kWinAfter;
 
 __device__ __forceinline__ int hex4(const uint8_t* p)
@@ -245,14 +286,49 @@ __device__ int emit_byte(const uint8_t* w, uint64_t st, int j, uint64_t q, uint6
     return 1;
 }
 
-// a warp decodes the content src[0, len) of one string into out, staging
-// through `stage` (kStage bytes of shared memory, this warp's); every lane
-// returns the decoded length, or -1 when it is not a valid JSON string
+// the four-bit mask of the bytes of w equal to the byte of c4 (repeated), and
+// of those below it: bit i for byte i
+__device__ __forceinline__ uint32_t nib_eq(uint32_t w, uint32_t c4)
+{
+    return ((__vcmpeq4(w, c4) & 0x80808080u) * 0x00204081u) >> 28;
+}
+__device__ __forceinline__ uint32_t nib_lt(uint32_t w, uint32_t c4)
+{
+    return ((__vcmpltu4(w, c4) & 0x80808080u) * 0x00204081u) >> 28;
+}
+
+// escape starts (backslashes that are not themselves escaped) of the bytes
+// whose backslashes are `bs` (bit i = byte i), byte 0 escaped when e0: each
+// run of backslashes starts an escape at every other byte from its first --
+// from its second when the run starts at an escaped byte 0.  The runs that
+// start at odd bits are found by the carry of one addition per run.
+__device__ __forceinline__ uint64_t escape_starts(uint64_t bs, uint32_t e0)
+{
+    constexpr uint64_t kEven = 0x5555555555555555ull;
+    const uint64_t starts = bs & ~(bs << 1);
+    const uint64_t os = (starts & ~kEven) | (e0 ? (bs & 1ull) : 0ull);     // runs whose first escape is at an odd bit
+    const uint64_t odd_runs = ((bs + os) ^ bs) & bs;
+    return ((bs & ~odd_runs) & kEven) | (odd_runs & ~kEven);
+}
+
+__device__ __forceinline__ uint8_t unescape(uint8_t c)
+{
+    return c == 'b' ? '\b' : c == 'f' ? '\f' : c == 'n' ? '\n' : c == 'r' ? '\r' : c == 't' ? '\t' : c;
+}
+
+// a warp decodes the content src[0, len) of one string into out, staging its
+// input through `stage` (kStage bytes) and its output through `ostage`
+// (kWarpStep + 8 bytes) of shared memory, this warp's; every lane returns the
+// decoded length, or -1 when it is not a valid JSON string.  A lane whose
+// window holds no escaped u takes its bytes by masks: an escape start emits
+// its unescaped character, the escaped character nothing, any other byte
+// itself; a lane with an escaped u goes byte by byte.
 __device__ int64_t decode_string_warp(const uint8_t* __restrict__ src, uint64_t len, uint8_t* __restrict__ out,
-                                      uint8_t* stage)
+                                      uint8_t* stage, uint8_t* ostage)
 {
     const int lane = (int)(threadIdx.x & 31);
     const uint8_t* w = stage + kLaneBytes * lane;               // this lane's window
+    const uint32_t* ww = reinterpret_cast<const uint32_t*>(w);
     uint32_t carry = 0;           // escaped-state at the step's first byte
     uint32_t prev8 = 0;           // that state 8 bytes before lane 0's first byte
     uint64_t done = 0;            // bytes written
@@ -263,15 +339,21 @@ __device__ int64_t decode_string_warp(const uint8_t* __restrict__ src, uint64_t 
             stage[k] = (q >= 0 && (uint64_t)q < len) ? __ldg(src + q) : (uint8_t)0;
         }
         __syncwarp();
-        // this lane's state map, then the warp's scan of maps
-        uint32_t e0 = 0, e1 = 1;
-        for (int j = kWinBefore; j < kWinBefore + kLaneBytes; j++) {
-            const uint32_t bs = w[j] == '\\';
-            e0 = !e0 & bs;
-            e1 = !e1 & bs;
+        // masks of the window's 36 bytes: backslashes, u, quotes, control bytes
+        uint64_t B = 0, U = 0, Q = 0, C = 0;
+#pragma unroll
+        for (int k = 0; k < kWin / 4; k++) {
+            const uint32_t x = ww[k];
+            B |= (uint64_t)nib_eq(x, 0x5C5C5C5Cu) << (4 * k);
+            U |= (uint64_t)nib_eq(x, 0x75757575u) << (4 * k);
+            Q |= (uint64_t)nib_eq(x, 0x22222222u) << (4 * k);
+            C |= (uint64_t)nib_lt(x, 0x20202020u) << (4 * k);
         }
-        uint32_t m = e0 | (e1 << 1);
-        #pragma unroll
+        // this lane's state map over its own 16 bytes, then the warp's scan of maps
+        const uint64_t bown = (B >> kWinBefore) & 0xFFFFull;
+        const uint64_t st0 = escape_starts(bown, 0), st1 = escape_starts(bown, 1);
+        uint32_t m = (uint32_t)((st0 >> 15) & 1u) | (uint32_t)(((st1 >> 15) & 1u) << 1);
+#pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
             const uint32_t up = __shfl_up_sync(~0u, m, d);
             if (lane >= d) m = ((m >> (up & 1u)) & 1u) | (((m >> ((up >> 1) & 1u)) & 1u) << 1);
@@ -280,37 +362,57 @@ __device__ int64_t decode_string_warp(const uint8_t* __restrict__ src, uint64_t 
         const uint32_t cin = lane ? (excl >> carry) & 1u : carry;
         carry = (__shfl_sync(~0u, m, 31) >> carry) & 1u;
         // the state 8 bytes in, handed to the next lane as its window's start
-        uint32_t e = cin;
-        for (int j = kWinBefore; j < kWinBefore + 8; j++) e = !e & (uint32_t)(w[j] == '\\');
-        uint32_t start = __shfl_up_sync(~0u, e, 1);
+        const uint32_t e8 = (uint32_t)(((cin ? st1 : st0) >> 7) & 1u);
+        uint32_t start = __shfl_up_sync(~0u, e8, 1);
         if (lane == 0) start = prev8;
-        prev8 = __shfl_sync(~0u, e, 31);
-        uint64_t st = 0;
-        e = start;
-        for (int j = 0; j < kWinBefore + kLaneBytes + kWinAfter; j++) {
-            e = !e & (uint32_t)(w[j] == '\\');
-            st |= (uint64_t)e << j;
-        }
-        // count, place, write
+        prev8 = __shfl_sync(~0u, e8, 31);
+        const uint64_t st = escape_starts(B & ((1ull << kWin) - 1), start);
+        const uint64_t esc = (st << 1) | start;                 // escaped bytes
+        // count and check this lane's bytes
         const uint64_t q0 = c0 + (uint64_t)kLaneBytes * lane;
         const int own = q0 >= len ? 0 : len - q0 < (uint64_t)kLaneBytes ? (int)(len - q0) : kLaneBytes;
+        const uint64_t ownm = (((1ull << own) - 1) << kWinBefore);
+        const bool slow = (U & esc & (0x1FFFFFull << 4)) != 0;  // an escaped u whose escape reaches this lane
         int n = 0;
         bool bad = false;
-        for (int j = 0; j < own; j++) {
-            const int k = emit_byte(w, st, kWinBefore + j, q0 + j, len, nullptr);
-            bad |= k < 0;
-            n += k;
+        if (slow) {
+            for (int j = 0; j < own; j++) {
+                const int k = emit_byte(w, st, kWinBefore + j, q0 + j, len, nullptr);
+                bad |= k < 0;
+                n += k;
+            }
+        } else {
+            n = __popcll(ownm & ~esc);
+            bad = (ownm & ~esc & ~st & (Q | C)) != 0;            // a bare quote or control byte
+            // escapes: of what follows each start, a backslash or quote is
+            // always valid; the rest are checked one by one
+            const uint64_t est = st & ownm;
+            if (est >> (kWinBefore + own - 1) & 1ull && q0 + own == len) bad = true;   // the last byte
+            for (uint64_t r = (est << 1) & ~(B | Q); r; r &= r - 1) {
+                const uint8_t c = w[__ffsll((long long)r) - 1];
+                bad |= !(c == '/' || c == 'b' || c == 'f' || c == 'n' || c == 'r' || c == 't');
+            }
         }
         if (__any_sync(~0u, bad)) return -1;
         int pre = n;
-        #pragma unroll
+#pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
             const int up = __shfl_up_sync(~0u, pre, d);
             if (lane >= d) pre += up;
         }
-        uint8_t* o = out + done + (pre - n);
-        for (int j = 0; j < own; j++) o += emit_byte(w, st, kWinBefore + j, q0 + j, len, o);
-        done += (uint64_t)__shfl_sync(~0u, pre, 31);
+        uint8_t* o = ostage + (pre - n);
+        if (slow) {
+            for (int j = 0; j < own; j++) o += emit_byte(w, st, kWinBefore + j, q0 + j, len, o);
+        } else {
+            for (uint64_t r = ownm & ~esc; r; r &= r - 1) {
+                const int j = __ffsll((long long)r) - 1;
+                *o++ = (st >> j) & 1ull ? unescape(w[j + 1]) : w[j];
+            }
+        }
+        __syncwarp();
+        const int total = __shfl_sync(~0u, pre, 31);
+        for (int k = lane; k < total; k += 32) out[done + k] = ostage[k];
+        done += (uint64_t)total;
     }
     return (int64_t)done;
 }
@@ -678,13 +780,19 @@ __device__ void trim_warp(Reader& rd, uint64_t& a, uint64_t& b)
     b = top;
 }
 
-__device__ uint8_t decode_slot(const ValueParams& P, Reader& rd, uint64_t i, uint64_t a, uint64_t b)
+// slot i's trimmed text [a, b) decoded.  With defer_escapes, a string that
+// holds an escape is left to the warp kernel (kValDeferred): one long escaped
+// string would otherwise hold up the 31 other slots of its warp.
+__device__ uint8_t decode_slot(const ValueParams& P, Reader& rd, uint64_t i, uint64_t a, uint64_t b,
+                               bool defer_escapes)
 {
     if (a == b) return kValNone;
     const uint8_t c = rd.at(a);
     if (c == '"') {
         if (b - a < 2 || rd.at(b - 1) != '"') return kValInvalid;
-        const int64_t n = decode_string(rd, a, b - 1, P.str_out);
+        int64_t n = a >= rd.lo ? copy_plain(rd, a + 1, b - 1, P.str_out) : -1;
+        if (n < 0 && defer_escapes) return kValDeferred;
+        if (n < 0) n = decode_string(rd, a, b - 1, P.str_out);
         if (n < 0) return kValInvalid;
         P.num[i] = a + 1;                 // where the decoded bytes start
         P.len[i] = (uint32_t)n;
@@ -721,16 +829,20 @@ __global__ void __launch_bounds__(kValThreads) decode_slots(ValueParams P)
         uint8_t t = kValNone;
         if (!long_slot) {
             trim(rd, a, b);
-            t = decode_slot(P, rd, i, a, b);
+            t = decode_slot(P, rd, i, a, b, true);
         }
-        if (long_slot || t == kValDeferred) {
-            const uint32_t k = atomicAdd(P.n_long, 1u);
+        if (long_slot) {
+            const uint32_t k = atomicAdd(P.counters, 1u);
             if (k < P.long_cap) {
                 P.long_list[k] = (uint32_t)i;                        // decided by decode_deferred
-            } else if (long_slot) {                                  // the list is full
+            } else {                                                 // (cannot fill: kept for safety)
                 trim(rd, a, b);
-                t = decode_slot(P, rd, i, a, b);                     // kValDeferred: left for decode_swept
+                t = decode_slot(P, rd, i, a, b, false);
             }
+        } else if (t == kValDeferred) {
+            const uint32_t k = atomicAdd(P.counters + 1, 1u);
+            if (k < P.short_cap) P.short_list[k] = (uint32_t)i;       // decided by decode_deferred
+            else t = decode_slot(P, rd, i, a, b, false);             // strings here; numbers left for decode_swept
         }
         P.type[i] = t;
     }
@@ -743,38 +855,52 @@ __device__ void decode_deferred_number(const ValueParams& P, Reader& rd, uint64_
     P.type[i] = kValDouble;
 }
 
-// a warp per listed slot (a long one, or a number that needs the exact
-// conversion): trimmed by the warp, then a string decoded by the whole warp,
-// anything else by its first lane
+// a warp per listed slot: trimmed by the warp, then a string decoded by the
+// whole warp, anything else by its first lane
+__device__ void decode_listed(const ValueParams& P, uint64_t i, uint8_t* stage, uint8_t* ostage, uint8_t* digits)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    Reader rd{&P, 0, 0, 0, nullptr};
+    uint64_t a, b;
+    slot_bounds(P, i, a, b);
+    trim_warp(rd, a, b);
+    if (a < b && rd.at(a) == '"' && b - a >= 2 && rd.at(b - 1) == '"' && a >= rd.lo) {
+        // the whole string lies in the segment of its closing quote
+        const int64_t m = decode_string_warp(rd.base + (a + 1 - rd.lo), b - a - 2, P.str_out + a + 1, stage, ostage);
+        if (lane == 0) {
+            P.num[i] = m < 0 ? 0 : a + 1;
+            P.len[i] = m < 0 ? 0u : (uint32_t)m;
+            P.type[i] = m < 0 ? kValInvalid : kValString;
+        }
+    } else if (lane == 0) {
+        const uint8_t t = decode_slot(P, rd, i, a, b, false);
+        if (t == kValDeferred) decode_deferred_number(P, rd, i, a, b, digits);
+        else P.type[i] = t;
+    }
+}
+
+// the long slots first, a warp each in turn; then the short list, taken four
+// entries at a time from a ticket, so that warps done early take more
 __global__ void __launch_bounds__(kDeferredThreads) decode_deferred(ValueParams P)
 {
     constexpr int kWarps = kDeferredThreads / 32;
+    constexpr uint32_t kTake = 4;
     __shared__ uint8_t digits[kWarps][kDecBuf];
-    __shared__ uint8_t stage[kWarps][kStage];
+    __shared__ __align__(16) uint8_t stage[kWarps][kStage];
+    __shared__ uint8_t ostage[kWarps][kWarpStep + 8];    // a step's escape may emit 3 bytes past its input
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     allow_next_grid();
     wait_previous_grid();
-    const uint32_t n = min(*P.n_long, P.long_cap);
-    for (uint32_t k = blockIdx.x * kWarps + warp; k < n; k += gridDim.x * kWarps) {
-        const uint64_t i = P.long_list[k];
-        Reader rd{&P, 0, 0, 0, nullptr};
-        uint64_t a, b;
-        slot_bounds(P, i, a, b);
-        trim_warp(rd, a, b);
-        if (a < b && rd.at(a) == '"' && b - a >= 2 && rd.at(b - 1) == '"' && a >= rd.lo) {
-            // the whole string lies in the segment of its closing quote
-            const int64_t m = decode_string_warp(rd.base + (a + 1 - rd.lo), b - a - 2, P.str_out + a + 1,
-                                                 stage[warp]);
-            if (lane == 0) {
-                P.num[i] = m < 0 ? 0 : a + 1;
-                P.len[i] = m < 0 ? 0u : (uint32_t)m;
-                P.type[i] = m < 0 ? kValInvalid : kValString;
-            }
-        } else if (lane == 0) {
-            const uint8_t t = decode_slot(P, rd, i, a, b);
-            if (t == kValDeferred) decode_deferred_number(P, rd, i, a, b, digits[warp]);
-            else P.type[i] = t;
-        }
+    const uint32_t nl = min(__ldcg(P.counters), P.long_cap), ns = min(__ldcg(P.counters + 1), P.short_cap);
+    for (uint32_t k = blockIdx.x * kWarps + warp; k < nl; k += gridDim.x * kWarps)
+        decode_listed(P, P.long_list[k], stage[warp], ostage[warp], digits[warp]);
+    for (;;) {
+        uint32_t k = 0;
+        if (lane == 0) k = atomicAdd(P.counters + 2, kTake);
+        k = __shfl_sync(FULL_MASK, k, 0);
+        if (k >= ns) break;
+        for (uint32_t e = k; e < k + kTake && e < ns; e++)
+            decode_listed(P, P.short_list[e], stage[warp], ostage[warp], digits[warp]);
     }
 }
 
@@ -785,7 +911,7 @@ __global__ void __launch_bounds__(kSweptThreads) decode_swept(ValueParams P)
     __shared__ uint8_t digits[kSweptThreads][kDecBuf];
     allow_next_grid();
     wait_previous_grid();
-    if (*P.n_long <= P.long_cap) return;                      // the list held every entry
+    if (P.counters[0] <= P.long_cap && P.counters[1] <= P.short_cap) return;   // the lists held every entry
     const uint64_t n = (uint64_t)P.S + 1;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         if (P.type[i] != kValDeferred) continue;
@@ -797,16 +923,29 @@ __global__ void __launch_bounds__(kSweptThreads) decode_swept(ValueParams P)
     }
 }
 
-// type counts
+// type counts: four slots a word, a count per type in registers, summed by
+// warp, block and grid
 __global__ void __launch_bounds__(kValThreads) count_types(ValueParams P)
 {
     __shared__ unsigned long long c[kValTypes];
     if (threadIdx.x < kValTypes) c[threadIdx.x] = 0;
     wait_previous_grid();
     __syncthreads();
-    const uint64_t n = (uint64_t)P.S + 1;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-        atomicAdd(&c[min((uint32_t)P.type[i], (uint32_t)kValTypes - 1u)], 1ull);
+    const uint64_t n = (uint64_t)P.S + 1, words = (n + 3) / 4;
+    uint32_t k[kValTypes] = {};
+    const uint32_t* tw = reinterpret_cast<const uint32_t*>(P.type);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < words; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t w = __ldg(tw + i);
+        const uint64_t left = n - 4 * i;
+        const uint32_t live = left >= 4 ? 0x01010101u : (0x01010101u >> (8 * (4 - (uint32_t)left)));
+#pragma unroll
+        for (int t = 0; t < kValTypes; t++) k[t] += __popc(__vcmpeq4(w, 0x01010101u * (uint32_t)t) & live);
+    }
+#pragma unroll
+    for (int t = 0; t < kValTypes; t++) {
+        const uint32_t v = __reduce_add_sync(FULL_MASK, k[t]);
+        if ((threadIdx.x & 31) == 0 && v) atomicAdd(&c[t], (unsigned long long)v);
+    }
     __syncthreads();
     if (threadIdx.x < kValTypes && c[threadIdx.x]) atomicAdd(P.counts + threadIdx.x, c[threadIdx.x]);
 }

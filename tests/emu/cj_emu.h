@@ -30,7 +30,7 @@
 #define __noinline__
 #define __shared__ static
 #define __launch_bounds__(...)
-#define __align__(n) alignas(n)
+#define __align__(n) __attribute__((aligned(n)))
 
 struct dim3 {
     unsigned x, y, z;
@@ -232,6 +232,20 @@ template <class T> inline T __shfl_xor_sync(unsigned, T v, int m, int = 32)
 inline unsigned __ballot_sync(unsigned, int p) { return (unsigned)cj_emu::collective(cj_emu::kBallot, p != 0, 0); }
 inline int __any_sync(unsigned, int p) { return (int)cj_emu::collective(cj_emu::kAny, p != 0, 0); }
 inline int __all_sync(unsigned, int p) { return (int)cj_emu::collective(cj_emu::kAll, p != 0, 0); }
+inline unsigned __vcmpltu4(unsigned a, unsigned b)
+{
+    unsigned r = 0;
+    for (int i = 0; i < 4; i++)
+        if (((a >> (8 * i)) & 0xFFu) < ((b >> (8 * i)) & 0xFFu)) r |= 0xFFu << (8 * i);
+    return r;
+}
+inline unsigned __vcmpeq4(unsigned a, unsigned b)
+{
+    unsigned r = 0;
+    for (int i = 0; i < 4; i++)
+        if (((a >> (8 * i)) & 0xFFu) == ((b >> (8 * i)) & 0xFFu)) r |= 0xFFu << (8 * i);
+    return r;
+}
 inline unsigned __reduce_add_sync(unsigned, unsigned v) { return (unsigned)cj_emu::collective(cj_emu::kRedAdd, v, 0); }
 inline unsigned __reduce_or_sync(unsigned, unsigned v) { return (unsigned)cj_emu::collective(cj_emu::kRedOr, v, 0); }
 inline unsigned __match_any_sync(unsigned, unsigned v) { return (unsigned)cj_emu::collective(cj_emu::kMatch, v, 0); }
@@ -243,6 +257,12 @@ inline unsigned __reduce_max_sync(unsigned, unsigned v) { return (unsigned)cj_em
 inline int __popc(uint32_t x) { return __builtin_popcount(x); }
 inline int __clz(int x) { return x == 0 ? 32 : __builtin_clz((uint32_t)x); }
 inline int __ffs(int x) { return x == 0 ? 0 : __builtin_ctz((uint32_t)x) + 1; }
+inline unsigned __funnelshift_r(unsigned lo, unsigned hi, unsigned sh)
+{
+    return (unsigned)((((unsigned long long)hi << 32) | lo) >> (sh & 31u));
+}
+inline int __popcll(unsigned long long x) { return __builtin_popcountll(x); }
+inline int __ffsll(long long x) { return x == 0 ? 0 : __builtin_ctzll((unsigned long long)x) + 1; }
 inline int __clzll(long long x) { return x == 0 ? 64 : __builtin_clzll((unsigned long long)x); }
 inline unsigned long long __umul64hi(unsigned long long a, unsigned long long b) {
     return (unsigned long long)(((unsigned __int128)a * b) >> 64);

@@ -219,14 +219,16 @@ int run(const uint8_t* data, const size_t* sizes, size_t n, bool lines, bool bat
         vp.pos = pos;
         vp.S = (uint32_t)S;
         vp.n_bytes = total;
-        vp.type = galloc<uint8_t>(slots);
+        vp.type = galloc<uint8_t>(slots + 4);
         vp.num = galloc<uint64_t>(slots);
         vp.len = galloc<uint32_t>(slots);
         vp.str_out = galloc<uint8_t>(total + 1);
-        const uint64_t long_cap = total / 256 + 1;
-        vp.long_list = galloc<uint32_t>(long_cap + 1);
+        const uint64_t long_cap = total / 256 + 1, short_cap = total / 64 + 1;
+        vp.long_list = galloc<uint32_t>(long_cap + short_cap + 3);
         vp.long_cap = (uint32_t)long_cap;
-        vp.n_long = vp.long_list + long_cap;
+        vp.short_list = vp.long_list + long_cap;
+        vp.short_cap = (uint32_t)short_cap;
+        vp.counters = vp.long_list + long_cap + short_cap;
         vp.counts = galloc<unsigned long long>(kValTypes);
         uint64_t* pow5 = galloc<uint64_t>(2 * 651);
         std::copy(kPow5Table, kPow5Table + 2 * 651, pow5);

@@ -183,7 +183,7 @@ def long_strings_doc(seed: int, n: int) -> bytes:
               "\\u0041", "\\u00e9", "\\u20AC", "\\uffff", "\\ud83d\\ude00", "\\uD800\\uDFFF",
               "\u00e9", "\u20ac", "\U0001f600", "\\\\\\\\", "\\\\u0041", " "]
     faults = ["\\ud800", "\\udc00", "\\ude00\\ud83d", "\\x", "\\u12G4", "\\u12", "\x01",
-              "\\ud83d\\u0041", "\\ud83dx"]
+              "\\ud83d\\u0041", "\\ud83dx", "\\\x01", "\\\x1f", "\\ "]
     out = []
     for k in range(n):
         parts, size = [], rng.randint(300, 3000)
@@ -251,9 +251,18 @@ def test_deferred_list_overflow(emu):
     are found by the sweep."""
     d = ("[" + ",".join(f"{k % 97 + 1}e-{310 + k % 13}" for k in range(6000)) + "]").encode()
     pos, t, nums, lens, strs, counts = emu_values(emu, d)
-    assert len(t) // 7 > len(d) // 256
+    assert 6000 > len(d) // 64 + 1                 # the short list's capacity
     check_values(d, pos, t, nums, lens, strs)
     assert counts[DOUBLE] == 6000
+
+
+def test_escaped_strings_past_the_list(emu):
+    """More escaped strings than the deferred list holds: the rest are
+    decoded where they are."""
+    d = ("[" + ",".join(f'"a\\n{k}\\u00e9"' for k in range(20000)) + "]").encode()
+    pos, t, nums, lens, strs, counts = emu_values(emu, d)
+    assert counts[STRING] > len(d) // 64 + 1       # the short list's capacity
+    check_values(d, pos, t, nums, lens, strs)
 
 
 def test_generated_documents(emu):
