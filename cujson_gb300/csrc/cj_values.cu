@@ -332,13 +332,24 @@ __device__ int64_t decode_string_warp(const uint8_t* __restrict__ src, uint64_t 
     uint32_t carry = 0;           // escaped-state at the step's first byte
     uint32_t prev8 = 0;           // that state 8 bytes before lane 0's first byte
     uint64_t done = 0;            // bytes written
+    // the staged bytes of a step, loaded one step ahead
+    constexpr int kPer = (kStage + 31) / 32;
+    uint32_t nx[kPer];
+    auto load_step = [&](uint64_t c) {
+#pragma unroll
+        for (int r = 0; r < kPer; r++) {
+            const int64_t q = (int64_t)c - kWinBefore + lane + 32 * r;
+            nx[r] = (q >= 0 && (uint64_t)q < len && lane + 32 * r < kStage) ? __ldg(src + q) : 0u;
+        }
+    };
+    load_step(0);
     for (uint64_t c0 = 0; c0 < len; c0 += kWarpStep) {
         __syncwarp();
-        for (int k = lane; k < kStage; k += 32) {
-            const int64_t q = (int64_t)c0 - kWinBefore + k;
-            stage[k] = (q >= 0 && (uint64_t)q < len) ? __ldg(src + q) : (uint8_t)0;
-        }
+#pragma unroll
+        for (int r = 0; r < kPer; r++)
+            if (lane + 32 * r < kStage) stage[lane + 32 * r] = (uint8_t)nx[r];
         __syncwarp();
+        if (c0 + kWarpStep < len) load_step(c0 + kWarpStep);
         // masks of the window's 36 bytes: backslashes, u, quotes, control bytes
         uint64_t B = 0, U = 0, Q = 0, C = 0;
 #pragma unroll
