@@ -296,6 +296,78 @@ def _gpu_values(cj, ctx, data: bytes, lines=False):
     return types, lens
 
 
+def _random_string(rng) -> str:
+    n = rng.choice([0, 1, 3, 10, 40, 200, 300, 700, 2000])
+    plain = [c for c in map(chr, range(0x20, 0x7F)) if c not in '"\\']
+    out = []
+    while len(out) < n:
+        k = rng.random()
+        if k < 0.5:
+            out.append(rng.choice(plain))
+        elif k < 0.6:
+            out.append(chr(rng.randint(0xA0, 0xD7FF)))
+        elif k < 0.65:
+            out.append(chr(rng.randint(0x10000, 0x10FFFF)))
+        elif k < 0.8:
+            out.append(rng.choice(['\\"', "\\\\", "\\/", "\\b", "\\f", "\\n", "\\r", "\\t"]))
+        elif k < 0.9:
+            out.append("\\u%04x" % rng.choice([rng.randint(0, 0xD7FF), rng.randint(0xE000, 0xFFFF)]))
+        elif k < 0.95:
+            cp = rng.randint(0x10000, 0x10FFFF) - 0x10000
+            out.append("\\u%04X\\u%04x" % (0xD800 + (cp >> 10), 0xDC00 + (cp & 0x3FF)))
+        else:
+            out.append("\\\\" * rng.randint(1, 50))
+    return '"' + "".join(out) + '"'
+
+
+def _random_number(rng) -> str:
+    k = rng.random()
+    if k < 0.3:
+        return str(rng.randint(-10 ** rng.randint(1, 25), 10 ** rng.randint(1, 25)))
+    if k < 0.6:
+        return repr(rng.uniform(-1, 1) * 10 ** rng.randint(-320, 308))
+    if k < 0.8:
+        d = "".join(rng.choice("0123456789") for _ in range(rng.randint(1, 60))).lstrip("0") or "0"
+        return (rng.choice(["", "-"]) + d[0] + ("." + d[1:] if len(d) > 1 else "") + "e"
+                + str(rng.randint(-400, 400)))
+    return rng.choice(["0", "-0", "0.0", "1e-324", "2.4703282292062328e-324", "1.7976931348623157e308", "1e309"])
+
+
+def _random_value(rng, depth: int) -> str:
+    k = rng.random()
+    if depth < 4 and k < 0.15:
+        return "[" + ", ".join(_random_value(rng, depth + 1) for _ in range(rng.randint(0, 6))) + "]"
+    if depth < 4 and k < 0.3:
+        return "{" + ", ".join(_random_string(rng) + ": " + _random_value(rng, depth + 1)
+                               for _ in range(rng.randint(0, 6))) + "}"
+    if k < 0.6:
+        return _random_string(rng)
+    if k < 0.9:
+        return _random_number(rng)
+    return rng.choice(["true", "false", "null"])
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_random_documents(emu, seed):
+    """Random documents: strings of every escape and of 0-2000 bytes,
+    numbers of up to 60 digits and any exponent, nesting, and sometimes a
+    long whitespace tail; standard JSON, then the same values as JSON Lines
+    in chunks cut at line ends."""
+    rng = random.Random(seed)
+    doc = ("[" + ", ".join(_random_value(rng, 0) for _ in range(rng.randint(1, 150))) + "]"
+           + " " * rng.choice([0, 1, 5000])).encode()
+    pos, t, nums, lens, strs, counts = emu_values(emu, doc)
+    check_values(doc, pos, t, nums, lens, strs)
+    lines = [("{" + ", ".join(_random_string(rng) + ": " + _random_value(rng, 1)
+                              for _ in range(rng.randint(1, 8))) + "}").encode() for _ in range(rng.randint(2, 40))]
+    data = b"\n".join(lines) + b"\n"
+    ends = np.cumsum([len(x) + 1 for x in lines])
+    cuts = sorted(rng.sample(range(1, len(lines)), min(3, len(lines) - 1)))
+    sizes = np.diff(np.concatenate([[0], ends[np.array(cuts) - 1], [len(data)]])).tolist()
+    pos, t, nums, lens, strs, counts = emu_values(emu, data, lines=True, chunks=sizes)
+    check_values(data, pos, t, nums, lens, strs)
+
+
 @pytest.mark.gpu
 def test_gpu_values(cj, ctx):
     _gpu_values(cj, ctx, STRING_DOC)
