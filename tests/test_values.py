@@ -388,3 +388,16 @@ def test_gpu_values_long_strings(cj, ctx):
                              huge_string_min=64 << 10, huge_string_max=128 << 10).tobytes()
     types, lens = _gpu_values(cj, ctx, d)
     assert int(lens.max()) > 32 << 10
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", range(4))
+def test_gpu_random_documents(cj, ctx, seed):
+    rng = random.Random(100 + seed)
+    doc = ("[" + ", ".join(_random_value(rng, 0) for _ in range(rng.randint(100, 400))) + "]"
+           + " " * rng.choice([0, 5000])).encode()
+    _gpu_values(cj, ctx, doc)
+    lines = b"\n".join(("{" + ", ".join(_random_string(rng) + ": " + _random_value(rng, 1)
+                                         for _ in range(rng.randint(1, 8))) + "}").encode()
+                        for _ in range(rng.randint(50, 200))) + b"\n"
+    _gpu_values(cj, ctx, lines, lines=True)
