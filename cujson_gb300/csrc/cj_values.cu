@@ -179,20 +179,20 @@ __device__ __forceinline__ uint32_t load4(const uint8_t* p)
 // Returns its length, or -1 when it holds a byte that needs decode_string.
 __device__ int64_t copy_plain(Reader& rd, uint64_t s0, uint64_t e, uint8_t* out)
 {
-    const uint8_t* src = rd.base - rd.lo;                       // logical offset x at src + x
+    const uint8_t* src = rd.base + (s0 - rd.lo);                // logical offset x at src + (x - s0)
     uint64_t x = s0;
     for (; x < e && (x & 3u); x++) {
-        const uint8_t c = __ldg(src + x);
+        const uint8_t c = __ldg(src + (x - s0));
         if (c == '\\' || c == '"' || c < 0x20u) return -1;
         out[x] = c;
     }
     for (; x + 4 <= e; x += 4) {
-        const uint32_t v = load4(src + x);
+        const uint32_t v = load4(src + (x - s0));
         if (__vcmpeq4(v, 0x5C5C5C5Cu) | __vcmpeq4(v, 0x22222222u) | __vcmpltu4(v, 0x20202020u)) return -1;
         *reinterpret_cast<uint32_t*>(out + x) = v;
     }
     for (; x < e; x++) {
-        const uint8_t c = __ldg(src + x);
+        const uint8_t c = __ldg(src + (x - s0));
         if (c == '\\' || c == '"' || c < 0x20u) return -1;
         out[x] = c;
     }
