@@ -515,7 +515,8 @@ class Context:
     def timing(self, enable: int = 1) -> None:
         """cj_context_timing: 0 off; 1 (True) an event at every kernel
         boundary; 2 events at the run's start, the scan's end and the run's
-        end only, so the kernels overlap their launches as untimed runs do."""
+        end only, so the scan's kernels overlap their launches as untimed runs
+        do; 3 events at the run's start and end only."""
         _check(lib().cj_context_timing(self._h, int(enable)), "timing")
 
     def phase_ms(self):

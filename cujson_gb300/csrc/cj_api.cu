@@ -177,7 +177,8 @@ struct cj_context {
     int64_t launches = 0;
     size_t dev_bytes = 0;
 
-    int timing = 0;                     // 0 off, 1 an event at every kernel boundary, 2 scan and run ends
+    int timing = 0;                     // 0 off, 1 an event at every kernel boundary, 2 scan and run ends,
+                                        // 3 run ends only
     std::vector<cudaEvent_t> events;   // kEventsPerRun per recorded run
     size_t events_used = 0;
 
@@ -521,7 +522,7 @@ cj_status enqueue(cj_context* ctx, bool graph)
         launch_scan(sp, ctx->lines, shape, ctx->stream, fine ? ev + 1 : nullptr);
         ctx->launches += scan_launches(ctx->n_regions);
     }
-    if (ev && !fine) {
+    if (ev && ctx->timing == 2) {
         // coarse timing: no events between the scan's kernels, which would
         // keep each from being scheduled while the one before it finishes
         for (int k = 1; k <= 3; k++) CJ_CUDA(cudaEventRecord(ev[k], ctx->stream));
@@ -560,6 +561,9 @@ cj_status enqueue(cj_context* ctx, bool graph)
     launch_pair(pp, grid, ctx->stream, (int)pthreads);
     if (fine) CJ_CUDA(cudaEventRecord(ev[4], ctx->stream));
     launch_spine(pp, grid, ctx->stream, (int)pthreads);
+    // timing 3 (the run's ends only): the scan's events at the run's end
+    if (ev && ctx->timing == 3)
+        for (int k = 1; k <= 3; k++) CJ_CUDA(cudaEventRecord(ev[k], ctx->stream));
     if (ev && !fine) CJ_CUDA(cudaEventRecord(ev[4], ctx->stream));
     if (ev) CJ_CUDA(cudaEventRecord(ev[5], ctx->stream));
     ctx->launches += 2;
@@ -1321,7 +1325,7 @@ void cj_context_destroy(cj_context* ctx)
 cj_status cj_context_timing(cj_context* ctx, int enable)
 {
     if (!ctx) return CJ_ERR_INVALID_ARGUMENT;
-    ctx->timing = enable < 0 ? 0 : (enable > 2 ? 1 : enable);
+    ctx->timing = enable < 0 ? 0 : (enable > 3 ? 1 : enable);
     ctx->events_used = 0;
     return CJ_OK;
 }

@@ -341,8 +341,10 @@ cj_status cj_server_replay(cj_server* s, const uint8_t* const* docs, const size_
  * (re-)enabled.  enable = 1: an event at every kernel boundary (each phase
  * timed, but a kernel then cannot be scheduled while the one before it
  * finishes); enable = 2: events only at the run's start, the scan's end and
- * the run's end -- the scan and the whole run timed as they run untimed;
- * pair_ms is then pair + spine and the scan's split reads as all tables. */
+ * the run's end -- the scan timed as it runs untimed; pair_ms is then pair +
+ * spine and the scan's split reads as all tables; enable = 3: events only at
+ * the run's start and end -- the whole run timed as it runs untimed (scan_ms
+ * then covers the whole run). */
 cj_status cj_context_timing(cj_context* ctx, int enable);
 cj_status cj_context_phase_ms(cj_context* ctx, double* scan_ms, double* pair_ms,
                               double* spine_ms, int64_t* runs);

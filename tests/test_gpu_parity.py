@@ -145,11 +145,12 @@ def test_repeat_deterministic(cj, ctx):
         assert np.array_equal(ctx.parse_standard_json(d).buffer, first)
 
 
-@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("mode", [1, 2, 3])
 def test_timed_runs_same_result(cj, ctx, oracle, mode):
-    """Runs with events at every kernel boundary (1) or at the scan's and the
-    run's ends only (2, the kernels launched to overlap) give the oracle's
-    result; the phases add up to the span."""
+    """Runs with events at every kernel boundary (1), at the scan's and the
+    run's ends only (2) or at the run's ends only (3) -- the kernels launched
+    to overlap in 2 and 3 -- give the oracle's result; the phases add up to
+    the span."""
     d = synth.synth_document(321, 24 << 20, max_depth=12)
     ref = oracle.parse(d)
     ctx.stage_standard(d)
@@ -160,9 +161,10 @@ def test_timed_runs_same_result(cj, ctx, oracle, mode):
     tables, prefix, emit, _ = ctx.scan_phase_ms()
     span = ctx.span_ms()
     ctx.timing(0)
-    assert runs == 4 and scan > 0 and pair > 0 and span >= scan + pair + spine - 1e-3
+    assert runs == 4 and scan > 0 and span >= scan + pair + spine - 1e-3
+    assert pair > 0 if mode != 3 else pair < 0.02
     assert abs(tables + prefix + emit - scan) < 0.01
-    if mode == 2:                           # back-to-back events: next to nothing between them
+    if mode >= 2:                           # back-to-back events: next to nothing between them
         assert spine < 0.02 and prefix < 0.02 and emit < 0.02
     assert_same(ctx.staged_result(), ref)
 
