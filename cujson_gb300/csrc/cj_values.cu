@@ -33,10 +33,15 @@
 // to even; 800 digits are held, more only set a sticky flag, and the
 // exact halfway points of doubles need at most 767.
 //
-//   decode_deferred  the list (long strings and deferred numbers), with a
-//                    digit buffer per thread in shared memory;
-//   decode_swept     only when the list overflowed: the deferred numbers it
-//                    did not hold, found by a pass over the types.
+//   decode_deferred  a warp per listed slot: the long list (slots longer than
+//                    kShortBytes) a warp each in turn, then the short list
+//                    (escaped strings, numbers for the exact conversion) from
+//                    a ticket; whitespace trimmed and strings decoded by the
+//                    whole warp, numbers by one lane with a digit buffer per
+//                    warp in shared memory;
+//   decode_swept     only when the short list overflowed: the deferred
+//                    numbers it did not hold, found by a pass over the types;
+//   count_types      the totals per type.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -48,7 +53,7 @@ namespace cj {
 
 namespace {
 
-constexpr uint32_t kShortBytes = 256;     // longer strings go to the second kernel
+constexpr uint32_t kShortBytes = 256;     // longer slots go to the second kernel
 constexpr uint32_t FULL_MASK = 0xFFFFFFFFu;
 constexpr int kValThreads = 256;
 
