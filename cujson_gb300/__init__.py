@@ -151,6 +151,7 @@ _SIGNATURES = {
     "cj_staged_device_outputs": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p),
                                                 ctypes.POINTER(ctypes.c_void_p)]),
     "cj_context_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "cj_context_set_dependent_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "cj_context_phase_ms": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
                                            ctypes.POINTER(ctypes.c_double),
                                            ctypes.POINTER(ctypes.c_double),
@@ -511,6 +512,11 @@ class Context:
         _check(lib().cj_autotune_staged(self._h, reps, ctypes.byref(best), tried, len(tried), ctypes.byref(n)),
                "autotune")
         return best, [tried[i] for i in range(min(n.value, len(tried)))]
+
+    def set_dependent_launch(self, enable: bool) -> None:
+        """cj_context_set_dependent_launch: whether the kernels after the first
+        of a run are scheduled while the one before finishes (default on)."""
+        _check(lib().cj_context_set_dependent_launch(self._h, int(bool(enable))), "set_dependent_launch")
 
     def timing(self, enable: int = 1) -> None:
         """cj_context_timing: 0 off; 1 (True) an event at every kernel

@@ -177,6 +177,7 @@ struct cj_context {
     int64_t launches = 0;
     size_t dev_bytes = 0;
 
+    bool dependent_launch = true;       // the kernels after the first of a run are dependent launches
     int timing = 0;                     // 0 off, 1 an event at every kernel boundary, 2 scan and run ends,
                                         // 3 run ends only
     std::vector<cudaEvent_t> events;   // kEventsPerRun per recorded run
@@ -497,6 +498,7 @@ cj_status enqueue(cj_context* ctx, bool graph)
     sp.region_steps = ctx->run_region_steps;
     sp.sm_count = ctx->sm_count;
     sp.prefetch_steps = ctx->tune_prefetch_steps;
+    sp.dependent_launch = ctx->dependent_launch ? 1u : 0u;
     ScanShape shape{ctx->tune_tables_per_sm, ctx->tune_emit_per_sm};
     if (ctx->n_waves > 1) {
         // waves: each scans its regions from the previous wave's end value,
@@ -529,11 +531,12 @@ cj_status enqueue(cj_context* ctx, bool graph)
     }
     if (ctx->batch) {
         launch_batch_prefix(ctx->segs.p, ctx->seg_out.p, ctx->n_segs, ctx->layout_off.p, ctx->rchunk_off.p,
-                            ctx->stream);
+                            ctx->stream, ctx->dependent_launch);
         ctx->launches += 1;
     }
 
     PairParams pp{};
+    pp.dependent_launch = ctx->dependent_launch ? 1u : 0u;
     pp.brk = ctx->brk.p;
     pp.pair = ctx->pair.p;
     pp.spine = ctx->spine.p;
@@ -569,7 +572,7 @@ cj_status enqueue(cj_context* ctx, bool graph)
     ctx->launches += 2;
     if (ctx->batch) {
         launch_batch_layout(ctx->segs.p, ctx->seg_out.p, ctx->n_segs, ctx->pos.p, ctx->pair.p,
-                            ctx->layout_off.p, ctx->layout.p, ctx->sm_count, ctx->stream);
+                            ctx->layout_off.p, ctx->layout.p, ctx->sm_count, ctx->stream, ctx->dependent_launch);
         ctx->launches += 1;
         ctx->batch_read = false;
     }
@@ -1322,6 +1325,14 @@ void cj_context_destroy(cj_context* ctx)
     delete ctx;
 }
 
+cj_status cj_context_set_dependent_launch(cj_context* ctx, int enable)
+{
+    if (!ctx) return CJ_ERR_INVALID_ARGUMENT;
+    ctx->dependent_launch = enable != 0;
+    ctx->graph_valid = false;           // a captured graph holds the old launches
+    return CJ_OK;
+}
+
 cj_status cj_context_timing(cj_context* ctx, int enable)
 {
     if (!ctx) return CJ_ERR_INVALID_ARGUMENT;
@@ -1816,6 +1827,7 @@ cj_status cj_decode_values(cj_context* ctx, cj_value_counts* counts)
         CJ_CUDA(cudaMemcpy(ctx->pow5.p, kPow5Table, sizeof(kPow5Table), cudaMemcpyHostToDevice));
     }
     ValueParams vp{};
+    vp.dependent_launch = ctx->dependent_launch ? 1u : 0u;
     vp.in = ctx->in.p;
     vp.segs = ctx->segs.p;
     vp.n_segs = ctx->n_segs;

@@ -220,16 +220,16 @@ void launch_batch_scatter(const uint8_t* packed, const uint64_t* src_off, const 
 }
 
 void launch_batch_prefix(const Segment* segs, const SegmentOut* seg_out, uint32_t n, uint64_t* layout_off,
-                         uint64_t* rchunk_off, cudaStream_t stream)
+                         uint64_t* rchunk_off, cudaStream_t stream, bool dep)
 {
-    launch_dependent(batch_prefix, 1, 1024, 0, stream, segs, seg_out, n, layout_off, rchunk_off);
+    launch_dependent(batch_prefix, 1, 1024, 0, stream, dep, segs, seg_out, n, layout_off, rchunk_off);
 }
 
 void launch_batch_layout(const Segment* segs, const SegmentOut* seg_out, uint32_t n, const int32_t* pos,
                          const int32_t* pair, const uint64_t* off, int32_t* layout, int sm_count,
-                         cudaStream_t stream)
+                         cudaStream_t stream, bool dep)
 {
-    launch_dependent(batch_layout, sm_count * 8, 256, 0, stream, segs, seg_out, n, pos, pair, off, layout);
+    launch_dependent(batch_layout, sm_count * 8, 256, 0, stream, dep, segs, seg_out, n, pos, pair, off, layout);
 }
 
 }  // namespace cj

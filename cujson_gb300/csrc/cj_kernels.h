@@ -31,9 +31,12 @@ __device__ __forceinline__ void allow_next_grid()
 // turns it off, for comparison)
 bool dependent_launch_enabled();
 #ifndef CJ_EMU
+// (dep false: a plain launch -- for a context whose stream shares the GPU with
+// others, where a dependent kernel waiting on its SMs would hold resources
+// another stream's kernels could use)
 template <typename... Params, typename... Args>
 inline cudaError_t launch_dependent(void (*kernel)(Params...), int grid, int block, size_t smem,
-                                    cudaStream_t stream, Args... args)
+                                    cudaStream_t stream, bool dep, Args... args)
 {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
@@ -44,7 +47,7 @@ inline cudaError_t launch_dependent(void (*kernel)(Params...), int grid, int blo
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
-    cfg.numAttrs = dependent_launch_enabled() ? 1 : 0;
+    cfg.numAttrs = (dep && dependent_launch_enabled()) ? 1 : 0;
     return cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 #endif
@@ -78,6 +81,7 @@ struct ScanParams {
     int region_steps;           // 1 KiB steps per region: 4, 8 or 16
     int sm_count;
     uint32_t prefetch_steps;    // the table kernel's L2 prefetch distance in steps (0: 4)
+    uint32_t dependent_launch;  // nonzero: the kernels after the first are dependent launches
     // A wave: the launch scans regions [r_begin, r_end) only (r_end 0: all),
     // starting from the value in carry_in (nullptr: the document start) and
     // leaving the value after r_end - 1 in carry_out (nullptr: not kept);
@@ -131,6 +135,7 @@ struct PairParams {
     uint32_t* seg_err;
     int32_t* seg_depth;
     uint64_t n_chunks;                    // size of the batch's chunk index space
+    uint32_t dependent_launch;            // nonzero: both kernels are dependent launches
 };
 
 // cinfo fill of a batch chunk without records (bytes 0x7F): above every level
@@ -181,6 +186,7 @@ struct ValueParams {
     uint32_t* counters;            // entries wanted in each list, then the short list's ticket
     unsigned long long* counts;    // kValTypes
     const uint64_t* pow5;          // kPow5Table on the device
+    uint32_t dependent_launch;     // nonzero: the kernels after the first are dependent launches
 };
 cudaError_t launch_decode_values(const ValueParams& p, int sm_count, cudaStream_t stream);
 cudaError_t preload_value_kernels();
@@ -216,9 +222,9 @@ void launch_batch_scatter(const uint8_t* packed, const uint64_t* src_off, const 
                           const Segment* segs, uint32_t n, uint64_t total_words, uint8_t* in, int sm_count,
                           cudaStream_t stream);
 void launch_batch_prefix(const Segment* segs, const SegmentOut* seg_out, uint32_t n, uint64_t* layout_off,
-                         uint64_t* rchunk_off, cudaStream_t stream);
+                         uint64_t* rchunk_off, cudaStream_t stream, bool dep);
 void launch_batch_layout(const Segment* segs, const SegmentOut* seg_out, uint32_t n, const int32_t* pos,
                          const int32_t* pair, const uint64_t* off, int32_t* layout, int sm_count,
-                         cudaStream_t stream);
+                         cudaStream_t stream, bool dep);
 
 }  // namespace cj

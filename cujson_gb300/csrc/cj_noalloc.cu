@@ -192,6 +192,7 @@ cj_status parse_noalloc(const uint8_t* d_data, size_t size, int32_t* d_out, size
     noalloc_setup<<<1, 32, 0, stream>>>(s, size);
 
     ScanParams sp{};
+    sp.dependent_launch = 1;
     sp.in = s->in;
     sp.segs = &s->seg;
     sp.region_seg = nullptr;
@@ -213,6 +214,7 @@ cj_status parse_noalloc(const uint8_t* d_data, size_t size, int32_t* d_out, size
     launch_scan(sp, false, ScanShape{0, 0}, stream);
 
     PairParams pp{};
+    pp.dependent_launch = 1;
     pp.brk = s->brk;
     pp.pair = s->pair;
     pp.spine = s->spine;

@@ -403,7 +403,7 @@ void launch_pair(const PairParams& p, int grid, cudaStream_t stream, int threads
     (void)stream;
     cj_emu::launch(grid, threads, smem, [&] { pair_chunks(p); });
 #else
-    launch_dependent(pair_chunks, grid, threads, smem, stream, p);
+    launch_dependent(pair_chunks, grid, threads, smem, stream, p.dependent_launch != 0, p);
 #endif
 }
 
@@ -413,7 +413,7 @@ void launch_spine(const PairParams& p, int grid, cudaStream_t stream, int thread
     (void)stream;
     cj_emu::launch(grid, threads, 0, [&] { pair_spine(p); });
 #else
-    launch_dependent(pair_spine, grid, threads, 0, stream, p);
+    launch_dependent(pair_spine, grid, threads, 0, stream, p.dependent_launch != 0, p);
 #endif
 }
 

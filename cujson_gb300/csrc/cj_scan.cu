@@ -965,10 +965,11 @@ void launch_r(const ScanParams& p, bool lines, int tables_grid, int emit_grid, c
     if (lines) scan_tables<true, R><<<tables_grid, kThreads, 0, stream>>>(p);
     else scan_tables<false, R><<<tables_grid, kThreads, 0, stream>>>(p);
     if (ev) cudaEventRecord(ev[0], stream);
-    if (nb > 1) launch_dependent(prefix_reduce, (int)nb, kPrefixPerBlock, 0, stream, p);
-    launch_dependent(prefix_apply, (int)nb, kPrefixPerBlock, 0, stream, p);
+    const bool dep = p.dependent_launch != 0;
+    if (nb > 1) launch_dependent(prefix_reduce, (int)nb, kPrefixPerBlock, 0, stream, dep, p);
+    launch_dependent(prefix_apply, (int)nb, kPrefixPerBlock, 0, stream, dep, p);
     if (ev) cudaEventRecord(ev[1], stream);
-    launch_dependent(scan_emit<R>, emit_grid, kThreads, 0, stream, p);
+    launch_dependent(scan_emit<R>, emit_grid, kThreads, 0, stream, dep, p);
     if (ev) cudaEventRecord(ev[2], stream);
 #endif
 }

@@ -244,6 +244,9 @@ cj_status cj_server_create(const cj_server_config* cfg, cj_server** out)
     s->slots.resize(s->cfg.slots);
     for (Slot& sl : s->slots) {
         cj_status st = cj_context_create(s->cfg.device, &sl.ctx);
+        // the slots' streams share the GPU: a dependent kernel of one slot
+        // waiting on its SMs would hold resources the other slot's kernels need
+        if (!st) st = cj_context_set_dependent_launch(sl.ctx, 0);
         if (!st && cudaEventCreateWithFlags(&sl.done_ev, cudaEventDisableTiming) != cudaSuccess) st = CJ_ERR_CUDA;
         if (st) {
             cj_server_destroy(s);

@@ -981,9 +981,10 @@ cudaError_t launch_decode_values(const ValueParams& p, int sm_count, cudaStream_
     return cudaSuccess;
 #else
     decode_slots<<<grid, kValThreads, 0, stream>>>(p);
-    launch_dependent(decode_deferred, sm_count * 16, kDeferredThreads, 0, stream, p);
-    launch_dependent(decode_swept, sm_count * 8, kSweptThreads, 0, stream, p);
-    launch_dependent(count_types, grid, kValThreads, 0, stream, p);
+    const bool dep = p.dependent_launch != 0;
+    launch_dependent(decode_deferred, sm_count * 16, kDeferredThreads, 0, stream, dep, p);
+    launch_dependent(decode_swept, sm_count * 8, kSweptThreads, 0, stream, dep, p);
+    launch_dependent(count_types, grid, kValThreads, 0, stream, dep, p);
     return cudaGetLastError();
 #endif
 }

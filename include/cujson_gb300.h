@@ -346,6 +346,12 @@ cj_status cj_server_replay(cj_server* s, const uint8_t* const* docs, const size_
  * the run's start and end -- the whole run timed as it runs untimed (scan_ms
  * then covers the whole run). */
 cj_status cj_context_timing(cj_context* ctx, int enable);
+/* Dependent launches (default on): each kernel of a run after the first may
+ * be scheduled while the one before it finishes, and waits on the device for
+ * its results.  Its blocks then hold SM resources while they wait, which a
+ * kernel of another stream sharing the GPU could have used; a context whose
+ * stream shares the GPU with others' (the server's slots) may turn them off. */
+cj_status cj_context_set_dependent_launch(cj_context* ctx, int enable);
 cj_status cj_context_phase_ms(cj_context* ctx, double* scan_ms, double* pair_ms,
                               double* spine_ms, int64_t* runs);
 /* The scan's own split over the same runs: its table kernel (one read of the

@@ -169,6 +169,21 @@ def test_timed_runs_same_result(cj, ctx, oracle, mode):
     assert_same(ctx.staged_result(), ref)
 
 
+def test_plain_launches_same_result(cj, ctx, oracle):
+    """With the dependent launches off (as the server's slots run) the runs
+    give the same results."""
+    d = synth.synth_document(322, 8 << 20, max_depth=12)
+    ref = oracle.parse(d)
+    ctx.set_dependent_launch(False)
+    try:
+        ctx.stage_standard(d)
+        ctx.run()
+        assert_same(ctx.staged_result(), ref)
+        assert_same(ctx.parse_standard_json(d), ref)
+    finally:
+        ctx.set_dependent_launch(True)
+
+
 def test_staged_and_into(cj, ctx, oracle):
     d = synth.synth_document(123, 1 << 20)
     ref = oracle.parse(d)
